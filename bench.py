@@ -1,0 +1,313 @@
+"""Benchmark of the radiance pass on GB300: probe-rays/s on the demo-scale plain workload.
+
+Workload (one "step"): the 64x64x16-block terrain world plus 2000 random blocks of 32 types,
+8 successive passes (multi-bounce, each reading the previous pass's volume), each over a seeded
+10% subset of the probes, 256 rays per probe, max_dist 256, blend 0.1, FP32 radiance.
+
+  value      probe-rays/s with every input resident in HBM (request lists uploaded once);
+             CUDA events on the pass stream around each step; L2 flushed (256 MiB write)
+             between steps, outside the timed region.
+  e2e        the same metric through the C ABI with host buffers: each pass copies its request
+             list host->device, each step reads the radiance volume back.
+  roofline   algorithmic bytes of the pass kernel per launch (3 B per grid+palette lookup,
+             16+8*12 B per hit, 8+2*12 B per probe; counts exact from the kernel's counters)
+             over the kernel's own event-timed duration, against the measured HBM copy peak.
+  cpu_baseline  the CPU oracle (OpenMP, all host cores) on a bounded sample of pass 0.
+
+--impl reference times the CPU implementation of the same workload on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from lum_gb300 import worldgen  # noqa: E402
+
+WORKLOAD = {
+    "workload": "plain radiance update, demo scale: 64x64x16 blocks + 2000 random blocks, "
+                "32 block types, 8 passes x 10% probes, 256 rays/probe, max_dist 256, FP32",
+    "world_blocks": [64, 64, 16], "extra_blocks": 2000, "block_types": 32, "passes_per_step": 8,
+    "probe_fraction": 0.1, "rays_per_probe": 256, "max_dist": 256.0, "blend": 0.1, "seed": 1234,
+}
+PASSES = 8
+RAYS = 256
+MAX_DIST = 256.0
+BLEND = 0.1
+SEED = 1234
+S_R = 12            # bytes of FP32 RGB radiance per probe
+
+
+def pass_lists(dims):
+    return [worldgen.probe_subset(dims, 0.1, seed=SEED, stream=p) for p in range(PASSES)]
+
+
+def algorithmic_bytes(steps: int, hits: int, probes: int) -> int:
+    return 3 * steps + hits * (16 + 8 * S_R) + probes * (8 + 2 * S_R)
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(world, lists, budget_s: float = 12.0):
+    """The CPU oracle (OpenMP over probes, all host cores) on a bounded prefix of pass 0."""
+    import oracle
+    req = lists[0]
+    cores = oracle.max_threads()
+    n = min(64, req.shape[0])
+    t0 = time.perf_counter()
+    oracle.radiance_pass(world, req[:n], rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=0)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    n = int(min(req.shape[0], max(n, n * budget_s / dt)))
+    t0 = time.perf_counter()
+    oracle.radiance_pass(world, req[:n], rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=0)
+    dt = time.perf_counter() - t0
+    return {"value": n * RAYS / dt, "unit": "probe-rays/s", "cores": cores, "kind": "port",
+            "sample": f"first {n} probes of pass 0 ({n * RAYS} rays), one pass, {dt:.1f} s"}
+
+
+def dist_setup(args):
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world_size > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        pg = dist
+    return rank, local, world_size, pg
+
+
+def run_reference(args, rank, world_size, pg):
+    """CPU implementation of the same workload (the oracle, OpenMP over all host cores)."""
+    if rank != 0:
+        return
+    import oracle
+    world = worldgen.demo_world(SEED)
+    lists = pass_lists(world.dims)
+    cores = oracle.max_threads()
+    n_sample = 192        # probes per pass per step: a bounded sample of each pass
+    prev = np.zeros(world.grid.shape + (3,), dtype=np.float32)
+    t_total = 0.0
+    rays_total = 0
+    for step in range(args.warmup + args.steps):
+        cur = prev
+        t0 = time.perf_counter()
+        for p in range(PASSES):
+            cur, _, _ = oracle.radiance_pass(world, lists[p][:n_sample], rays=RAYS, max_dist=MAX_DIST,
+                                             blend=BLEND, time_seed=p, prev=cur)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            t_total += dt
+            rays_total += PASSES * n_sample * RAYS
+    value = rays_total / t_total
+    line = {"metric": "probe-rays/s", "value": value, "unit": "probe-rays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded terrain world)", "impl": "reference",
+            "config": dict(WORKLOAD, sample=f"first {n_sample} probes of each of the 8 passes per step"),
+            "cpu_baseline": {"value": value, "unit": "probe-rays/s", "cores": cores, "kind": "port",
+                             "sample": f"first {n_sample} probes of each pass, {PASSES} passes per step"},
+            "e2e": {"value": value, "unit": "probe-rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's own implementation is a Vulkan compute shader (unavailable on this box); "
+                    "this arm runs the CPU restatement of it"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    rank, local, world_size, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world_size, pg)
+        return
+
+    import torch
+    import lum_gb300
+
+    torch.cuda.set_device(local)
+    world = worldgen.demo_world(SEED)
+    lists = pass_lists(world.dims)
+    probes_per_step = sum(l.shape[0] for l in lists)
+    rays_per_step = probes_per_step * RAYS
+
+    # ---------------------------------------------------------------- resident (value)
+    rw = lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], device=local)
+    rw.load(world)
+    for p, l in enumerate(lists):
+        rw.upload_requests(p, l)
+    stream = torch.cuda.ExternalStream(rw.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def params(p):
+        return lum_gb300.pass_params(rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=p)
+
+    # exact per-pass counters (identical on every run: the traversal is deterministic)
+    pass_bytes = []
+    pass_steps = []
+    for p in range(PASSES):
+        rw.radiance_pass_resident(p, params(p))
+        st = rw.pass_stats()
+        pass_steps.append(st["steps"])
+        pass_bytes.append(algorithmic_bytes(st["steps"], st["hits"], st["probes"]))
+    for _ in range(args.warmup):
+        for p in range(PASSES):
+            rw.radiance_pass_resident(p, params(p))
+    rw.synchronize()
+
+    step_ms = []
+    kernel_ms = []
+    with ClockSampler(local) as clocks:
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            for p in range(PASSES):
+                rw.radiance_pass_resident(p, params(p))
+            e1.record(stream)
+            kt = rw.kernel_times(PASSES)   # synchronises after the step's passes
+            kernel_ms.extend(kt.tolist())
+            step_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+    total_ms = float(sum(step_ms))
+    if pg:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world_size * args.steps * rays_per_step / (total_ms / 1000.0)
+
+    hbm_peak, peak_kind = load_peaks()
+    bytes_per_launch = float(np.mean(pass_bytes))
+    kern_avg_s = float(np.mean(kernel_ms)) / 1000.0
+    achieved = bytes_per_launch / kern_avg_s / 1e9
+
+    # ---------------------------------------------------------------- end to end (e2e)
+    rw2 = lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], device=local)
+    rw2.load(world)
+    for _ in range(max(1, args.warmup)):
+        for p in range(PASSES):
+            rw2.radiance_pass(lists[p], params(p))
+        rw2.get_radiance()
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for p in range(PASSES):
+            rw2.radiance_pass(lists[p], params(p))
+        rw2.get_radiance()
+        e2e_s += time.perf_counter() - t0
+    e2e_value = world_size * args.steps * rays_per_step / e2e_s
+    h2d = int(sum(l.shape[0] * 8 for l in lists))
+    d2h = int(world.n_blocks * 16)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(world, lists)
+
+    if rank == 0:
+        line = {
+            "metric": "probe-rays/s", "value": value, "unit": "probe-rays/s", "n_gpus": world_size,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded value-noise terrain, splitmix64)",
+            "config": dict(WORKLOAD, l2="flushed between steps (256 MiB write)",
+                           parallelism="replicas" if world_size > 1 else "single GPU"),
+            "e2e": {"value": e2e_value, "unit": "probe-rays/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_launch": bytes_per_launch, "kernel_ms_avg": kern_avg_s * 1e3,
+                         "ray_steps_per_s": float(np.mean(pass_steps)) / kern_avg_s},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": PASSES * args.steps,
+        }
+        print(json.dumps(line))
+    rw.close()
+    rw2.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

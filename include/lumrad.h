@@ -1,0 +1,190 @@
+/*
+ * lumrad.h — C ABI of the GB300 radiance-field update (Lum's per-block radiance pass).
+ *
+ * One context holds one world resident in device memory: the int16 block grid, the 16^3 uint8
+ * block palettes, the 256-entry material table and the radiance volume (one probe per block).
+ * A pass traces R rays per listed probe through the two-level voxel grid and blends the mean
+ * into the probe, exactly as Lum's shaders/radiance.comp does (see "Semantics" below).
+ *
+ * Conventions (modelled on Lum's C99 API, src/renderer/api/crenderer.h:19-114):
+ *   - opaque handles (typedef void*), like `LumRenderer` (crenderer.h:20);
+ *   - every call returns a status: 0 = LUMRAD_OK, negative = error; nothing aborts;
+ *   - the caller owns every array it passes; arrays are copied before the call returns;
+ *   - a context is not thread-safe (Lum's renderer is single-threaded too); different
+ *     contexts may be used from different host threads;
+ *   - grids and radiance volumes are x-fastest: index = x + X*(y + Y*z)
+ *     (table3d, src/renderer/src/internal_render.hpp:136-143).
+ *
+ * Semantics that differ from the Vulkan pass, by design (each one is a definition where the
+ * shader's behaviour is undefined or a data race):
+ *   - out-of-range texel fetches return 0 (robust-access semantics);
+ *   - a pass reads the previous volume and writes a new one (ping-pong): the shader binds the
+ *     same image for read and write (internal_render.cpp:240-241), which races;
+ *   - radiance is stored as FP32 (or FP16/BF16) RGB clamped to [0,1] — the clamp of the
+ *     A2B10G10R10_UNORM image, without its 10-bit quantisation;
+ *   - world size and rays per probe are runtime values (consts.glsl:1, radiance.comp:37);
+ *   - the trilinear radiance fetch uses exact FP32 weights (hardware uses 8-bit weights);
+ *   - the subgroup sum is a fixed xor-butterfly order; the coarse march stops after
+ *     2*max_dist+2 steps, a bound a finite ray never reaches (a NaN fraction would otherwise
+ *     loop forever in the shader).
+ */
+#ifndef LUMRAD_H
+#define LUMRAD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define LUMRAD_OK        0
+#define LUMRAD_EINVAL   -1  /* bad argument (null pointer, size out of range, bad id) */
+#define LUMRAD_ENOMEM   -2  /* device or host allocation failed, or HBM budget exceeded */
+#define LUMRAD_EDEVICE  -3  /* CUDA error; the message is kept by lumrad_last_error() */
+#define LUMRAD_ETIMEOUT -4  /* a bounded wait ran out */
+#define LUMRAD_ESTATE   -5  /* call not valid in the current state (e.g. no hits recorded) */
+
+/* ---- constants (src/renderer/src/internal_types.hpp:13-25) -------------------------------- */
+#define LUMRAD_BLOCK_SIZE          16     /* BLOCK_SIZE */
+#define LUMRAD_MATERIALS           256    /* MATERIAL_PALETTE_SIZE */
+#define LUMRAD_MAX_BLOCK_SLOTS     4096   /* BLOCK_PALETTE_SIZE_X * BLOCK_PALETTE_SIZE_Y */
+#define LUMRAD_SPECIAL_BLOCK       32767  /* SPECIAL_BLOCK */
+
+#define LUMRAD_PRECISION_FP32 0
+#define LUMRAD_PRECISION_FP16 1
+#define LUMRAD_PRECISION_BF16 2
+
+typedef void* LumRadContext;
+
+/* World settings; replaces the radiance-relevant part of LumSettings (crenderer.h:28-39). */
+typedef struct {
+    int world_size[3];      /* blocks per axis, each 1..2047 (LumSettings.world_size) */
+    int max_block_types;    /* palette slots kept on the device, 1..4096
+                               (LumSettings.static_block_palette_size) */
+    int precision;          /* LUMRAD_PRECISION_*: radiance storage type; math is FP32 */
+    int device;             /* CUDA device ordinal */
+} LumRadSettings;
+
+/* One material; identical layout to LumInternal::Material (internal_types.hpp:26-30),
+ * uploaded as the 6x256 R32_SFLOAT image by updateMaterialPalette (load_stuff.cpp:89-111). */
+typedef struct {
+    float color[4];         /* rgb albedo + alpha (alpha unused by the pass) */
+    float emmit;            /* emission */
+    float rough;            /* roughness (unused by the pass) */
+} LumRadMaterial;
+
+/* Per-pass parameters; replaces radiance.comp's push constants (radiance.comp:30-35),
+ * RAYS_PER_PROBE (:37), REACTIVNESS (:28) and max_dist (:193). */
+typedef struct {
+    int   rays_per_probe;   /* R: multiple of 32, 32..1024 (reference: 64) */
+    float max_dist;         /* coarse-march length limit in voxels, (0, 16384] (reference: 128) */
+    float blend;            /* temporal blend factor in [0,1] (reference REACTIVNESS: 0.01) */
+    int   time_seed;        /* pco.timeSeed: the frame index in the reference */
+    int   size;             /* pco.size (magicSize): process requests shift, shift+size, ...;
+                               0 = adaptive time slicing as update_radiance does */
+    int   shift;            /* pco.sihft: first request, 0 <= shift < size */
+    int   record_hits;      /* 1 = keep one LumRadHit per traced ray for lumrad_get_hits */
+} LumRadPassParams;
+
+/* One traced ray, recorded when LumRadPassParams.record_hits = 1.  Layout is fixed (24 B). */
+typedef struct {
+    int32_t  voxel[3];      /* hit: voxel where the refine DDA stopped; miss: 0 */
+    int16_t  block;         /* block id read at the last coarse-march position */
+    uint8_t  voxel_id;      /* hit: palette value of that voxel (the material index) */
+    uint8_t  flags;         /* LUMRAD_HIT_* bits */
+    uint16_t coarse_steps;  /* coarse-march iterations (one grid+palette lookup each) */
+    uint8_t  refine_steps;  /* refine-DDA iterations, 0..5 */
+    uint8_t  coarse_voxel;  /* palette value that ended the coarse march (0 on a miss) */
+    float    fraction;      /* hit: refine distance; miss: final coarse distance */
+} LumRadHit;
+
+#define LUMRAD_HIT_HIT      0x01  /* CastRay_fast returned true */
+#define LUMRAD_HIT_STEP_X   0x02  /* last refine step moved along x (normal = -sign(dir.x)) */
+#define LUMRAD_HIT_STEP_Y   0x04
+#define LUMRAD_HIT_STEP_Z   0x08
+#define LUMRAD_HIT_CAPPED   0x10  /* stopped by the 2*max_dist+2 step bound */
+
+/* Counters of the last pass (exact; identical on every implementation of the pass). */
+typedef struct {
+    uint64_t probes;        /* probes updated */
+    uint64_t rays;          /* rays traced */
+    uint64_t steps;         /* grid+palette lookups: coarse steps + refine lookups */
+    uint64_t hits;          /* rays that hit a voxel */
+    float    gpu_ms;        /* device time of the pass kernel (CUDA events) */
+} LumRadPassStats;
+
+/* ---- context lifetime (lum_create_instance / lum_init / lum_destroy_instance) ------------- */
+int  lumrad_create(const LumRadSettings* settings, LumRadContext* out);
+void lumrad_destroy(LumRadContext ctx);
+const char* lumrad_last_error(void);          /* last error message of this host thread */
+int  lumrad_synchronize(LumRadContext ctx);    /* lum_wait_idle (crenderer.h:108) */
+
+/* ---- inputs ------------------------------------------------------------------------------- */
+/* lum_load_world (crenderer.h:72): X*Y*Z int16 ids, x-fastest. */
+int  lumrad_load_world(LumRadContext ctx, const int16_t* blocks);
+/* lum_set_world_block / lum_get_world_block (crenderer.h:75-76). */
+int  lumrad_set_world_block(LumRadContext ctx, int x, int y, int z, int16_t block);
+int  lumrad_get_world_block(LumRadContext ctx, int x, int y, int z, int16_t* block);
+/* lum_load_block (crenderer.h:78): 4096 voxels as BlockVoxels[x][y][z] (z fastest). */
+int  lumrad_load_block(LumRadContext ctx, int16_t block, const uint8_t* voxels);
+/* lum_upload_block_palette_to_gpu (crenderer.h:81). */
+int  lumrad_upload_block_palette(LumRadContext ctx);
+/* 256 materials (Lum's material palette) and lum_upload_material_palette_to_gpu (crenderer.h:82). */
+int  lumrad_load_materials(LumRadContext ctx, const LumRadMaterial* materials);
+int  lumrad_upload_material_palette(LumRadContext ctx);
+
+/* ---- radiance volume ---------------------------------------------------------------------- */
+/* X*Y*Z*3 floats (rgb), x-fastest.  set clamps to [0,1] like a UNORM upload. */
+int  lumrad_get_radiance(LumRadContext ctx, float* rgb);
+int  lumrad_set_radiance(LumRadContext ctx, const float* rgb);
+
+/* ---- the pass ----------------------------------------------------------------------------- */
+/* Update list of LumInternalRenderer::update_radiance (internal_render.cpp:1142-1168):
+ * blocks whose clamped 3x3x3 neighbourhood sums to > 0, then the queued special requests.
+ * Writes up to `cap` entries of (x,y,z,0) into out; *n = full list length. */
+int  lumrad_build_update_list(LumRadContext ctx, int16_t* out, int cap, int* n);
+/* Queue one special request (specialRadianceUpdates, internal_render.cpp:1164-1168). */
+int  lumrad_request_update(LumRadContext ctx, int x, int y, int z);
+
+/* The drop-in for LumInternalRenderer::update_radiance() (internal_render.cpp:1129-1214):
+ * builds the update list, uploads it and runs one pass.  With params->size == 0 the time
+ * slicing adapts as the reference does (magicSize in [1,10], 1.8-2.2 ms target) and
+ * time_seed/shift follow the context's frame counter. */
+int  lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params);
+
+/* One pass over an explicit update list of n entries (x,y,z,w) — the body of
+ * radiance.comp:361-413 dispatched over n/size workgroups.  int16 coordinates. */
+int  lumrad_radiance_pass(LumRadContext ctx, const int16_t* requests, int n,
+                          const LumRadPassParams* params);
+/* Same with the reference's i8vec4 request encoding (internal_render.hpp:410). */
+int  lumrad_radiance_pass_i8(LumRadContext ctx, const int8_t* requests, int n,
+                             const LumRadPassParams* params);
+
+/* Resident request lists: upload once, run passes without host traffic. */
+int  lumrad_upload_requests(LumRadContext ctx, int slot, const int16_t* requests, int n);
+int  lumrad_radiance_pass_resident(LumRadContext ctx, int slot, const LumRadPassParams* params);
+
+/* Hit records of the last pass run with record_hits = 1: n_groups*R entries in dispatch
+ * order (entry g*R + r = ray r of workgroup g).  *n = number available. */
+int  lumrad_get_hits(LumRadContext ctx, LumRadHit* out, size_t cap, size_t* n);
+/* Counters and device time of the last pass (synchronises). */
+int  lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out);
+
+/* The CUDA stream (cudaStream_t) every call of this context enqueues on, for callers that
+ * order their own work or time passes with their own events on it. */
+int  lumrad_get_stream(LumRadContext ctx, void** stream);
+/* Device times (ms, CUDA events around the pass kernel) of the last min(cap, 64) passes,
+ * oldest first; *n = number written.  Synchronises. */
+int  lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n);
+
+/* Direction table used for rays_per_probe = R (sphericalFibonacci, radiance.comp:293-314):
+ * R*3 floats.  cos/sin are evaluated in double and rounded to float. */
+int  lumrad_direction_table(int rays_per_probe, float* xyz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LUMRAD_H */

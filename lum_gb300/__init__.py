@@ -1,0 +1,177 @@
+"""lum_gb300 — GB300-native per-block radiance-field update (Lum's radiance pass).
+
+The product is the shared library liblumrad.so behind include/lumrad.h; this package builds it
+(`lum_gb300.build`) and wraps it for Python callers (`RadianceWorld`), in the shape of Lum's C API
+(src/renderer/api/crenderer.h): create a world, load blocks, materials and the block grid, run
+radiance passes, read the radiance volume back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._native import (HIT_DTYPE, PRECISION, LumRadError, Material, PassParams, PassStats, Settings,
+                      check, load, ptr)
+
+__all__ = ["RadianceWorld", "PassParams", "LumRadError", "HIT_DTYPE", "load", "pass_params"]
+
+
+def pass_params(rays: int = 64, max_dist: float = 128.0, blend: float = 0.01, time_seed: int = 0,
+                size: int = 1, shift: int = 0, record_hits: bool = False) -> PassParams:
+    """Pass parameters; the defaults are radiance.comp's own constants."""
+    return PassParams(rays, max_dist, blend, time_seed, size, shift, 1 if record_hits else 0)
+
+
+class RadianceWorld:
+    """One world resident on one GPU (a LumRadContext)."""
+
+    def __init__(self, world_size, max_block_types: int = 64, precision: str = "fp32", device: int = 0):
+        self.lib = load()
+        X, Y, Z = (int(v) for v in world_size)
+        self.dims = (X, Y, Z)
+        s = Settings((C.c_int * 3)(X, Y, Z), int(max_block_types), PRECISION[precision], int(device))
+        h = C.c_void_p()
+        check(self.lib.lumrad_create(C.byref(s), C.byref(h)))
+        self.h = h
+        self.precision = precision
+        self.max_block_types = max_block_types
+
+    # ---- lifetime
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.lumrad_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_blocks(self) -> int:
+        return self.dims[0] * self.dims[1] * self.dims[2]
+
+    def synchronize(self) -> None:
+        check(self.lib.lumrad_synchronize(self.h))
+
+    # ---- inputs
+    def load_world(self, grid: np.ndarray) -> None:
+        g = np.ascontiguousarray(grid, dtype=np.int16)
+        assert g.size == self.n_blocks
+        check(self.lib.lumrad_load_world(self.h, ptr(g)))
+
+    def set_world_block(self, x: int, y: int, z: int, block: int) -> None:
+        check(self.lib.lumrad_set_world_block(self.h, x, y, z, block))
+
+    def get_world_block(self, x: int, y: int, z: int) -> int:
+        out = C.c_int16()
+        check(self.lib.lumrad_get_world_block(self.h, x, y, z, C.byref(out)))
+        return int(out.value)
+
+    def load_block(self, block: int, voxels_xyz: np.ndarray) -> None:
+        """voxels indexed [x][y][z] (Lum's BlockVoxels)."""
+        v = np.ascontiguousarray(voxels_xyz, dtype=np.uint8)
+        assert v.shape == (16, 16, 16)
+        check(self.lib.lumrad_load_block(self.h, block, ptr(v)))
+
+    def upload_block_palette(self) -> None:
+        check(self.lib.lumrad_upload_block_palette(self.h))
+
+    def load_materials(self, mats: np.ndarray) -> None:
+        m = np.ascontiguousarray(mats, dtype=np.float32)
+        assert m.shape == (256, 6)
+        check(self.lib.lumrad_load_materials(self.h, ptr(m)))
+
+    def upload_material_palette(self) -> None:
+        check(self.lib.lumrad_upload_material_palette(self.h))
+
+    def load(self, world) -> None:
+        """Loads a worldgen.World: grid, every palette slot and the materials, then uploads."""
+        self.load_world(world.grid)
+        for slot in range(min(world.palette.shape[0], self.max_block_types)):
+            self.load_block(slot, world.block_voxels(slot))
+        self.upload_block_palette()
+        self.load_materials(world.materials)
+        self.upload_material_palette()
+
+    # ---- radiance volume
+    def get_radiance(self) -> np.ndarray:
+        X, Y, Z = self.dims
+        out = np.empty((Z, Y, X, 3), dtype=np.float32)
+        check(self.lib.lumrad_get_radiance(self.h, ptr(out)))
+        return out
+
+    def set_radiance(self, rgb: np.ndarray) -> None:
+        r = np.ascontiguousarray(rgb, dtype=np.float32)
+        assert r.size == 3 * self.n_blocks
+        check(self.lib.lumrad_set_radiance(self.h, ptr(r)))
+
+    # ---- passes
+    def build_update_list(self) -> np.ndarray:
+        n = C.c_int()
+        check(self.lib.lumrad_build_update_list(self.h, None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 4), dtype=np.int16)
+        check(self.lib.lumrad_build_update_list(self.h, ptr(out), n.value, C.byref(n)))
+        return out[: n.value]
+
+    def request_update(self, x: int, y: int, z: int) -> None:
+        check(self.lib.lumrad_request_update(self.h, x, y, z))
+
+    def update_radiance(self, params: PassParams) -> None:
+        check(self.lib.lumrad_update_radiance(self.h, C.byref(params)))
+
+    def radiance_pass(self, requests: np.ndarray, params: PassParams) -> None:
+        req = np.ascontiguousarray(requests)
+        assert req.ndim == 2 and req.shape[1] == 4
+        if req.dtype == np.int8:
+            check(self.lib.lumrad_radiance_pass_i8(self.h, ptr(req), req.shape[0], C.byref(params)))
+        else:
+            req = req.astype(np.int16, copy=False)
+            check(self.lib.lumrad_radiance_pass(self.h, ptr(req), req.shape[0], C.byref(params)))
+
+    def upload_requests(self, slot: int, requests: np.ndarray) -> None:
+        req = np.ascontiguousarray(requests, dtype=np.int16)
+        check(self.lib.lumrad_upload_requests(self.h, slot, ptr(req), req.shape[0]))
+
+    def radiance_pass_resident(self, slot: int, params: PassParams) -> None:
+        check(self.lib.lumrad_radiance_pass_resident(self.h, slot, C.byref(params)))
+
+    def get_hits(self) -> np.ndarray:
+        n = C.c_size_t()
+        rc = self.lib.lumrad_get_hits(self.h, None, 0, C.byref(n))
+        check(rc)
+        out = np.zeros(n.value, dtype=HIT_DTYPE)
+        check(self.lib.lumrad_get_hits(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    def stream(self) -> int:
+        """cudaStream_t of this context as an integer handle."""
+        out = C.c_void_p()
+        check(self.lib.lumrad_get_stream(self.h, C.byref(out)))
+        return int(out.value or 0)
+
+    def kernel_times(self, cap: int = 64) -> np.ndarray:
+        """Device ms of the pass kernels of the last min(cap, 64) passes, oldest first."""
+        out = np.zeros(cap, dtype=np.float32)
+        n = C.c_int()
+        check(self.lib.lumrad_get_kernel_times(self.h, ptr(out), cap, C.byref(n)))
+        return out[: n.value]
+
+    def pass_stats(self) -> dict:
+        s = PassStats()
+        check(self.lib.lumrad_get_pass_stats(self.h, C.byref(s)))
+        return {"probes": s.probes, "rays": s.rays, "steps": s.steps, "hits": s.hits, "gpu_ms": s.gpu_ms}
+
+
+def direction_table(rays: int) -> np.ndarray:
+    out = np.zeros((rays, 3), dtype=np.float32)
+    check(load().lumrad_direction_table(rays, ptr(out)))
+    return out

@@ -1,0 +1,121 @@
+"""ctypes binding of liblumrad.so (include/lumrad.h).
+
+This is the binding a Python caller of the C ABI writes; the tests and the benchmark use it.
+It never falls back to anything: if the shared library is missing or does not load, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LUMRAD_OK = 0
+LUMRAD_EINVAL = -1
+LUMRAD_ENOMEM = -2
+LUMRAD_EDEVICE = -3
+LUMRAD_ETIMEOUT = -4
+LUMRAD_ESTATE = -5
+
+PRECISION = {"fp32": 0, "fp16": 1, "bf16": 2}
+
+
+class Settings(C.Structure):
+    _fields_ = [("world_size", C.c_int * 3), ("max_block_types", C.c_int),
+                ("precision", C.c_int), ("device", C.c_int)]
+
+
+class Material(C.Structure):
+    _fields_ = [("color", C.c_float * 4), ("emmit", C.c_float), ("rough", C.c_float)]
+
+
+class PassParams(C.Structure):
+    _fields_ = [("rays_per_probe", C.c_int), ("max_dist", C.c_float), ("blend", C.c_float),
+                ("time_seed", C.c_int), ("size", C.c_int), ("shift", C.c_int),
+                ("record_hits", C.c_int)]
+
+
+class PassStats(C.Structure):
+    _fields_ = [("probes", C.c_uint64), ("rays", C.c_uint64), ("steps", C.c_uint64),
+                ("hits", C.c_uint64), ("gpu_ms", C.c_float)]
+
+
+# LumRadHit as a numpy record (24 bytes, same layout as the C struct)
+HIT_DTYPE = np.dtype([("voxel", "<i4", (3,)), ("block", "<i2"), ("voxel_id", "u1"), ("flags", "u1"),
+                      ("coarse_steps", "<u2"), ("refine_steps", "u1"), ("coarse_voxel", "u1"),
+                      ("fraction", "<f4")])
+assert HIT_DTYPE.itemsize == 24
+
+# every symbol include/lumrad.h declares, with (restype, argtypes)
+_P = C.c_void_p
+_SIGS = {
+    "lumrad_create": (C.c_int, [C.POINTER(Settings), C.POINTER(_P)]),
+    "lumrad_destroy": (None, [_P]),
+    "lumrad_last_error": (C.c_char_p, []),
+    "lumrad_synchronize": (C.c_int, [_P]),
+    "lumrad_load_world": (C.c_int, [_P, _P]),
+    "lumrad_set_world_block": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int16]),
+    "lumrad_get_world_block": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int16)]),
+    "lumrad_load_block": (C.c_int, [_P, C.c_int16, _P]),
+    "lumrad_upload_block_palette": (C.c_int, [_P]),
+    "lumrad_load_materials": (C.c_int, [_P, _P]),
+    "lumrad_upload_material_palette": (C.c_int, [_P]),
+    "lumrad_get_radiance": (C.c_int, [_P, _P]),
+    "lumrad_set_radiance": (C.c_int, [_P, _P]),
+    "lumrad_build_update_list": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
+    "lumrad_request_update": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "lumrad_update_radiance": (C.c_int, [_P, C.POINTER(PassParams)]),
+    "lumrad_radiance_pass": (C.c_int, [_P, _P, C.c_int, C.POINTER(PassParams)]),
+    "lumrad_radiance_pass_i8": (C.c_int, [_P, _P, C.c_int, C.POINTER(PassParams)]),
+    "lumrad_upload_requests": (C.c_int, [_P, C.c_int, _P, C.c_int]),
+    "lumrad_radiance_pass_resident": (C.c_int, [_P, C.c_int, C.POINTER(PassParams)]),
+    "lumrad_get_hits": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "lumrad_get_pass_stats": (C.c_int, [_P, C.POINTER(PassStats)]),
+    "lumrad_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "lumrad_get_kernel_times": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
+    "lumrad_direction_table": (C.c_int, [C.c_int, _P]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads liblumrad.so (building it first if it is absent); raises if that fails."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"liblumrad.so not built: {path}")
+        _build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class LumRadError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lumrad error {code}: {msg}")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    if rc != LUMRAD_OK:
+        raise LumRadError(rc, load().lumrad_last_error().decode(errors="replace"))
+
+
+def ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data

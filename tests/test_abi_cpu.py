@@ -1,0 +1,67 @@
+"""The C ABI library without a GPU: it loads, exports every symbol include/lumrad.h declares,
+and rejects bad arguments before touching a device."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import lum_gb300
+from lum_gb300 import _native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "lumrad.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(lumrad_\w+)\s*\(", src)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = lum_gb300.load()
+    names = declared_symbols()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) <= set(_native._SIGS), "binding lacks a signature for a declared symbol"
+
+
+def test_struct_sizes_match_header():
+    assert C.sizeof(_native.Settings) == 24
+    assert C.sizeof(_native.Material) == 24
+    assert C.sizeof(_native.PassParams) == 28
+    assert _native.HIT_DTYPE.itemsize == 24
+
+
+def test_create_rejects_bad_settings_without_gpu():
+    lib = lum_gb300.load()
+    h = C.c_void_p()
+    for ws, slots, prec in [((0, 4, 4), 8, 0), ((4, 4, 4), 0, 0), ((4, 4, 4), 5000, 0), ((4, 4, 4), 8, 7),
+                            ((2048, 4, 4), 8, 0)]:
+        s = _native.Settings((C.c_int * 3)(*ws), slots, prec, 0)
+        rc = lib.lumrad_create(C.byref(s), C.byref(h))
+        assert rc == _native.LUMRAD_EINVAL, (ws, slots, prec, rc)
+        assert lib.lumrad_last_error()
+
+
+def test_null_arguments_are_errors_not_crashes():
+    lib = lum_gb300.load()
+    assert lib.lumrad_create(None, None) == _native.LUMRAD_EINVAL
+    assert lib.lumrad_load_world(None, None) == _native.LUMRAD_EINVAL
+    assert lib.lumrad_radiance_pass(None, None, 0, None) == _native.LUMRAD_EINVAL
+    assert lib.lumrad_get_hits(None, None, 0, None) == _native.LUMRAD_EINVAL
+    assert lib.lumrad_direction_table(0, None) == _native.LUMRAD_EINVAL
+    lib.lumrad_destroy(None)
+
+
+def test_create_without_gpu_reports_device_error():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except Exception:
+        pass
+    with pytest.raises(lum_gb300.LumRadError) as e:
+        lum_gb300.RadianceWorld((4, 4, 4))
+    assert e.value.code == _native.LUMRAD_EDEVICE

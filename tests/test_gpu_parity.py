@@ -1,0 +1,111 @@
+"""GPU pass vs CPU oracle through the C ABI: hit records bit-exact, radiance within 1e-5 relative.
+
+Cases follow the pass's parameters and the edge cases of its inputs: rays per probe 32..256,
+time slicing (size/shift), i8vec4 requests, multi-pass Jacobi chains, non-power-of-two worlds
+(REPEAT wrap of the radiance fetch), out-of-world requests, negative / unloaded / special block
+ids, a non-empty palette slot 0, empty lists.
+"""
+import numpy as np
+import pytest
+
+from lum_gb300 import worldgen
+from tests.helpers import RTOL, assert_hits_equal, gpu_pass, oracle_pass, random_prev, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(world, req, prev, **params):
+    got, hits, stats = gpu_pass(world, req, prev, **params)
+    ref, ref_hits, ref_stats = oracle_pass(world, req, prev, **params)
+    assert_hits_equal(hits, ref_hits)
+    assert rel_err(got, ref).max() <= RTOL
+    assert stats["steps"] == ref_stats["steps"] and stats["hits"] == ref_stats["hits"]
+    return got, ref
+
+
+def test_small_world_reference_constants():
+    """8x8x8 world, all 512 probes, 64 rays, max_dist 128, blend 0.1."""
+    w = worldgen.small_world()
+    got, ref = _check(w, worldgen.all_probes(w.dims), random_prev(w), rays=64, max_dist=128.0, blend=0.1,
+                      time_seed=0)
+    assert np.array_equal(got, ref), "FP32 radiance is expected bit-identical to the oracle"
+
+
+@pytest.mark.parametrize("rays", [32, 96, 128, 256])
+def test_rays_per_probe(rays):
+    w = worldgen.small_world(seed=11)
+    req = worldgen.probe_subset(w.dims, 0.25, seed=5)
+    _check(w, req, random_prev(w), rays=rays, max_dist=128.0, blend=0.1, time_seed=17)
+
+
+def test_time_slicing_size_shift():
+    w = worldgen.small_world(seed=3)
+    req = worldgen.all_probes(w.dims)
+    _check(w, req, random_prev(w), rays=64, max_dist=128.0, blend=0.01, time_seed=5, size=3, shift=2)
+
+
+def test_i8_requests_match_i16():
+    import lum_gb300
+    w = worldgen.small_world(seed=4)
+    req = worldgen.probe_subset(w.dims, 0.5, seed=2)
+    prev = random_prev(w)
+    outs = []
+    for r in (req, req.astype(np.int8)):
+        with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+            rw.load(w)
+            rw.set_radiance(prev)
+            rw.radiance_pass(r, lum_gb300.pass_params(rays=64, blend=0.1, time_seed=9))
+            outs.append(rw.get_radiance())
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_multi_pass_chain():
+    w = worldgen.terrain_world((12, 10, 6), seed=21, extra_blocks=40)
+    req = worldgen.all_probes(w.dims)
+    _check(w, req, random_prev(w), passes=3, seeds=[0, 1, 2], rays=64, max_dist=256.0, blend=0.1)
+
+
+def test_non_power_of_two_world():
+    w = worldgen.terrain_world((5, 7, 3), seed=8, n_types=5)
+    req = worldgen.all_probes(w.dims)
+    _check(w, req, random_prev(w), rays=64, max_dist=200.0, blend=0.3, time_seed=2)
+
+
+def test_odd_ids_and_slot0():
+    """Negative ids (OpSMod palette aliasing), ids past the loaded slots, SPECIAL_BLOCK, and a
+    non-empty palette slot 0 (air blocks are then not empty)."""
+    w = worldgen.terrain_world((9, 9, 5), seed=30, n_types=8)
+    g = w.grid.reshape(-1).copy()
+    idx = worldgen.randint(31, 1, 60, 0, g.size)
+    vals = np.array([-1, -5, -63, -64, -200, 9, 40, 4095, 32767, 12], dtype=np.int16)
+    g[idx] = vals[np.arange(60) % vals.size]
+    pal = w.palette.copy()
+    pal[0, 3:5, :, 6:9] = 17
+    w2 = worldgen.World(grid=g.reshape(w.grid.shape), palette=pal, materials=w.materials)
+    _check(w2, worldgen.all_probes(w2.dims), random_prev(w2), rays=64, max_dist=160.0, blend=0.2, time_seed=4)
+
+
+def test_out_of_world_requests_and_empty_list():
+    w = worldgen.small_world(seed=12)
+    req = worldgen.probe_subset(w.dims, 0.2, seed=1)
+    req = np.concatenate([req, np.array([[-1, 2, 2, 0], [8, 0, 0, 0], [3, 3, 40, 0]], dtype=np.int16)])
+    _check(w, req, random_prev(w), rays=32, max_dist=128.0, blend=0.5, time_seed=1)
+    _check(w, np.zeros((0, 4), np.int16), random_prev(w), rays=64, max_dist=128.0, blend=0.1, time_seed=0)
+    _check(w, req[:2], random_prev(w), rays=64, max_dist=128.0, blend=0.1, time_seed=0, size=3, shift=0)
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_low_precision_storage_vs_fp64(precision):
+    """FP16/BF16 storage with FP32 math: hits stay bit-exact; radiance error vs the FP64 oracle
+    is bounded by the storage rounding (2^-11 / 2^-8 relative per pass, compounded)."""
+    w = worldgen.terrain_world((10, 10, 6), seed=5, extra_blocks=20)
+    req = worldgen.all_probes(w.dims)
+    prev = random_prev(w)
+    got, hits, _ = gpu_pass(w, req, prev, precision=precision, passes=2, seeds=[0, 1], rays=64,
+                            max_dist=128.0, blend=0.1)
+    ref, ref_hits, _ = oracle_pass(w, req, prev, passes=2, seeds=[0, 1], precision="f64", rays=64,
+                                   max_dist=128.0, blend=0.1)
+    assert_hits_equal(hits, ref_hits)
+    tol = 2e-3 if precision == "fp16" else 1.6e-2
+    err = rel_err(got, ref, floor=1e-3)
+    assert err.max() <= tol, (precision, err.max())
