@@ -1,27 +1,27 @@
 // lumrad_host.cpp — the C ABI of include/lumrad.h: contexts, resident device data, passes.
 //
-// One context = one world resident on one GPU (grid, palettes, materials, two radiance volumes
-// for ping-pong) plus a stream, events and pinned staging for update lists.  It replaces the
-// radiance part of LumInternal::LumInternalRenderer: the resources of createImages
-// (src/renderer/src/internal_render.cpp:107-209), the uploads of updateBlockPalette /
-// updateMaterialPalette (load_stuff.cpp:36-111) and exec_copies' world upload
-// (internal_render.cpp:1460-1475), and update_radiance itself (internal_render.cpp:1129-1214).
+// One context = one world resident on one GPU plus a stream, events and pinned staging for
+// update lists.  It replaces the radiance part of LumInternal::LumInternalRenderer: the
+// resources of createImages (src/renderer/src/internal_render.cpp:107-209), the uploads of
+// updateBlockPalette / updateMaterialPalette (load_stuff.cpp:36-111) and exec_copies' world
+// upload (internal_render.cpp:1460-1475), and update_radiance itself (internal_render.cpp:1129-1214).
+//
+// Device layout of a world (all resident between passes):
+//   grid      int16  X*Y*Z            block ids, x-fastest
+//   cgrid     uint8 / uint16 X*Y*Z    compact ids (0 = air), rebuilt when the grid or palette changes
+//   cbits     uint32 128 per compact id   voxel occupancy of each compact id
+//   pal       uint8  slots*4096       voxel values, voxel (x,y,z) at x + 16y + 256z
+//   mats      float4 256              (r, g, b, emission)
+//   rad[2]    float4 or 4x16-bit per probe   previous / next radiance (ping-pong)
+//   scratch   float4 per (probe, subgroup); probe_count int per probe (zero between passes)
 
-#include <cuda_runtime.h>
-#include <cuda_fp16.h>
-#include <cuda_bf16.h>
+#include "lumrad_world.h"
 
 #include <algorithm>
 #include <cmath>
-#include <cstdint>
 #include <cstring>
-#include <map>
-#include <string>
-#include <vector>
 
-#include "lumrad_internal.h"
-
-namespace {
+namespace lumrad {
 
 thread_local std::string g_error;
 
@@ -29,13 +29,6 @@ int fail(int code, const std::string& msg) {
     g_error = msg;
     return code;
 }
-
-#define LUMRAD_CUDA(expr)                                                                  \
-    do {                                                                                   \
-        cudaError_t e_ = (expr);                                                           \
-        if (e_ != cudaSuccess)                                                             \
-            return fail(LUMRAD_EDEVICE, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
 
 // Spherical-Fibonacci directions of radiance.comp:293-306 with n = R.  The float arithmetic
 // follows the shader; cos/sin are evaluated in double and rounded to float.
@@ -57,66 +50,119 @@ void fibonacci_table(int n, float* xyz) {
     }
 }
 
-float unorm_clamp(float v) { return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f; }
+static float unorm_clamp(float v) { return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f; }
+static float exact_inverse(int v) { return (v > 0 && (v & (v - 1)) == 0) ? 1.0f / (float)v : 0.0f; }
 
-struct Context {
-    int X = 0, Y = 0, Z = 0;
-    size_t W = 0;
-    int n_slots = 0;
-    int precision = 0;
-    int device = 0;
-    int num_sms = 0;
-    size_t rad_stride = 16;   // bytes per probe
-
-    std::vector<int16_t> h_grid;
-    std::vector<uint8_t> h_pal;          // n_slots * 4096, device layout
-    std::vector<LumRadMaterial> h_mats;  // 256
-    std::vector<int16_t> specials;       // queued (x,y,z,w)
-    bool grid_dirty = true;
-    bool slot0_empty = true;
-
-    int16_t* d_grid = nullptr;
-    uint8_t* d_pal = nullptr;
-    float4* d_mats = nullptr;
-    void* d_rad[2] = {nullptr, nullptr};
-    int cur = 0;
-    short4* d_req = nullptr;
-    size_t req_cap = 0;
-    int16_t* h_req_pinned = nullptr;
-    size_t h_req_cap = 0;
-    std::map<int, float4*> d_dirs;
-    struct Resident { short4* ptr = nullptr; int n = 0; };
-    std::map<int, Resident> resident;
-    LumRadHit* d_hits = nullptr;
-    size_t hits_cap = 0, hits_n = 0;
-    bool hits_recorded = false;          // the last pass ran with record_hits = 1
-    unsigned long long* d_counters = nullptr;
-
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_req = nullptr;
-    static constexpr int kRing = 64;      // kernel-time history
-    cudaEvent_t ring0[kRing] = {}, ring1[kRing] = {};
-    long long n_passes = 0;
-    bool have_pass = false;
-    bool req_copy_pending = false;
-    LumRadPassStats last{};
-
-    // adaptive time slicing state (internal_render.cpp:1190-1203)
-    int frame = 0;
-    int magic_size = 1;
-    float last_ms = 0.0f;
-};
-
-Context* as_ctx(LumRadContext c) { return reinterpret_cast<Context*>(c); }
-
-int set_device(Context* c) {
-    LUMRAD_CUDA(cudaSetDevice(c->device));
+// ---------------------------------------------------------------- DeviceWorld
+int DeviceWorld::init(int X_, int Y_, int Z_, int slots, int precision_, cudaStream_t stream) {
+    X = X_; Y = Y_; Z = Z_;
+    W = (size_t)X * Y * Z;
+    n_slots = slots;
+    precision = precision_;
+    rad_stride = precision == LUMRAD_PRECISION_FP32 ? 16 : 8;
+    h_grid.assign(W, 0);
+    h_pal.assign((size_t)n_slots * 4096, 0);
+    h_pal_dev.assign((size_t)n_slots * 4096, 0);
+    h_mats.assign(LUMRAD_MATERIALS, LumRadMaterial{});
+    LUMRAD_TRY(cudaMalloc(&d_grid, W * sizeof(int16_t)));
+    LUMRAD_TRY(cudaMalloc(&d_cgrid, W * sizeof(uint16_t)));
+    LUMRAD_TRY(cudaMalloc(&d_pal, h_pal.size()));
+    LUMRAD_TRY(cudaMalloc(&d_mats, LUMRAD_MATERIALS * sizeof(float4)));
+    LUMRAD_TRY(cudaMalloc(&d_stats, 2 * sizeof(unsigned long long)));
+    for (int i = 0; i < 2; i++) {
+        LUMRAD_TRY(cudaMalloc(&d_rad[i], W * rad_stride));
+        LUMRAD_TRY(cudaMemsetAsync(d_rad[i], 0, W * rad_stride, stream));
+    }
+    LUMRAD_TRY(cudaMemsetAsync(d_grid, 0, W * sizeof(int16_t), stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_pal, 0, h_pal.size(), stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_mats, 0, LUMRAD_MATERIALS * sizeof(float4), stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
+    grid_dirty = false;
+    compact_dirty = true;
     return LUMRAD_OK;
 }
 
-int ensure_dirs(Context* c, int R, const float4** out) {
-    auto it = c->d_dirs.find(R);
-    if (it != c->d_dirs.end()) {
+void DeviceWorld::release() {
+    cudaFree(d_grid); cudaFree(d_cgrid); cudaFree(d_cbits); cudaFree(d_pal); cudaFree(d_mats);
+    cudaFree(d_rad[0]); cudaFree(d_rad[1]); cudaFree(d_scratch); cudaFree(d_probe_count); cudaFree(d_stats);
+    cudaFree(d_hits);
+    for (auto& kv : d_dirs) cudaFree(kv.second);
+    d_dirs.clear();
+    d_grid = nullptr; d_cgrid = nullptr; d_cbits = nullptr; d_pal = nullptr; d_mats = nullptr;
+    d_rad[0] = d_rad[1] = nullptr; d_scratch = nullptr; d_probe_count = nullptr; d_stats = nullptr; d_hits = nullptr;
+}
+
+// Renumbers the block ids present in the grid into compact ids (0 stays 0; every id whose palette
+// slot is absent shares one all-empty compact id) and builds each compact id's occupancy mask
+// from the palette as uploaded.
+void DeviceWorld::build_compact() {
+    std::vector<int32_t> id_to_c(65536, -1);
+    std::vector<int> reps;   // representative block id of each compact id (-100000: empty)
+    auto slot_of = [&](int b) { return b >= 0 ? b : b + 64; };
+    auto has_slot = [&](int b) { return b >= -63 && slot_of(b) < n_slots; };
+    id_to_c[0] = 0;
+    reps.push_back(0);
+    int empty_c = -1;
+    for (size_t i = 0; i < W; i++) {
+        const int b = h_grid[i];
+        int32_t& c = id_to_c[(uint16_t)b];
+        if (c >= 0) continue;
+        if (has_slot(b)) {
+            c = (int32_t)reps.size();
+            reps.push_back(b);
+        } else {
+            if (empty_c < 0) {
+                empty_c = (int)reps.size();
+                reps.push_back(-100000);
+            }
+            c = empty_c;
+        }
+    }
+    n_compact = (int)reps.size();
+    cgrid_wide = n_compact > 256;
+    h_cgrid.resize(W * (cgrid_wide ? 2 : 1));
+    for (size_t i = 0; i < W; i++) {
+        const int32_t c = id_to_c[(uint16_t)h_grid[i]];
+        if (cgrid_wide) reinterpret_cast<uint16_t*>(h_cgrid.data())[i] = (uint16_t)c;
+        else h_cgrid[i] = (uint8_t)c;
+    }
+    h_cbits.assign((size_t)n_compact * 128, 0u);
+    for (int c = 0; c < n_compact; c++) {
+        if (reps[c] == -100000 || !has_slot(reps[c])) continue;
+        const uint8_t* v = h_pal_dev.data() + (size_t)slot_of(reps[c]) * 4096;
+        uint32_t* bits = h_cbits.data() + (size_t)c * 128;
+        for (int k = 0; k < 4096; k++)
+            if (v[k]) bits[k >> 5] |= 1u << (k & 31);
+    }
+}
+
+int DeviceWorld::sync_inputs(cudaStream_t stream) {
+    if (grid_dirty) {
+        LUMRAD_TRY(cudaMemcpyAsync(d_grid, h_grid.data(), W * sizeof(int16_t), cudaMemcpyHostToDevice, stream));
+        grid_dirty = false;
+        compact_dirty = true;
+    }
+    if (compact_dirty) {
+        build_compact();
+        if ((size_t)n_compact > cbits_cap) {
+            cudaFree(d_cbits);
+            d_cbits = nullptr;
+            cbits_cap = 0;
+            LUMRAD_TRY(cudaMalloc(&d_cbits, (size_t)n_compact * 128 * sizeof(uint32_t)));
+            cbits_cap = (size_t)n_compact;
+        }
+        LUMRAD_TRY(cudaMemcpyAsync(d_cgrid, h_cgrid.data(), h_cgrid.size(), cudaMemcpyHostToDevice, stream));
+        LUMRAD_TRY(cudaMemcpyAsync(d_cbits, h_cbits.data(), h_cbits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                   stream));
+        LUMRAD_TRY(cudaStreamSynchronize(stream));   // host vectors may be rebuilt by the next call
+        compact_dirty = false;
+    }
+    return LUMRAD_OK;
+}
+
+int DeviceWorld::ensure_dirs(int R, cudaStream_t stream, const float4** out) {
+    auto it = d_dirs.find(R);
+    if (it != d_dirs.end()) {
         *out = it->second;
         return LUMRAD_OK;
     }
@@ -125,411 +171,226 @@ int ensure_dirs(Context* c, int R, const float4** out) {
     std::vector<float4> t(R);
     for (int i = 0; i < R; i++) t[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
     float4* d = nullptr;
-    LUMRAD_CUDA(cudaMalloc(&d, sizeof(float4) * R));
-    LUMRAD_CUDA(cudaMemcpyAsync(d, t.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    c->d_dirs[R] = d;
+    LUMRAD_TRY(cudaMalloc(&d, sizeof(float4) * R));
+    LUMRAD_TRY(cudaMemcpyAsync(d, t.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    d_dirs[R] = d;
     *out = d;
     return LUMRAD_OK;
 }
 
-int upload_grid(Context* c) {
-    if (!c->grid_dirty) return LUMRAD_OK;
-    LUMRAD_CUDA(cudaMemcpyAsync(c->d_grid, c->h_grid.data(), c->W * sizeof(int16_t),
-                                cudaMemcpyHostToDevice, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    c->grid_dirty = false;
+int DeviceWorld::ensure_scratch(size_t groups, int R) {
+    const size_t nsub = (size_t)(R / 32);
+    if (groups * nsub > scratch_cap) {
+        cudaFree(d_scratch);
+        d_scratch = nullptr;
+        scratch_cap = 0;
+        const size_t cap = std::max<size_t>(groups * nsub, 1024);
+        LUMRAD_TRY(cudaMalloc(&d_scratch, cap * sizeof(float4)));
+        scratch_cap = cap;
+    }
+    if (groups > count_cap) {
+        cudaFree(d_probe_count);
+        d_probe_count = nullptr;
+        count_cap = 0;
+        const size_t cap = std::max<size_t>(groups, 1024);
+        LUMRAD_TRY(cudaMalloc(&d_probe_count, cap * sizeof(int)));
+        LUMRAD_TRY(cudaMemset(d_probe_count, 0, cap * sizeof(int)));
+        count_cap = cap;
+    }
     return LUMRAD_OK;
 }
 
-int check_params(const Context* c, const LumRadPassParams* p) {
-    if (!p) return fail(LUMRAD_EINVAL, "params is null");
-    if (p->rays_per_probe < 32 || p->rays_per_probe > 1024 || p->rays_per_probe % 32 != 0)
-        return fail(LUMRAD_EINVAL, "rays_per_probe must be a multiple of 32 in [32, 1024]");
-    if (!(p->max_dist > 0.0f) || p->max_dist > 16384.0f)
-        return fail(LUMRAD_EINVAL, "max_dist must be in (0, 16384]");
-    if (!(p->blend >= 0.0f && p->blend <= 1.0f)) return fail(LUMRAD_EINVAL, "blend must be in [0, 1]");
-    if (p->size < 0 || p->size > (1 << 20)) return fail(LUMRAD_EINVAL, "size out of range");
-    if (p->size > 0 && (p->shift < 0 || p->shift >= p->size))
-        return fail(LUMRAD_EINVAL, "shift must be in [0, size)");
-    (void)c;
+int DeviceWorld::ensure_hits(size_t n) {
+    if (n <= hits_cap) return LUMRAD_OK;
+    cudaFree(d_hits);
+    d_hits = nullptr;
+    hits_cap = 0;
+    LUMRAD_TRY(cudaMalloc(&d_hits, std::max<size_t>(n, 1) * sizeof(LumRadHit)));
+    hits_cap = std::max<size_t>(n, 1);
     return LUMRAD_OK;
 }
 
-int ensure_req_capacity(Context* c, size_t n) {
-    if (n <= c->req_cap) return LUMRAD_OK;
-    if (c->d_req) cudaFree(c->d_req);
-    c->d_req = nullptr;
-    size_t cap = std::max<size_t>(n, 1024);
-    LUMRAD_CUDA(cudaMalloc(&c->d_req, cap * sizeof(short4)));
-    c->req_cap = cap;
+// Fills the kernel's view of one pass over `d_req` (n requests) with parameters `p`
+// (size >= 1) reading rad[cur] and writing rad[1-cur].
+int DeviceWorld::prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream,
+                              WorldPass* out) {
+    int rc = sync_inputs(stream);
+    if (rc) return rc;
+    const float4* dirs = nullptr;
+    if ((rc = ensure_dirs(p.rays_per_probe, stream, &dirs))) return rc;
+    const int R = p.rays_per_probe;
+    const int groups = n / p.size;
+    if ((long long)groups * (R / 32) >= (1LL << 31)) return fail(LUMRAD_EINVAL, "pass has too many subgroups (>= 2^31)");
+    if ((rc = ensure_scratch((size_t)std::max(groups, 1), R))) return rc;
+    if (p.record_hits && (rc = ensure_hits((size_t)groups * R))) return rc;
+    WorldPass& w = *out;
+    std::memset(&w, 0, sizeof w);
+    w.X = X; w.Y = Y; w.Z = Z;
+    w.cgrid_wide = cgrid_wide ? 1 : 0;
+    w.cgrid = d_cgrid;
+    w.cbits = d_cbits;
+    w.grid = d_grid;
+    w.pal = d_pal;
+    w.n_slots = n_slots;
+    w.mats = d_mats;
+    w.prev = d_rad[cur];
+    w.next = d_rad[1 - cur];
+    w.req = d_req;
+    w.n_groups = groups;
+    w.size = p.size;
+    w.shift = p.shift;
+    w.R = R;
+    w.max_dist = p.max_dist;
+    w.max_steps = (int)(2.0f * p.max_dist) + 2;
+    w.alpha = p.blend;
+    w.one_minus_alpha = 1.0f - p.blend;
+    w.seed = (uint32_t)p.time_seed;
+    w.inv_dim[0] = exact_inverse(X);
+    w.inv_dim[1] = exact_inverse(Y);
+    w.inv_dim[2] = exact_inverse(Z);
+    w.inv_nsub = exact_inverse(R / 32);
+    w.dirs = dirs;
+    w.hits = p.record_hits ? d_hits : nullptr;
+    w.scratch = d_scratch;
+    w.probe_count = d_probe_count;
+    w.stats = d_stats;
+    w.task_begin = 0;
+    w.n_tasks = (long long)groups * (R / 32);
+    hits_recorded = p.record_hits != 0;
+    hits_n = p.record_hits ? (size_t)groups * R : 0;
+    // probes not in the list keep their value: next starts as a copy of prev
+    LUMRAD_TRY(cudaMemcpyAsync(d_rad[1 - cur], d_rad[cur], W * rad_stride, cudaMemcpyDeviceToDevice, stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
     return LUMRAD_OK;
 }
 
-// Copies n requests (x,y,z,w int16) into the device list through pinned staging.
-int stage_requests(Context* c, const int16_t* req, size_t n) {
-    int rc = ensure_req_capacity(c, n);
+// ---------------------------------------------------------------- Context
+int Context::ensure_req_capacity(size_t n) {
+    if (n <= req_cap) return LUMRAD_OK;
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    cudaFree(d_req);
+    d_req = nullptr;
+    req_cap = 0;
+    const size_t cap = std::max<size_t>(n, 1024);
+    LUMRAD_TRY(cudaMalloc(&d_req, cap * sizeof(short4)));
+    req_cap = cap;
+    return LUMRAD_OK;
+}
+
+int Context::stage_requests(const int16_t* req, size_t n) {
+    int rc = ensure_req_capacity(n);
     if (rc) return rc;
     if (n == 0) return LUMRAD_OK;
-    if (c->req_copy_pending) {
-        LUMRAD_CUDA(cudaEventSynchronize(c->ev_req));
-        c->req_copy_pending = false;
+    if (req_copy_pending) {
+        LUMRAD_TRY(cudaEventSynchronize(ev_req));
+        req_copy_pending = false;
     }
-    if (n > c->h_req_cap) {
-        if (c->h_req_pinned) cudaFreeHost(c->h_req_pinned);
-        c->h_req_pinned = nullptr;
-        size_t cap = std::max<size_t>(n, 1024);
-        LUMRAD_CUDA(cudaMallocHost(&c->h_req_pinned, cap * 4 * sizeof(int16_t)));
-        c->h_req_cap = cap;
+    if (n > h_req_cap) {
+        if (h_req_pinned) cudaFreeHost(h_req_pinned);
+        h_req_pinned = nullptr;
+        h_req_cap = 0;
+        const size_t cap = std::max<size_t>(n, 1024);
+        LUMRAD_TRY(cudaMallocHost(&h_req_pinned, cap * 4 * sizeof(int16_t)));
+        h_req_cap = cap;
     }
-    std::memcpy(c->h_req_pinned, req, n * 4 * sizeof(int16_t));
-    LUMRAD_CUDA(cudaMemcpyAsync(c->d_req, c->h_req_pinned, n * sizeof(short4), cudaMemcpyHostToDevice,
-                                c->stream));
-    LUMRAD_CUDA(cudaEventRecord(c->ev_req, c->stream));
-    c->req_copy_pending = true;
+    std::memcpy(h_req_pinned, req, n * 4 * sizeof(int16_t));
+    LUMRAD_TRY(cudaMemcpyAsync(d_req, h_req_pinned, n * sizeof(short4), cudaMemcpyHostToDevice, stream));
+    LUMRAD_TRY(cudaEventRecord(ev_req, stream));
+    req_copy_pending = true;
     return LUMRAD_OK;
 }
 
-// One pass over `n` requests already on the device at `d_req`.
-int run_pass(Context* c, const short4* d_req, int n, const LumRadPassParams* p_in) {
+int Context::check_error() {
+    if (!have_pass) return LUMRAD_OK;
+    int e = 0;
+    LUMRAD_TRY(cudaMemcpyAsync(&e, d_error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    if (e != 0) {
+        cudaMemsetAsync(d_error, 0, sizeof(int), stream);
+        cudaMemsetAsync(d_queue, 0, 2 * sizeof(unsigned long long), stream);
+        cudaMemsetAsync(world.d_probe_count, 0, world.count_cap * sizeof(int), stream);
+        cudaStreamSynchronize(stream);
+        return fail(LUMRAD_EDEVICE, "radiance kernel scheduler stopped making progress (code " + std::to_string(e) + ")");
+    }
+    return LUMRAD_OK;
+}
+
+int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in) {
     LumRadPassParams p = *p_in;
     if (p.size == 0) {
         // adaptive slicing of update_radiance (internal_render.cpp:1190-1203)
-        if (c->last_ms < 1.8f) c->magic_size--;
-        else if (c->last_ms > 2.2f) c->magic_size++;
-        c->magic_size = std::min(std::max(c->magic_size, 1), 10);
-        p.size = c->magic_size;
-        p.shift = c->frame % c->magic_size;
-        p.time_seed = c->frame;
+        if (last_ms < 1.8f) magic_size--;
+        else if (last_ms > 2.2f) magic_size++;
+        magic_size = std::min(std::max(magic_size, 1), 10);
+        p.size = magic_size;
+        p.shift = frame % magic_size;
+        p.time_seed = frame;
     }
-    c->frame++;
-    int rc = upload_grid(c);
+    frame++;
+    LaunchArgs la;
+    std::memset(&la, 0, sizeof la);
+    int rc = world.prepare_pass(d_reqs, n, p, stream, &la.single);
     if (rc) return rc;
-    const float4* dirs = nullptr;
-    rc = ensure_dirs(c, p.rays_per_probe, &dirs);
-    if (rc) return rc;
-    const int groups = n / p.size;
-    const int R = p.rays_per_probe;
-    if (p.record_hits) {
-        const size_t need = (size_t)groups * R;
-        if (need > c->hits_cap) {
-            if (c->d_hits) cudaFree(c->d_hits);
-            c->d_hits = nullptr;
-            c->hits_cap = 0;
-            LUMRAD_CUDA(cudaMalloc(&c->d_hits, std::max<size_t>(need, 1) * sizeof(LumRadHit)));
-            c->hits_cap = std::max<size_t>(need, 1);
-        }
-        c->hits_n = need;
-        c->hits_recorded = true;
-    } else {
-        c->hits_n = 0;
-        c->hits_recorded = false;
+    la.worlds = nullptr;
+    la.n_worlds = 1;
+    la.n_tasks = la.single.n_tasks;
+    la.queue = d_queue;
+    la.error = d_error;
+    const int slot = (int)(n_passes % kRing);
+    LUMRAD_TRY(cudaEventRecord(ev_start, stream));
+    LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
+    LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream));
+    LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
+    LUMRAD_TRY(cudaEventRecord(ev_end, stream));
+    n_passes++;
+    world.cur = 1 - world.cur;
+    have_pass = true;
+    last.probes = (uint64_t)la.single.n_groups;
+    last.rays = (uint64_t)la.single.n_groups * la.single.R;
+    return LUMRAD_OK;
+}
+
+void Context::release() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    world.release();
+    cudaFree(d_req);
+    cudaFree(d_queue);
+    cudaFree(d_error);
+    for (auto& kv : resident) cudaFree(kv.second.ptr);
+    if (h_req_pinned) cudaFreeHost(h_req_pinned);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_end) cudaEventDestroy(ev_end);
+    if (ev_req) cudaEventDestroy(ev_req);
+    for (int i = 0; i < kRing; i++) {
+        if (ring0[i]) cudaEventDestroy(ring0[i]);
+        if (ring1[i]) cudaEventDestroy(ring1[i]);
     }
-    const int src = c->cur, dst = 1 - c->cur;
-    LUMRAD_CUDA(cudaMemcpyAsync(c->d_rad[dst], c->d_rad[src], c->W * c->rad_stride,
-                                cudaMemcpyDeviceToDevice, c->stream));
-    LUMRAD_CUDA(cudaMemsetAsync(c->d_counters, 0, 2 * sizeof(unsigned long long), c->stream));
-
-    lumrad::PassArgs a{};
-    a.w.X = c->X; a.w.Y = c->Y; a.w.Z = c->Z;
-    a.w.n_slots = c->n_slots;
-    a.w.slot0_empty = c->slot0_empty ? 1 : 0;
-    a.w.grid = c->d_grid;
-    a.w.pal = c->d_pal;
-    a.w.mats = c->d_mats;
-    a.prev = c->d_rad[src];
-    a.next = c->d_rad[dst];
-    a.req = d_req;
-    a.n_groups = groups;
-    a.size = p.size;
-    a.shift = p.shift;
-    a.R = R;
-    a.probes_per_unit = R <= lumrad::kPool ? lumrad::kPool / R : 1;
-    a.max_dist = p.max_dist;
-    a.max_steps = (int)(2.0f * p.max_dist) + 2;
-    a.alpha = p.blend;
-    a.one_minus_alpha = 1.0f - p.blend;
-    a.seed = (uint32_t)p.time_seed;
-    a.dirs = dirs;
-    a.hits = p.record_hits ? c->d_hits : nullptr;
-    a.counters = c->d_counters;
-
-    const int slot = (int)(c->n_passes % Context::kRing);
-    LUMRAD_CUDA(cudaEventRecord(c->ev_start, c->stream));
-    LUMRAD_CUDA(cudaEventRecord(c->ring0[slot], c->stream));
-    LUMRAD_CUDA(lumrad::launch_radiance_pass(a, c->precision, p.record_hits != 0, true, c->num_sms,
-                                             c->stream));
-    LUMRAD_CUDA(cudaEventRecord(c->ring1[slot], c->stream));
-    LUMRAD_CUDA(cudaEventRecord(c->ev_end, c->stream));
-    c->n_passes++;
-    c->cur = dst;
-    c->have_pass = true;
-    c->last.probes = (uint64_t)groups;
-    c->last.rays = (uint64_t)groups * R;
-    return LUMRAD_OK;
+    if (stream) cudaStreamDestroy(stream);
 }
 
-}  // namespace
+Context* as_ctx(LumRadContext c) { return reinterpret_cast<Context*>(c); }
 
-extern "C" {
-
-const char* lumrad_last_error(void) { return g_error.c_str(); }
-
-int lumrad_create(const LumRadSettings* s, LumRadContext* out) {
-    if (!s || !out) return fail(LUMRAD_EINVAL, "null argument");
-    *out = nullptr;
-    for (int i = 0; i < 3; i++)
-        if (s->world_size[i] < 1 || s->world_size[i] > 2047)
-            return fail(LUMRAD_EINVAL, "world_size must be in [1, 2047] per axis");
-    const uint64_t W = (uint64_t)s->world_size[0] * s->world_size[1] * s->world_size[2];
-    if (W >= (1ull << 31)) return fail(LUMRAD_EINVAL, "world has too many blocks (>= 2^31)");
-    if (s->max_block_types < 1 || s->max_block_types > LUMRAD_MAX_BLOCK_SLOTS)
-        return fail(LUMRAD_EINVAL, "max_block_types must be in [1, 4096]");
-    if (s->precision < 0 || s->precision > 2) return fail(LUMRAD_EINVAL, "unknown precision");
-    int ndev = 0;
-    cudaError_t e = cudaGetDeviceCount(&ndev);
-    if (e != cudaSuccess || ndev == 0)
-        return fail(LUMRAD_EDEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
-    if (s->device < 0 || s->device >= ndev) return fail(LUMRAD_EINVAL, "device ordinal out of range");
-
-    Context* c = new Context();
-    c->X = s->world_size[0]; c->Y = s->world_size[1]; c->Z = s->world_size[2];
-    c->W = (size_t)W;
-    c->n_slots = s->max_block_types;
-    c->precision = s->precision;
-    c->device = s->device;
-    c->rad_stride = s->precision == LUMRAD_PRECISION_FP32 ? 16 : 8;
-    c->h_grid.assign(c->W, 0);
-    c->h_pal.assign((size_t)c->n_slots * 4096, 0);
-    c->h_mats.assign(LUMRAD_MATERIALS, LumRadMaterial{});
-    auto cleanup = [&](int rc) {
-        lumrad_destroy(c);
-        return rc;
-    };
-    int rc = set_device(c);
-    if (rc) return cleanup(rc);
-#define CREATE_CUDA(expr)                                                                      \
-    do {                                                                                       \
-        cudaError_t e_ = (expr);                                                               \
-        if (e_ != cudaSuccess)                                                                 \
-            return cleanup(fail(e_ == cudaErrorMemoryAllocation ? LUMRAD_ENOMEM : LUMRAD_EDEVICE, \
-                                std::string(#expr) + ": " + cudaGetErrorString(e_)));          \
-    } while (0)
-    CREATE_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
-    CREATE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    CREATE_CUDA(cudaEventCreate(&c->ev_start));
-    CREATE_CUDA(cudaEventCreate(&c->ev_end));
-    CREATE_CUDA(cudaEventCreateWithFlags(&c->ev_req, cudaEventDisableTiming));
-    for (int i = 0; i < Context::kRing; i++) {
-        CREATE_CUDA(cudaEventCreate(&c->ring0[i]));
-        CREATE_CUDA(cudaEventCreate(&c->ring1[i]));
-    }
-    CREATE_CUDA(cudaMalloc(&c->d_grid, c->W * sizeof(int16_t)));
-    CREATE_CUDA(cudaMalloc(&c->d_pal, c->h_pal.size()));
-    CREATE_CUDA(cudaMalloc(&c->d_mats, LUMRAD_MATERIALS * sizeof(float4)));
-    for (int i = 0; i < 2; i++) {
-        CREATE_CUDA(cudaMalloc(&c->d_rad[i], c->W * c->rad_stride));
-        CREATE_CUDA(cudaMemsetAsync(c->d_rad[i], 0, c->W * c->rad_stride, c->stream));
-    }
-    CREATE_CUDA(cudaMalloc(&c->d_counters, 2 * sizeof(unsigned long long)));
-    CREATE_CUDA(cudaMemsetAsync(c->d_grid, 0, c->W * sizeof(int16_t), c->stream));
-    CREATE_CUDA(cudaMemsetAsync(c->d_pal, 0, c->h_pal.size(), c->stream));
-    CREATE_CUDA(cudaMemsetAsync(c->d_mats, 0, LUMRAD_MATERIALS * sizeof(float4), c->stream));
-    CREATE_CUDA(cudaStreamSynchronize(c->stream));
-#undef CREATE_CUDA
-    c->grid_dirty = false;
-    *out = c;
-    return LUMRAD_OK;
-}
-
-void lumrad_destroy(LumRadContext ctx) {
-    Context* c = as_ctx(ctx);
-    if (!c) return;
-    cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->d_grid);
-    cudaFree(c->d_pal);
-    cudaFree(c->d_mats);
-    cudaFree(c->d_rad[0]);
-    cudaFree(c->d_rad[1]);
-    cudaFree(c->d_req);
-    cudaFree(c->d_hits);
-    cudaFree(c->d_counters);
-    for (auto& kv : c->d_dirs) cudaFree(kv.second);
-    for (auto& kv : c->resident) cudaFree(kv.second.ptr);
-    if (c->h_req_pinned) cudaFreeHost(c->h_req_pinned);
-    if (c->ev_start) cudaEventDestroy(c->ev_start);
-    if (c->ev_end) cudaEventDestroy(c->ev_end);
-    if (c->ev_req) cudaEventDestroy(c->ev_req);
-    for (int i = 0; i < Context::kRing; i++) {
-        if (c->ring0[i]) cudaEventDestroy(c->ring0[i]);
-        if (c->ring1[i]) cudaEventDestroy(c->ring1[i]);
-    }
-    if (c->stream) cudaStreamDestroy(c->stream);
-    delete c;
-}
-
-int lumrad_synchronize(LumRadContext ctx) {
-    Context* c = as_ctx(ctx);
-    if (!c) return fail(LUMRAD_EINVAL, "null context");
-    LUMRAD_CUDA(cudaSetDevice(c->device));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    return LUMRAD_OK;
-}
-
-int lumrad_load_world(LumRadContext ctx, const int16_t* blocks) {
-    Context* c = as_ctx(ctx);
-    if (!c || !blocks) return fail(LUMRAD_EINVAL, "null argument");
-    std::memcpy(c->h_grid.data(), blocks, c->W * sizeof(int16_t));
-    c->grid_dirty = true;
-    int rc = set_device(c);
-    if (rc) return rc;
-    return upload_grid(c);
-}
-
-int lumrad_set_world_block(LumRadContext ctx, int x, int y, int z, int16_t block) {
-    Context* c = as_ctx(ctx);
-    if (!c) return fail(LUMRAD_EINVAL, "null context");
-    if (x < 0 || y < 0 || z < 0 || x >= c->X || y >= c->Y || z >= c->Z)
-        return fail(LUMRAD_EINVAL, "block coordinate out of the world");
-    c->h_grid[(size_t)x + (size_t)c->X * ((size_t)y + (size_t)c->Y * z)] = block;
-    c->grid_dirty = true;   // uploaded before the next pass, as exec_copies does every frame
-    return LUMRAD_OK;
-}
-
-int lumrad_get_world_block(LumRadContext ctx, int x, int y, int z, int16_t* block) {
-    Context* c = as_ctx(ctx);
-    if (!c || !block) return fail(LUMRAD_EINVAL, "null argument");
-    if (x < 0 || y < 0 || z < 0 || x >= c->X || y >= c->Y || z >= c->Z)
-        return fail(LUMRAD_EINVAL, "block coordinate out of the world");
-    *block = c->h_grid[(size_t)x + (size_t)c->X * ((size_t)y + (size_t)c->Y * z)];
-    return LUMRAD_OK;
-}
-
-int lumrad_load_block(LumRadContext ctx, int16_t block, const uint8_t* voxels) {
-    Context* c = as_ctx(ctx);
-    if (!c || !voxels) return fail(LUMRAD_EINVAL, "null argument");
-    if (block < 0 || block >= c->n_slots) return fail(LUMRAD_EINVAL, "block id outside the palette slots");
-    // BlockVoxels[x][y][z] (z fastest) -> x-fastest slot, as updateBlockPalette repacks it
-    uint8_t* dst = c->h_pal.data() + (size_t)block * 4096;
-    for (int x = 0; x < 16; x++)
-        for (int y = 0; y < 16; y++)
-            for (int z = 0; z < 16; z++) dst[x + 16 * y + 256 * z] = voxels[(x * 16 + y) * 16 + z];
-    return LUMRAD_OK;
-}
-
-int lumrad_upload_block_palette(LumRadContext ctx) {
-    Context* c = as_ctx(ctx);
-    if (!c) return fail(LUMRAD_EINVAL, "null context");
-    int rc = set_device(c);
-    if (rc) return rc;
-    c->slot0_empty = std::all_of(c->h_pal.begin(), c->h_pal.begin() + 4096, [](uint8_t v) { return v == 0; });
-    LUMRAD_CUDA(cudaMemcpyAsync(c->d_pal, c->h_pal.data(), c->h_pal.size(), cudaMemcpyHostToDevice, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    return LUMRAD_OK;
-}
-
-int lumrad_load_materials(LumRadContext ctx, const LumRadMaterial* materials) {
-    Context* c = as_ctx(ctx);
-    if (!c || !materials) return fail(LUMRAD_EINVAL, "null argument");
-    std::memcpy(c->h_mats.data(), materials, LUMRAD_MATERIALS * sizeof(LumRadMaterial));
-    return LUMRAD_OK;
-}
-
-int lumrad_upload_material_palette(LumRadContext ctx) {
-    Context* c = as_ctx(ctx);
-    if (!c) return fail(LUMRAD_EINVAL, "null context");
-    int rc = set_device(c);
-    if (rc) return rc;
-    std::vector<float4> m(LUMRAD_MATERIALS);
-    for (int i = 0; i < LUMRAD_MATERIALS; i++)
-        m[i] = make_float4(c->h_mats[i].color[0], c->h_mats[i].color[1], c->h_mats[i].color[2], c->h_mats[i].emmit);
-    LUMRAD_CUDA(cudaMemcpyAsync(c->d_mats, m.data(), m.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    return LUMRAD_OK;
-}
-
-int lumrad_get_radiance(LumRadContext ctx, float* rgb) {
-    Context* c = as_ctx(ctx);
-    if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
-    int rc = set_device(c);
-    if (rc) return rc;
-    if (c->precision == LUMRAD_PRECISION_FP32) {
-        std::vector<float4> h(c->W);
-        LUMRAD_CUDA(cudaMemcpyAsync(h.data(), c->d_rad[c->cur], c->W * 16, cudaMemcpyDeviceToHost, c->stream));
-        LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-        for (size_t i = 0; i < c->W; i++) {
-            rgb[3 * i] = h[i].x; rgb[3 * i + 1] = h[i].y; rgb[3 * i + 2] = h[i].z;
-        }
-    } else {
-        std::vector<uint16_t> h(c->W * 4);
-        LUMRAD_CUDA(cudaMemcpyAsync(h.data(), c->d_rad[c->cur], c->W * 8, cudaMemcpyDeviceToHost, c->stream));
-        LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-        for (size_t i = 0; i < c->W; i++)
-            for (int k = 0; k < 3; k++) {
-                uint16_t bits = h[4 * i + k];
-                float v;
-                if (c->precision == LUMRAD_PRECISION_FP16) {
-                    __half_raw r; r.x = bits;
-                    v = __half2float(__half(r));
-                } else {
-                    uint32_t u = (uint32_t)bits << 16;
-                    std::memcpy(&v, &u, 4);
-                }
-                rgb[3 * i + k] = v;
-            }
-    }
-    return LUMRAD_OK;
-}
-
-int lumrad_set_radiance(LumRadContext ctx, const float* rgb) {
-    Context* c = as_ctx(ctx);
-    if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
-    int rc = set_device(c);
-    if (rc) return rc;
-    if (c->precision == LUMRAD_PRECISION_FP32) {
-        std::vector<float4> h(c->W);
-        for (size_t i = 0; i < c->W; i++)
-            h[i] = make_float4(unorm_clamp(rgb[3 * i]), unorm_clamp(rgb[3 * i + 1]), unorm_clamp(rgb[3 * i + 2]), 1.0f);
-        LUMRAD_CUDA(cudaMemcpyAsync(c->d_rad[c->cur], h.data(), c->W * 16, cudaMemcpyHostToDevice, c->stream));
-        LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    } else {
-        std::vector<uint16_t> h(c->W * 4);
-        for (size_t i = 0; i < c->W; i++)
-            for (int k = 0; k < 4; k++) {
-                float v = k < 3 ? unorm_clamp(rgb[3 * i + k]) : 1.0f;
-                uint16_t bits;
-                if (c->precision == LUMRAD_PRECISION_FP16) {
-                    __half_raw r = __half_raw(__float2half_rn(v));
-                    bits = r.x;
-                } else {
-                    __nv_bfloat16_raw r = __nv_bfloat16_raw(__float2bfloat16_rn(v));
-                    bits = r.x;
-                }
-                h[4 * i + k] = bits;
-            }
-        LUMRAD_CUDA(cudaMemcpyAsync(c->d_rad[c->cur], h.data(), c->W * 8, cudaMemcpyHostToDevice, c->stream));
-        LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    }
-    return LUMRAD_OK;
-}
-
-int lumrad_request_update(LumRadContext ctx, int x, int y, int z) {
-    Context* c = as_ctx(ctx);
-    if (!c) return fail(LUMRAD_EINVAL, "null context");
-    if (x < 0 || y < 0 || z < 0 || x >= c->X || y >= c->Y || z >= c->Z)
-        return fail(LUMRAD_EINVAL, "request outside the world");
-    c->specials.insert(c->specials.end(), {(int16_t)x, (int16_t)y, (int16_t)z, 0});
+int check_params(const LumRadPassParams* p) {
+    if (!p) return fail(LUMRAD_EINVAL, "params is null");
+    if (p->rays_per_probe < 32 || p->rays_per_probe > 1024 || p->rays_per_probe % 32 != 0)
+        return fail(LUMRAD_EINVAL, "rays_per_probe must be a multiple of 32 in [32, 1024]");
+    if (!(p->max_dist > 0.0f) || p->max_dist > 16384.0f) return fail(LUMRAD_EINVAL, "max_dist must be in (0, 16384]");
+    if (!(p->blend >= 0.0f && p->blend <= 1.0f)) return fail(LUMRAD_EINVAL, "blend must be in [0, 1]");
+    if (p->size < 0 || p->size > (1 << 20)) return fail(LUMRAD_EINVAL, "size out of range");
+    if (p->size > 0 && (p->shift < 0 || p->shift >= p->size)) return fail(LUMRAD_EINVAL, "shift must be in [0, size)");
     return LUMRAD_OK;
 }
 
 // The 27-neighbour rule of update_radiance (internal_render.cpp:1142-1161) plus specials
 // (:1164-1168).  Specials are consumed, as the reference clears them.
-static int build_list(Context* c, std::vector<int16_t>& out) {
-    const int X = c->X, Y = c->Y, Z = c->Z;
-    std::vector<uint8_t> set(c->W, 0);
+void build_list(Context* c, std::vector<int16_t>& out) {
+    const DeviceWorld& w = c->world;
+    const int X = w.X, Y = w.Y, Z = w.Z;
+    std::vector<uint8_t> set(w.W, 0);
     out.clear();
-    const int16_t* g = c->h_grid.data();
+    const int16_t* g = w.h_grid.data();
     for (int z = 0; z < Z; z++)
         for (int y = 0; y < Y; y++)
             for (int x = 0; x < X; x++) {
@@ -552,18 +413,232 @@ static int build_list(Context* c, std::vector<int16_t>& out) {
         if (!set[(size_t)u[0] + (size_t)X * ((size_t)u[1] + (size_t)Y * u[2])]) out.insert(out.end(), u, u + 4);
     }
     c->specials.clear();
+}
+
+}  // namespace lumrad
+
+using namespace lumrad;
+
+extern "C" {
+
+const char* lumrad_last_error(void) { return g_error.c_str(); }
+
+int lumrad_create(const LumRadSettings* s, LumRadContext* out) {
+    if (!s || !out) return fail(LUMRAD_EINVAL, "null argument");
+    *out = nullptr;
+    for (int i = 0; i < 3; i++)
+        if (s->world_size[i] < 1 || s->world_size[i] > 2047)
+            return fail(LUMRAD_EINVAL, "world_size must be in [1, 2047] per axis");
+    const uint64_t W = (uint64_t)s->world_size[0] * s->world_size[1] * s->world_size[2];
+    if (W >= (1ull << 31)) return fail(LUMRAD_EINVAL, "world has too many blocks (>= 2^31)");
+    if (s->max_block_types < 1 || s->max_block_types > LUMRAD_MAX_BLOCK_SLOTS)
+        return fail(LUMRAD_EINVAL, "max_block_types must be in [1, 4096]");
+    if (s->precision < 0 || s->precision > 2) return fail(LUMRAD_EINVAL, "unknown precision");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(LUMRAD_EDEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (s->device < 0 || s->device >= ndev) return fail(LUMRAD_EINVAL, "device ordinal out of range");
+
+    Context* c = new Context();
+    c->device = s->device;
+    auto attempt = [&]() -> int {
+        LUMRAD_TRY(cudaSetDevice(c->device));
+        LUMRAD_TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
+        LUMRAD_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        LUMRAD_TRY(cudaEventCreate(&c->ev_start));
+        LUMRAD_TRY(cudaEventCreate(&c->ev_end));
+        LUMRAD_TRY(cudaEventCreateWithFlags(&c->ev_req, cudaEventDisableTiming));
+        for (int i = 0; i < Context::kRing; i++) {
+            LUMRAD_TRY(cudaEventCreate(&c->ring0[i]));
+            LUMRAD_TRY(cudaEventCreate(&c->ring1[i]));
+        }
+        LUMRAD_TRY(cudaMalloc(&c->d_queue, 2 * sizeof(unsigned long long)));
+        LUMRAD_TRY(cudaMalloc(&c->d_error, sizeof(int)));
+        LUMRAD_TRY(cudaMemsetAsync(c->d_queue, 0, 2 * sizeof(unsigned long long), c->stream));
+        LUMRAD_TRY(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream));
+        int rc = c->world.init(s->world_size[0], s->world_size[1], s->world_size[2], s->max_block_types,
+                               s->precision, c->stream);
+        if (rc) return rc;
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+        return LUMRAD_OK;
+    };
+    const int rc = attempt();
+    if (rc) {
+        const std::string msg = g_error;
+        c->release();
+        delete c;
+        return fail(rc, msg);
+    }
+    *out = c;
+    return LUMRAD_OK;
+}
+
+void lumrad_destroy(LumRadContext ctx) {
+    Context* c = as_ctx(ctx);
+    if (!c) return;
+    c->release();
+    delete c;
+}
+
+int lumrad_synchronize(LumRadContext ctx) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    return c->check_error();
+}
+
+int lumrad_load_world(LumRadContext ctx, const int16_t* blocks) {
+    Context* c = as_ctx(ctx);
+    if (!c || !blocks) return fail(LUMRAD_EINVAL, "null argument");
+    std::memcpy(c->world.h_grid.data(), blocks, c->world.W * sizeof(int16_t));
+    c->world.grid_dirty = true;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    return c->world.sync_inputs(c->stream);
+}
+
+int lumrad_set_world_block(LumRadContext ctx, int x, int y, int z, int16_t block) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    DeviceWorld& w = c->world;
+    if (x < 0 || y < 0 || z < 0 || x >= w.X || y >= w.Y || z >= w.Z)
+        return fail(LUMRAD_EINVAL, "block coordinate out of the world");
+    w.h_grid[(size_t)x + (size_t)w.X * ((size_t)y + (size_t)w.Y * z)] = block;
+    w.grid_dirty = true;   // uploaded before the next pass, as exec_copies does every frame
+    return LUMRAD_OK;
+}
+
+int lumrad_get_world_block(LumRadContext ctx, int x, int y, int z, int16_t* block) {
+    Context* c = as_ctx(ctx);
+    if (!c || !block) return fail(LUMRAD_EINVAL, "null argument");
+    const DeviceWorld& w = c->world;
+    if (x < 0 || y < 0 || z < 0 || x >= w.X || y >= w.Y || z >= w.Z)
+        return fail(LUMRAD_EINVAL, "block coordinate out of the world");
+    *block = w.h_grid[(size_t)x + (size_t)w.X * ((size_t)y + (size_t)w.Y * z)];
+    return LUMRAD_OK;
+}
+
+int lumrad_load_block(LumRadContext ctx, int16_t block, const uint8_t* voxels) {
+    Context* c = as_ctx(ctx);
+    if (!c || !voxels) return fail(LUMRAD_EINVAL, "null argument");
+    DeviceWorld& w = c->world;
+    if (block < 0 || block >= w.n_slots) return fail(LUMRAD_EINVAL, "block id outside the palette slots");
+    // BlockVoxels[x][y][z] (z fastest) -> x-fastest slot, as updateBlockPalette repacks it
+    uint8_t* dst = w.h_pal.data() + (size_t)block * 4096;
+    for (int x = 0; x < 16; x++)
+        for (int y = 0; y < 16; y++)
+            for (int z = 0; z < 16; z++) dst[x + 16 * y + 256 * z] = voxels[(x * 16 + y) * 16 + z];
+    return LUMRAD_OK;
+}
+
+int lumrad_upload_block_palette(LumRadContext ctx) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    DeviceWorld& w = c->world;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    w.h_pal_dev = w.h_pal;
+    LUMRAD_TRY(cudaMemcpyAsync(w.d_pal, w.h_pal_dev.data(), w.h_pal_dev.size(), cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    w.compact_dirty = true;
+    return LUMRAD_OK;
+}
+
+int lumrad_load_materials(LumRadContext ctx, const LumRadMaterial* materials) {
+    Context* c = as_ctx(ctx);
+    if (!c || !materials) return fail(LUMRAD_EINVAL, "null argument");
+    std::memcpy(c->world.h_mats.data(), materials, LUMRAD_MATERIALS * sizeof(LumRadMaterial));
+    return LUMRAD_OK;
+}
+
+int lumrad_upload_material_palette(LumRadContext ctx) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    std::vector<float4> m(LUMRAD_MATERIALS);
+    const auto& hm = c->world.h_mats;
+    for (int i = 0; i < LUMRAD_MATERIALS; i++) m[i] = make_float4(hm[i].color[0], hm[i].color[1], hm[i].color[2], hm[i].emmit);
+    LUMRAD_TRY(cudaMemcpyAsync(c->world.d_mats, m.data(), m.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    return LUMRAD_OK;
+}
+
+int lumrad_get_radiance(LumRadContext ctx, float* rgb) {
+    Context* c = as_ctx(ctx);
+    if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    DeviceWorld& w = c->world;
+    if (w.precision == LUMRAD_PRECISION_FP32) {
+        std::vector<float4> h(w.W);
+        LUMRAD_TRY(cudaMemcpyAsync(h.data(), w.d_rad[w.cur], w.W * 16, cudaMemcpyDeviceToHost, c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < w.W; i++) {
+            rgb[3 * i] = h[i].x; rgb[3 * i + 1] = h[i].y; rgb[3 * i + 2] = h[i].z;
+        }
+    } else {
+        std::vector<uint16_t> h(w.W * 4);
+        LUMRAD_TRY(cudaMemcpyAsync(h.data(), w.d_rad[w.cur], w.W * 8, cudaMemcpyDeviceToHost, c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < w.W; i++)
+            for (int k = 0; k < 3; k++) {
+                const uint16_t bits = h[4 * i + k];
+                float v;
+                if (w.precision == LUMRAD_PRECISION_FP16) {
+                    __half_raw r;
+                    r.x = bits;
+                    v = __half2float(__half(r));
+                } else {
+                    const uint32_t u = (uint32_t)bits << 16;
+                    std::memcpy(&v, &u, 4);
+                }
+                rgb[3 * i + k] = v;
+            }
+    }
+    return c->check_error();
+}
+
+int lumrad_set_radiance(LumRadContext ctx, const float* rgb) {
+    Context* c = as_ctx(ctx);
+    if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    DeviceWorld& w = c->world;
+    if (w.precision == LUMRAD_PRECISION_FP32) {
+        std::vector<float4> h(w.W);
+        for (size_t i = 0; i < w.W; i++)
+            h[i] = make_float4(unorm_clamp(rgb[3 * i]), unorm_clamp(rgb[3 * i + 1]), unorm_clamp(rgb[3 * i + 2]), 1.0f);
+        LUMRAD_TRY(cudaMemcpyAsync(w.d_rad[w.cur], h.data(), w.W * 16, cudaMemcpyHostToDevice, c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    } else {
+        std::vector<uint16_t> h(w.W * 4);
+        for (size_t i = 0; i < w.W; i++)
+            for (int k = 0; k < 4; k++) {
+                const float v = k < 3 ? unorm_clamp(rgb[3 * i + k]) : 1.0f;
+                if (w.precision == LUMRAD_PRECISION_FP16) h[4 * i + k] = __half_raw(__float2half_rn(v)).x;
+                else h[4 * i + k] = __nv_bfloat16_raw(__float2bfloat16_rn(v)).x;
+            }
+        LUMRAD_TRY(cudaMemcpyAsync(w.d_rad[w.cur], h.data(), w.W * 8, cudaMemcpyHostToDevice, c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    }
+    return LUMRAD_OK;
+}
+
+int lumrad_request_update(LumRadContext ctx, int x, int y, int z) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    const DeviceWorld& w = c->world;
+    if (x < 0 || y < 0 || z < 0 || x >= w.X || y >= w.Y || z >= w.Z) return fail(LUMRAD_EINVAL, "request outside the world");
+    c->specials.insert(c->specials.end(), {(int16_t)x, (int16_t)y, (int16_t)z, 0});
     return LUMRAD_OK;
 }
 
 int lumrad_build_update_list(LumRadContext ctx, int16_t* out, int cap, int* n) {
     Context* c = as_ctx(ctx);
     if (!c || !n || (cap > 0 && !out)) return fail(LUMRAD_EINVAL, "null argument");
-    std::vector<int16_t> specials = c->specials;   // building the list alone keeps the queue
+    const std::vector<int16_t> specials = c->specials;   // building the list alone keeps the queue
     std::vector<int16_t> list;
     build_list(c, list);
     c->specials = specials;
     const int total = (int)(list.size() / 4);
-    std::memcpy(out, list.data(), (size_t)std::min(total, std::max(cap, 0)) * 4 * sizeof(int16_t));
+    if (cap > 0) std::memcpy(out, list.data(), (size_t)std::min(total, cap) * 4 * sizeof(int16_t));
     *n = total;
     return LUMRAD_OK;
 }
@@ -571,30 +646,30 @@ int lumrad_build_update_list(LumRadContext ctx, int16_t* out, int cap, int* n) {
 int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
     Context* c = as_ctx(ctx);
     if (!c) return fail(LUMRAD_EINVAL, "null context");
-    int rc = check_params(c, params);
+    int rc = check_params(params);
     if (rc) return rc;
-    if ((rc = set_device(c))) return rc;
+    LUMRAD_TRY(cudaSetDevice(c->device));
     if (params->size == 0 && c->have_pass) {
-        LUMRAD_CUDA(cudaEventSynchronize(c->ev_end));
-        LUMRAD_CUDA(cudaEventElapsedTime(&c->last_ms, c->ev_start, c->ev_end));
+        LUMRAD_TRY(cudaEventSynchronize(c->ev_end));
+        LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ev_start, c->ev_end));
     }
     std::vector<int16_t> list;
     build_list(c, list);
     const size_t n = list.size() / 4;
-    if ((rc = stage_requests(c, list.data(), n))) return rc;
-    return run_pass(c, c->d_req, (int)n, params);
+    if ((rc = c->stage_requests(list.data(), n))) return rc;
+    return c->run_pass(c->d_req, (int)n, params);
 }
 
 int lumrad_radiance_pass(LumRadContext ctx, const int16_t* requests, int n, const LumRadPassParams* params) {
     Context* c = as_ctx(ctx);
     if (!c) return fail(LUMRAD_EINVAL, "null context");
     if (n < 0 || (n > 0 && !requests)) return fail(LUMRAD_EINVAL, "bad request list");
-    int rc = check_params(c, params);
+    int rc = check_params(params);
     if (rc) return rc;
     if (params->size == 0) return fail(LUMRAD_EINVAL, "size 0 (adaptive) is only valid for lumrad_update_radiance");
-    if ((rc = set_device(c))) return rc;
-    if ((rc = stage_requests(c, requests, (size_t)n))) return rc;
-    return run_pass(c, c->d_req, n, params);
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    if ((rc = c->stage_requests(requests, (size_t)n))) return rc;
+    return c->run_pass(c->d_req, n, params);
 }
 
 int lumrad_radiance_pass_i8(LumRadContext ctx, const int8_t* requests, int n, const LumRadPassParams* params) {
@@ -608,16 +683,15 @@ int lumrad_upload_requests(LumRadContext ctx, int slot, const int16_t* requests,
     Context* c = as_ctx(ctx);
     if (!c) return fail(LUMRAD_EINVAL, "null context");
     if (n < 0 || (n > 0 && !requests) || slot < 0) return fail(LUMRAD_EINVAL, "bad request list");
-    int rc = set_device(c);
-    if (rc) return rc;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     auto& r = c->resident[slot];
-    if (r.ptr) cudaFree(r.ptr);
+    cudaFree(r.ptr);
     r.ptr = nullptr;
     r.n = 0;
-    LUMRAD_CUDA(cudaMalloc(&r.ptr, std::max(n, 1) * sizeof(short4)));
-    if (n > 0)
-        LUMRAD_CUDA(cudaMemcpyAsync(r.ptr, requests, (size_t)n * sizeof(short4), cudaMemcpyHostToDevice, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
+    LUMRAD_TRY(cudaMalloc(&r.ptr, std::max(n, 1) * sizeof(short4)));
+    if (n > 0) LUMRAD_TRY(cudaMemcpyAsync(r.ptr, requests, (size_t)n * sizeof(short4), cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     r.n = n;
     return LUMRAD_OK;
 }
@@ -627,46 +701,43 @@ int lumrad_radiance_pass_resident(LumRadContext ctx, int slot, const LumRadPassP
     if (!c) return fail(LUMRAD_EINVAL, "null context");
     auto it = c->resident.find(slot);
     if (it == c->resident.end()) return fail(LUMRAD_EINVAL, "no request list uploaded in this slot");
-    int rc = check_params(c, params);
+    int rc = check_params(params);
     if (rc) return rc;
     if (params->size == 0) return fail(LUMRAD_EINVAL, "size 0 (adaptive) is only valid for lumrad_update_radiance");
-    if ((rc = set_device(c))) return rc;
-    return run_pass(c, it->second.ptr, it->second.n, params);
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    return c->run_pass(it->second.ptr, it->second.n, params);
 }
 
 int lumrad_get_hits(LumRadContext ctx, LumRadHit* out, size_t cap, size_t* n) {
     Context* c = as_ctx(ctx);
     if (!c || !n || (cap > 0 && !out)) return fail(LUMRAD_EINVAL, "null argument");
-    if (!c->have_pass || !c->hits_recorded) {
+    if (!c->have_pass || !c->world.hits_recorded) {
         *n = 0;
         return fail(LUMRAD_ESTATE, "the last pass did not record hits");
     }
-    int rc = set_device(c);
-    if (rc) return rc;
-    const size_t k = std::min(cap, c->hits_n);
-    if (k > 0)
-        LUMRAD_CUDA(cudaMemcpyAsync(out, c->d_hits, k * sizeof(LumRadHit), cudaMemcpyDeviceToHost, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
-    *n = c->hits_n;
-    return LUMRAD_OK;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    const size_t k = std::min(cap, c->world.hits_n);
+    if (k > 0) LUMRAD_TRY(cudaMemcpyAsync(out, c->world.d_hits, k * sizeof(LumRadHit), cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    *n = c->world.hits_n;
+    return c->check_error();
 }
 
 int lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out) {
     Context* c = as_ctx(ctx);
     if (!c || !out) return fail(LUMRAD_EINVAL, "null argument");
     if (!c->have_pass) return fail(LUMRAD_ESTATE, "no pass has run");
-    int rc = set_device(c);
-    if (rc) return rc;
+    LUMRAD_TRY(cudaSetDevice(c->device));
     unsigned long long h[2];
-    LUMRAD_CUDA(cudaMemcpyAsync(h, c->d_counters, sizeof h, cudaMemcpyDeviceToHost, c->stream));
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(h, c->world.d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     float ms = 0.0f;
-    LUMRAD_CUDA(cudaEventElapsedTime(&ms, c->ev_start, c->ev_end));
+    LUMRAD_TRY(cudaEventElapsedTime(&ms, c->ev_start, c->ev_end));
     *out = c->last;
     out->steps = h[0];
     out->hits = h[1];
     out->gpu_ms = ms;
-    return LUMRAD_OK;
+    return c->check_error();
 }
 
 int lumrad_get_stream(LumRadContext ctx, void** stream) {
@@ -679,18 +750,17 @@ int lumrad_get_stream(LumRadContext ctx, void** stream) {
 int lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n) {
     Context* c = as_ctx(ctx);
     if (!c || !n || (cap > 0 && !ms)) return fail(LUMRAD_EINVAL, "null argument");
-    int rc = set_device(c);
-    if (rc) return rc;
-    LUMRAD_CUDA(cudaStreamSynchronize(c->stream));
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     const long long avail = std::min<long long>(c->n_passes, Context::kRing);
     const int k = (int)std::min<long long>(avail, std::max(cap, 0));
     for (int i = 0; i < k; i++) {
         const long long pass = c->n_passes - k + i;
         const int slot = (int)(pass % Context::kRing);
-        LUMRAD_CUDA(cudaEventElapsedTime(&ms[i], c->ring0[slot], c->ring1[slot]));
+        LUMRAD_TRY(cudaEventElapsedTime(&ms[i], c->ring0[slot], c->ring1[slot]));
     }
     *n = k;
-    return LUMRAD_OK;
+    return c->check_error();
 }
 
 int lumrad_direction_table(int rays_per_probe, float* xyz) {

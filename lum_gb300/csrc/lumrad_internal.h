@@ -6,44 +6,64 @@
 
 namespace lumrad {
 
-// Rays per warp pool: a warp sets up, marches and reduces this many rays at a time.
-constexpr int kPool = 128;
 // Warps per CTA of the pass kernel.
 constexpr int kWarps = 8;
-// Shared memory per warp: origin, direction, 1/direction (float4 each) + fraction + info.
-constexpr int kSmemPerWarp = kPool * (3 * 16 + 4 + 4);
+// A task is one 32-ray subgroup of one probe; a warp keeps two tasks in flight.
+constexpr int kTaskRays = 32;
+constexpr int kRing = 2;
 
-// One resident world as the kernels see it (all pointers are device pointers).
-struct WorldView {
-    int X, Y, Z;              // blocks per axis
-    int n_slots;              // palette slots present on the device
-    int slot0_empty;          // 1 if palette slot 0 is all zero (lets air steps skip a load)
-    const int16_t* grid;      // X*Y*Z block ids, x-fastest
-    const uint8_t* pal;       // n_slots * 4096 voxels: voxel (x,y,z) at x + 16*y + 256*z
-    const float4* mats;       // 256 x (r, g, b, emission)
-};
-
-// One pass over one world.
-struct PassArgs {
-    WorldView w;
-    const void* prev;         // radiance volume read (storage type per precision)
-    void* next;               // radiance volume written (a copy of prev before the pass)
-    const short4* req;        // update list (x, y, z, w)
-    int n_groups;             // workgroups: n_requests / size
-    int size, shift;          // request r of group g is g*size + shift
-    int R;                    // rays per probe (multiple of 32)
-    int probes_per_unit;      // probes per warp work unit: kPool/R (>=1)
+// One world's pass as the kernel sees it (all pointers are device pointers).
+//
+// The coarse march and the refine DDA only ask "is this block air" and "is this voxel solid",
+// so they read a compact copy of the world: every distinct block id is renumbered (0 stays 0)
+// into uint8 (or uint16) compact ids, and each compact id has a 4096-bit voxel occupancy mask
+// (voxel (x,y,z) -> bit x + 16y + 256z).  Voxel values (material ids) and the original block ids
+// are read from the int16 grid and the uint8 palette only where a value is needed.
+struct WorldPass {
+    int X, Y, Z;                 // blocks per axis
+    int cgrid_wide;              // 0: uint8 compact ids, 1: uint16
+    const void* cgrid;           // X*Y*Z compact ids, x-fastest
+    const uint32_t* cbits;       // 128 words per compact id
+    const int16_t* grid;         // X*Y*Z block ids
+    const uint8_t* pal;          // n_slots * 4096 voxels, voxel (x,y,z) at x + 16y + 256z
+    int n_slots;
+    int pad0;
+    const float4* mats;          // 256 x (r, g, b, emission)
+    const void* prev;            // radiance read
+    void* next;                  // radiance written (holds a copy of prev before the pass)
+    const short4* req;           // update list (x, y, z, w)
+    int n_groups, size, shift;   // workgroup g updates request g*size + shift
+    int R;                       // rays per probe, multiple of 32
     float max_dist;
-    int max_steps;            // 2*max_dist + 2
+    int max_steps;               // 2*max_dist + 2
     float alpha, one_minus_alpha;
-    uint32_t seed;            // time seed
-    const float4* dirs;       // R spherical-Fibonacci directions
-    LumRadHit* hits;          // per-ray records or nullptr
-    unsigned long long* counters;  // [0] steps, [1] hits, or nullptr
+    uint32_t seed;               // time seed
+    float inv_dim[3];            // 1/X, 1/Y, 1/Z where that is exact (power of two), else 0
+    float inv_nsub;              // 1/(R/32) where exact, else 0
+    const float4* dirs;          // R spherical-Fibonacci directions
+    LumRadHit* hits;             // per-ray records, or nullptr
+    float4* scratch;             // n_groups * R/32 subgroup means (used when R > 32)
+    int* probe_count;            // n_groups finished-subgroup counters, zero between launches
+    unsigned long long* stats;   // [0] lookups, [1] hits (accumulated)
+    long long task_begin;        // first task of this world in the launch
+    long long n_tasks;           // n_groups * R/32
 };
 
-// Launches one pass on `stream`; returns a CUDA error code.
-cudaError_t launch_radiance_pass(const PassArgs& args, int precision, bool record, bool stats,
-                                 int num_sms, cudaStream_t stream);
+struct LaunchArgs {
+    WorldPass single;            // the world when n_worlds == 1 (passed by value)
+    const WorldPass* worlds;     // device array when n_worlds > 1
+    int n_worlds;
+    int total_warps;             // warps in the grid (set by the launcher)
+    long long n_tasks;
+    unsigned long long* queue;   // [0] next task, [1] warps finished; zero between launches
+    int* error;                  // set non-zero if a warp's scheduler stops making progress
+};
+
+// Launches one pass over `n_worlds` worlds (descriptors already on the device) on `stream`.
+cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms,
+                            cudaStream_t stream);
+
+// Number of CTAs launch_radiance uses on a device with `num_sms` SMs.
+int radiance_grid_size(int precision, bool record, int num_sms);
 
 }  // namespace lumrad

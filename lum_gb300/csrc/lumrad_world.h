@@ -1,0 +1,117 @@
+// lumrad_world.h — host-side state of a resident world and of a C-ABI context.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "lumrad_internal.h"
+
+namespace lumrad {
+
+extern thread_local std::string g_error;
+int fail(int code, const std::string& msg);
+void fibonacci_table(int n, float* xyz);
+
+#define LUMRAD_TRY(expr)                                                                            \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return ::lumrad::fail(e_ == cudaErrorMemoryAllocation ? LUMRAD_ENOMEM : LUMRAD_EDEVICE, \
+                                  std::string(#expr) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+// One world resident on the device (grid, compact copy, palettes, materials, radiance x2) and the
+// per-pass buffers that grow on demand (scratch, counters, hit records, direction tables).
+struct DeviceWorld {
+    int X = 0, Y = 0, Z = 0;
+    size_t W = 0;
+    int n_slots = 0;
+    int precision = 0;
+    size_t rad_stride = 16;
+
+    std::vector<int16_t> h_grid;          // the world as the caller set it
+    std::vector<uint8_t> h_pal;           // staged palette (lumrad_load_block)
+    std::vector<uint8_t> h_pal_dev;       // palette as uploaded
+    std::vector<LumRadMaterial> h_mats;
+    std::vector<uint8_t> h_cgrid;         // compact ids (uint8 or uint16)
+    std::vector<uint32_t> h_cbits;
+    bool grid_dirty = true;
+    bool compact_dirty = true;
+    int n_compact = 0;
+    bool cgrid_wide = false;
+
+    int16_t* d_grid = nullptr;
+    void* d_cgrid = nullptr;
+    uint32_t* d_cbits = nullptr;
+    size_t cbits_cap = 0;
+    uint8_t* d_pal = nullptr;
+    float4* d_mats = nullptr;
+    void* d_rad[2] = {nullptr, nullptr};
+    int cur = 0;                          // rad[cur] holds the current volume
+    float4* d_scratch = nullptr;
+    size_t scratch_cap = 0;
+    int* d_probe_count = nullptr;
+    size_t count_cap = 0;
+    unsigned long long* d_stats = nullptr;
+    LumRadHit* d_hits = nullptr;
+    size_t hits_cap = 0, hits_n = 0;
+    bool hits_recorded = false;
+    std::map<int, float4*> d_dirs;
+
+    int init(int X, int Y, int Z, int slots, int precision, cudaStream_t stream);
+    void release();
+    void build_compact();
+    int sync_inputs(cudaStream_t stream);
+    int ensure_dirs(int R, cudaStream_t stream, const float4** out);
+    int ensure_scratch(size_t groups, int R);
+    int ensure_hits(size_t n);
+    int prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, WorldPass* out);
+};
+
+// A LumRadContext: one world plus its stream, events and request staging.
+struct Context {
+    static constexpr int kRing = 64;      // kernel-time history
+    DeviceWorld world;
+    int device = 0;
+    int num_sms = 0;
+    std::vector<int16_t> specials;        // queued (x,y,z,w)
+    short4* d_req = nullptr;
+    size_t req_cap = 0;
+    int16_t* h_req_pinned = nullptr;
+    size_t h_req_cap = 0;
+    struct Resident { short4* ptr = nullptr; int n = 0; };
+    std::map<int, Resident> resident;
+    unsigned long long* d_queue = nullptr;
+    int* d_error = nullptr;
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_req = nullptr;
+    cudaEvent_t ring0[kRing] = {}, ring1[kRing] = {};
+    long long n_passes = 0;
+    bool have_pass = false;
+    bool req_copy_pending = false;
+    LumRadPassStats last{};
+
+    // adaptive time slicing state (internal_render.cpp:1190-1203)
+    int frame = 0;
+    int magic_size = 1;
+    float last_ms = 0.0f;
+
+    int ensure_req_capacity(size_t n);
+    int stage_requests(const int16_t* req, size_t n);
+    int run_pass(const short4* d_req, int n, const LumRadPassParams* p);
+    int check_error();
+    void release();
+};
+
+Context* as_ctx(LumRadContext c);
+int check_params(const LumRadPassParams* p);
+void build_list(Context* c, std::vector<int16_t>& out);
+
+}  // namespace lumrad

@@ -1,20 +1,28 @@
-// radiance_pass.cu — sm_103a kernels of the per-block radiance update.
+// radiance_pass.cu — sm_103a kernel of the per-block radiance update.
 //
 // Restates shaders/radiance.comp (main :361-413, trace_ray :316-346, CastRay_fast :183-291,
-// GetVoxel :121-143, sample_radiance :161-166, store_probe :349-354, hash33 :51-66) for one
-// warp per work unit instead of one 64-invocation workgroup per probe:
+// GetVoxel :121-143, sample_radiance :161-166, store_probe :349-354, hash33 :51-66).
 //
-//   setup    all 32 lanes build the rays of a pool (kPool rays, in lock step) into shared memory;
-//   march    a flat loop in which every lane advances its ray one coarse step per iteration and,
-//            when the ray ends, records (fraction, voxel) and takes the next ray of the pool —
-//            long and short rays share the warp without waiting for one another;
-//   finalize in lock step again: refine DDA, material, trilinear radiance fetch, shading; then
-//            the 32 lanes of each subgroup reduce by xor-butterfly and the last subgroup of a
-//            probe blends and stores it.
+// Work decomposition.  A task is one 32-ray subgroup of one probe (the unit the shader sums
+// with subgroupAdd).  Persistent warps take tasks from a queue in guided chunks (large early,
+// single tasks at the end), so the last tasks spread over all SMs.  A warp keeps two tasks in
+// flight and runs three phases:
+//   setup     lock step, one ray per lane: hash seeds, direction, origin (into shared memory);
+//   march     a flat loop: every lane advances its ray one coarse step per iteration; a lane
+//             whose ray ends stores (fraction, info) and takes the next unissued ray of the two
+//             tasks, so short and long rays share the warp;
+//   finalize  lock step when a task's 32 rays are done: refine DDA, material, trilinear fetch
+//             of the previous radiance, shading, xor-butterfly sum.  For R = 32 the probe is
+//             blended and stored at once; otherwise the subgroup mean goes to scratch and the
+//             task that completes a probe's last subgroup sums the means in subgroup order.
 //
-// All float arithmetic uses round-to-nearest intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn,
-// __fsqrt_rn), which the compiler never fuses into FMA, in the order the shader evaluates it,
-// so hit records are bit-exact and radiance bit-identical to the FP32 CPU restatement.
+// Exactness.  All float arithmetic uses round-to-nearest intrinsics (__fadd_rn, __fmul_rn,
+// __fdiv_rn, __frcp_rn, __fsqrt_rn), which are never fused into FMA, in the shader's order.
+// Divisions by powers of two are multiplications by the exact reciprocal (identical results).
+// Hit records are bit-exact and FP32 radiance bit-identical to the CPU restatement.
+//
+// Memory.  The march and refine tests read the compact world (uint8 ids + occupancy bits,
+// L1-resident); the two tasks of a warp use 2 KiB of shared memory, leaving L1 to the data.
 
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
@@ -31,18 +39,18 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
-// GLSL min/max definitions (y < x ? y : x, x < y ? y : x): identical NaN and signed-zero
-// behaviour on every implementation.
+// x / d where `inv` is 1/d if that is exact (d a power of two), else 0
+__device__ __forceinline__ float fdiv_by(float x, float d, float inv) { return inv != 0.0f ? fmul(x, inv) : fdiv(x, d); }
+// GLSL min/max definitions: identical NaN and signed-zero behaviour everywhere.
 __device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
 __device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
 // float -> int toward zero; PTX cvt.rzi saturates and maps NaN to 0.
 __device__ __forceinline__ int f2i(float f) { return __float2int_rz(f); }
-// SPIR-V OpSMod (sign of the divisor) for a positive divisor.
+// SPIR-V OpSMod for a positive divisor.
 __device__ __forceinline__ int smod(int a, int b) {
     int r = a % b;
     return (r < 0) ? r + b : r;
 }
-
 // Hit records report every NaN as the canonical quiet NaN 0x7FC00000.
 __device__ __forceinline__ float canon_nan(float f) { return f == f ? f : __int_as_float(0x7FC00000); }
 
@@ -53,9 +61,7 @@ struct StoreF32 {
         float4 v = __ldg(p + i);
         return make_float3(v.x, v.y, v.z);
     }
-    static __device__ __forceinline__ void store(T* p, int i, float3 v) {
-        p[i] = make_float4(v.x, v.y, v.z, 1.0f);
-    }
+    static __device__ __forceinline__ void store(T* p, int i, float3 v) { p[i] = make_float4(v.x, v.y, v.z, 1.0f); }
 };
 struct StoreF16 {
     typedef uint2 T;   // (r,g) (b,1) as two half2
@@ -92,26 +98,47 @@ struct StoreBF16 {
     }
 };
 
-// ---------------------------------------------------------------- voxel lookup
-// GetVoxel + voxel_in_palette (radiance.comp:97-143) on integer voxel coordinates.
-// Block coordinate = ix/16 truncated (OpSDiv); voxel in block = ix mod 16 floored (OpSMod,
-// i.e. ix & 15).  The grid fetch is in range iff -15 <= ix < 16*X, and then ix/16 == max(ix,0)>>4.
-// Block id b addresses palette slot (b mod 64) + 64*(b/64): slot b for b >= 0, slot b+64 for
-// -63 <= b < 0, nothing (0) otherwise or past the loaded slots.
-__device__ __forceinline__ int fetch_voxel(const WorldView& w, int ix, int iy, int iz, int& block) {
+// ---------------------------------------------------------------- voxel lookups
+// GetVoxel (radiance.comp:121-143) on integer voxel coordinates.  Block coordinate = ix/16
+// truncated (OpSDiv); voxel in block = ix mod 16 floored (OpSMod) = ix & 15.  The grid fetch is
+// in range iff -15 <= ix < 16*X, and then ix/16 == max(ix,0) >> 4; out of range reads block 0.
+__device__ __forceinline__ bool grid_index(int X, int Y, int Z, int ix, int iy, int iz, int& idx) {
+    const bool in = (unsigned)ix + 15u < (unsigned)(16 * X + 15) && (unsigned)iy + 15u < (unsigned)(16 * Y + 15) &&
+                    (unsigned)iz + 15u < (unsigned)(16 * Z + 15);
+    idx = (max(ix, 0) >> 4) + X * ((max(iy, 0) >> 4) + Y * (max(iz, 0) >> 4));
+    return in;
+}
+
+// What the march and refine tests read of the current world (kept in registers).
+struct MarchView {
+    int X, Y, Z;
+    int wide;                     // compact ids are uint16
+    const uint8_t* cgrid;
+    const uint32_t* cbits;
+};
+
+// Compact lookup: compact id of the block (0 iff block id 0) and whether the voxel is solid.
+__device__ __forceinline__ bool solid_at(const MarchView& m, int ix, int iy, int iz, int& cid) {
+    int idx;
+    int c = 0;
+    if (grid_index(m.X, m.Y, m.Z, ix, iy, iz, idx))
+        c = m.wide ? (int)__ldg(reinterpret_cast<const uint16_t*>(m.cgrid) + idx) : (int)__ldg(m.cgrid + idx);
+    cid = c;
+    const uint32_t word = __ldg(m.cbits + ((c << 7) | ((iz & 15) << 3) | ((iy & 15) >> 1)));
+    return (word >> (((iy & 1) << 4) | (ix & 15))) & 1u;
+}
+
+// Original lookup (voxel value and block id): block id b addresses palette slot
+// (b mod 64) + 64*(b/64) (voxel_in_palette :105-110 on the 64x64-slot image): slot b for
+// b >= 0, slot b+64 for -63 <= b < 0, nothing past the loaded slots.
+__device__ __forceinline__ int voxel_value(const WorldPass& w, int ix, int iy, int iz, int& block) {
+    int idx;
     int b = 0;
-    if ((unsigned)ix + 15u < (unsigned)(16 * w.X + 15) &&
-        (unsigned)iy + 15u < (unsigned)(16 * w.Y + 15) &&
-        (unsigned)iz + 15u < (unsigned)(16 * w.Z + 15)) {
-        int bx = max(ix, 0) >> 4, by = max(iy, 0) >> 4, bz = max(iz, 0) >> 4;
-        b = __ldg(w.grid + (bx + w.X * (by + w.Y * bz)));
-    }
+    if (grid_index(w.X, w.Y, w.Z, ix, iy, iz, idx)) b = __ldg(w.grid + idx);
     block = b;
-    int v = 0;
-    int slot = b < 0 ? b + 64 : b;
-    if (b >= -63 && slot < w.n_slots && !(b == 0 && w.slot0_empty))
-        v = __ldg(w.pal + ((slot << 12) | ((iz & 15) << 8) | ((iy & 15) << 4) | (ix & 15)));
-    return v;
+    const int slot = b < 0 ? b + 64 : b;
+    if (b < -63 || slot >= w.n_slots) return 0;
+    return __ldg(w.pal + ((slot << 12) | ((iz & 15) << 8) | ((iy & 15) << 4) | (ix & 15)));
 }
 
 // ---------------------------------------------------------------- ray setup (:362-381)
@@ -119,133 +146,50 @@ __device__ __forceinline__ float3 hash33(uint32_t x, uint32_t y, uint32_t z) {
     const uint32_t k = 1103515245u;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        uint32_t nx = ((x >> 8) ^ y) * k;
-        uint32_t ny = ((y >> 8) ^ z) * k;
-        uint32_t nz = ((z >> 8) ^ x) * k;
+        const uint32_t nx = ((x >> 8) ^ y) * k;
+        const uint32_t ny = ((y >> 8) ^ z) * k;
+        const uint32_t nz = ((z >> 8) ^ x) * k;
         x = nx; y = ny; z = nz;
     }
     const float s = 2.3283064365386963e-10f;   // 1/float(0xffffffffu) = 2^-32
-    return make_float3(fmul(__uint2float_rn(x), s), fmul(__uint2float_rn(y), s),
-                       fmul(__uint2float_rn(z), s));
+    return make_float3(fmul(__uint2float_rn(x), s), fmul(__uint2float_rn(y), s), fmul(__uint2float_rn(z), s));
 }
 
 __device__ __forceinline__ float3 normalize3(float3 v) {
-    float dd = fadd(fadd(fmul(v.x, v.x), fmul(v.y, v.y)), fmul(v.z, v.z));
-    float s = fdiv(1.0f, __fsqrt_rn(dd));
+    const float dd = fadd(fadd(fmul(v.x, v.x), fmul(v.y, v.y)), fmul(v.z, v.z));
+    const float s = fdiv(1.0f, __fsqrt_rn(dd));
     return make_float3(fmul(v.x, s), fmul(v.y, s), fmul(v.z, s));
 }
 
-// Ray `gr` = g*R + r of the dispatch: origin, direction and 1/direction.
-__device__ __forceinline__ void setup_ray(const PassArgs& a, long long gr, float4& o4, float4& d4,
-                                          float4& inv4) {
-    const int g = (int)(gr / a.R);
-    const int r = (int)(gr - (long long)g * a.R);
-    const short4 q = __ldg(a.req + ((long long)g * a.size + a.shift));
-    uint32_t sx = (uint32_t)gr + a.seed, sy = a.seed, sz = a.seed;
-    float3 c = make_float3(fadd(fmul((float)q.x, 16.0f), 8.0f), fadd(fmul((float)q.y, 16.0f), 8.0f),
-                           fadd(fmul((float)q.z, 16.0f), 8.0f));
-    const float4 f = __ldg(a.dirs + r);
-    float3 r1 = hash33(sx, sy, sz);
+// Ray r of workgroup g (global invocation id gr = g*R + r): origin and direction.
+__device__ __forceinline__ void setup_ray(const WorldPass& w, long long gr, float3& o, float3& d) {
+    const int g = (int)(gr / w.R);
+    const int r = (int)(gr - (long long)g * w.R);
+    const short4 q = __ldg(w.req + ((long long)g * w.size + w.shift));
+    uint32_t sx = (uint32_t)gr + w.seed;
+    const uint32_t sy = w.seed, sz = w.seed;
+    const float3 c = make_float3(fadd(fmul((float)q.x, 16.0f), 8.0f), fadd(fmul((float)q.y, 16.0f), 8.0f),
+                                 fadd(fmul((float)q.z, 16.0f), 8.0f));
+    const float4 f = __ldg(w.dirs + r);
+    const float3 r1 = hash33(sx, sy, sz);
     sx++;
-    float3 j = make_float3(fmul(0.1f, fmul(fsub(r1.x, 0.5f), 2.0f)), fmul(0.1f, fmul(fsub(r1.y, 0.5f), 2.0f)),
-                           fmul(0.1f, fmul(fsub(r1.z, 0.5f), 2.0f)));
-    float3 d = normalize3(make_float3(fadd(f.x, j.x), fadd(f.y, j.y), fadd(f.z, j.z)));
-    float3 o = make_float3(fadd(c.x, fmul(d.x, 6.0f)), fadd(c.y, fmul(d.y, 6.0f)), fadd(c.z, fmul(d.z, 6.0f)));
-    float3 r2 = hash33(sx, sy, sz);
+    const float3 j = make_float3(fmul(0.1f, fmul(fsub(r1.x, 0.5f), 2.0f)), fmul(0.1f, fmul(fsub(r1.y, 0.5f), 2.0f)),
+                                 fmul(0.1f, fmul(fsub(r1.z, 0.5f), 2.0f)));
+    d = normalize3(make_float3(fadd(f.x, j.x), fadd(f.y, j.y), fadd(f.z, j.z)));
+    o = make_float3(fadd(c.x, fmul(d.x, 6.0f)), fadd(c.y, fmul(d.y, 6.0f)), fadd(c.z, fmul(d.z, 6.0f)));
+    const float3 r2 = hash33(sx, sy, sz);
     o = make_float3(fadd(o.x, fmul(fsub(r2.x, 0.5f), 2.0f)), fadd(o.y, fmul(fsub(r2.y, 0.5f), 2.0f)),
                     fadd(o.z, fmul(fsub(r2.z, 0.5f), 2.0f)));
     if (r & 1) d = make_float3(-d.x, -d.y, -d.z);
-    o4 = make_float4(o.x, o.y, o.z, 0.0f);
-    d4 = make_float4(d.x, d.y, d.z, 0.0f);
-    inv4 = make_float4(fdiv(1.0f, d.x), fdiv(1.0f, d.y), fdiv(1.0f, d.z), 0.0f);
 }
 
-// ---------------------------------------------------------------- coarse march (:198-244)
-// info word: bits 0-15 coarse steps, 16-23 coarse voxel, 24 hit, 25 step bound reached.
-template <bool RECORD>
-__device__ __forceinline__ void march_pool(const WorldView& w, float4* so, const float4* sd,
-                                           const float4* sinv, float* sfrac, uint32_t* sinfo,
-                                           int n, float max_dist, int max_steps, int lane) {
-    const float wx = fmul((float)w.X, 16.0f), wy = fmul((float)w.Y, 16.0f), wz = fmul((float)w.Z, 16.0f);
-    int my = lane;
-    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, ix_ = 0, iy_ = 0, iz_ = 0;
-    float cx = 0, cy = 0, cz = 0, frac = 0.0f;
-    int steps = 0;
-    bool active = my < n;
-    auto load = [&](int i) {
-        float4 o = so[i], d = sd[i], v = sinv[i];
-        ox = o.x; oy = o.y; oz = o.z;
-        dx = d.x; dy = d.y; dz = d.z;
-        ix_ = v.x; iy_ = v.y; iz_ = v.z;
-        cx = dx > 0.0f ? 16.0f : 0.0f;
-        cy = dy > 0.0f ? 16.0f : 0.0f;
-        cz = dz > 0.0f ? 16.0f : 0.0f;
-        frac = 0.0f;
-        steps = 0;
-    };
-    if (active) load(my);
-    int next_ray = 32;
-    int done = 0;
-    while (done < n) {
-        bool fin = false;
-        uint32_t info = 0;
-        int block = 0;
-        if (active) {
-            frac = fadd(frac, 0.5f);
-            steps++;
-            const float px = fadd(ox, fmul(dx, frac));
-            const float py = fadd(oy, fmul(dy, frac));
-            const float pz = fadd(oz, fmul(dz, frac));
-            const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
-            const int vox = fetch_voxel(w, ix, iy, iz, block);
-            if (block == 0) {
-                const float bx = fadd((float)((ix / 16) * 16), cx);
-                const float by = fadd((float)((iy / 16) * 16), cy);
-                const float bz = fadd((float)((iz / 16) * 16), cz);
-                const float tx = fadd(fmul(bx, ix_), fmul(-px, ix_));
-                const float ty = fadd(fmul(by, iy_), fmul(-py, iy_));
-                const float tz = fadd(fmul(bz, iz_), fmul(-pz, iz_));
-                float f = gmin(tx, gmin(ty, tz));
-                f = gmax(f, 0.01f);
-                frac = fadd(frac, f);
-            }
-            if (vox != 0) {
-                fin = true;
-                info = (uint32_t)steps | ((uint32_t)vox << 16) | (1u << 24);
-            } else if (px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz ||
-                       frac >= max_dist) {
-                fin = true;
-                info = (uint32_t)steps;
-            } else if (steps >= max_steps) {
-                fin = true;
-                info = (uint32_t)steps | (1u << 25);
-            }
-        }
-        const unsigned fm = __ballot_sync(kFull, fin);
-        if (fm) {
-            if (fin) {
-                sfrac[my] = frac;
-                sinfo[my] = info;
-                if (RECORD) so[my].w = __int_as_float(block);   // block id kept for the record
-                const int rank = __popc(fm & ((1u << lane) - 1u));
-                my = next_ray + rank;
-                active = my < n;
-                if (active) load(my);
-            }
-            next_ray += __popc(fm);
-            done += __popc(fm);
-        }
-    }
-}
-
-// ---------------------------------------------------------------- finalize (:246-291, :316-346)
+// ---------------------------------------------------------------- finalize (:246-291, :316-354)
 template <class Store>
-__device__ __forceinline__ float3 sample_trilinear(const PassArgs& a, float ux, float uy, float uz) {
-    const WorldView& w = a.w;
-    const typename Store::T* rad = reinterpret_cast<const typename Store::T*>(a.prev);
-    const float u[3] = {fsub(fmul(ux, (float)w.X), 0.5f), fsub(fmul(uy, (float)w.Y), 0.5f),
-                        fsub(fmul(uz, (float)w.Z), 0.5f)};
-    const int n[3] = {w.X, w.Y, w.Z};
+__device__ __forceinline__ float3 sample_trilinear(const WorldPass& w, float ux, float uy, float uz) {
+    const typename Store::T* rad = reinterpret_cast<const typename Store::T*>(w.prev);
+    const int X = w.X, Y = w.Y, Z = w.Z;
+    const float u[3] = {fsub(fmul(ux, (float)X), 0.5f), fsub(fmul(uy, (float)Y), 0.5f), fsub(fmul(uz, (float)Z), 0.5f)};
+    const int n[3] = {X, Y, Z};
     int i0[3], i1[3];
     float t[3];
 #pragma unroll
@@ -256,7 +200,7 @@ __device__ __forceinline__ float3 sample_trilinear(const PassArgs& a, float ux, 
         i0[c] = ii;
         i1[c] = (ii + 1 == n[c]) ? 0 : ii + 1;
     }
-    auto tex = [&](int x, int y, int z) { return Store::load(rad, x + w.X * (y + w.Y * z)); };
+    auto tex = [&](int x, int y, int z) { return Store::load(rad, x + X * (y + Y * z)); };
     auto lerp = [](float3 p, float3 q, float s) {
         const float r = fsub(1.0f, s);
         return make_float3(fadd(fmul(p.x, r), fmul(q.x, s)), fadd(fmul(p.y, r), fmul(q.y, s)),
@@ -269,11 +213,12 @@ __device__ __forceinline__ float3 sample_trilinear(const PassArgs& a, float ux, 
     return lerp(lerp(c00, c10, t[1]), lerp(c01, c11, t[1]), t[2]);
 }
 
+// info word of a marched ray: bits 0-15 coarse steps, 16-23 coarse voxel (RECORD only),
+// 24 hit, 25 stopped by the step bound.
 template <class Store, bool RECORD>
-__device__ __forceinline__ float3 finalize_ray(const PassArgs& a, float4 o4, float4 d4, float4 inv4,
-                                               float coarse_frac, uint32_t info, int block,
-                                               long long gr, uint32_t& lookups) {
-    const WorldView& w = a.w;
+__device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchView& mv, float3 o, float3 d,
+                                               float coarse_frac, uint32_t info, int block, long long gr,
+                                               uint32_t& lookups) {
     const bool hit = (info >> 24) & 1u;
     const int coarse_steps = info & 0xffff;
     lookups = coarse_steps;
@@ -291,23 +236,25 @@ __device__ __forceinline__ float3 finalize_ray(const PassArgs& a, float4 o4, flo
     }
     if (hit) {
         // refine DDA (radiance.comp:246-288)
-        const float bhx = fadd(o4.x, fmul(d4.x, fsub(coarse_frac, 1.5f)));
-        const float bhy = fadd(o4.y, fmul(d4.y, fsub(coarse_frac, 1.5f)));
-        const float bhz = fadd(o4.z, fmul(d4.z, fsub(coarse_frac, 1.5f)));
-        const int stx = d4.x > 0.0f ? 1 : -1, sty = d4.y > 0.0f ? 1 : -1, stz = d4.z > 0.0f ? 1 : -1;
-        const float c1x = fdiv(fsub(floorf(bhx), bhx), d4.x);
-        const float c1y = fdiv(fsub(floorf(bhy), bhy), d4.y);
-        const float c1z = fdiv(fsub(floorf(bhz), bhz), d4.z);
-        float tmx = gmax(c1x, fadd(c1x, inv4.x));
-        float tmy = gmax(c1y, fadd(c1y, inv4.y));
-        float tmz = gmax(c1z, fadd(c1z, inv4.z));
-        const float tdx = fabsf(inv4.x), tdy = fabsf(inv4.y), tdz = fabsf(inv4.z);
+        const float back = fsub(coarse_frac, 1.5f);
+        const float bhx = fadd(o.x, fmul(d.x, back));
+        const float bhy = fadd(o.y, fmul(d.y, back));
+        const float bhz = fadd(o.z, fmul(d.z, back));
+        const int stx = d.x > 0.0f ? 1 : -1, sty = d.y > 0.0f ? 1 : -1, stz = d.z > 0.0f ? 1 : -1;
+        const float ivx = __frcp_rn(d.x), ivy = __frcp_rn(d.y), ivz = __frcp_rn(d.z);
+        const float c1x = fdiv(fsub(floorf(bhx), bhx), d.x);
+        const float c1y = fdiv(fsub(floorf(bhy), bhy), d.y);
+        const float c1z = fdiv(fsub(floorf(bhz), bhz), d.z);
+        float tmx = gmax(c1x, fadd(c1x, ivx));
+        float tmy = gmax(c1y, fadd(c1y, ivy));
+        float tmz = gmax(c1z, fadd(c1z, ivz));
+        const float tdx = fabsf(ivx), tdy = fabsf(ivy), tdz = fabsf(ivz);   // 1/|d| == |1/d|
         int vx = f2i(bhx), vy = f2i(bhy), vz = f2i(bhz);
-        int blk;
-        int cur = fetch_voxel(w, vx, vy, vz, blk);
+        int cid;
+        bool solid = solid_at(mv, vx, vy, vz, cid);
         float fsx = 0.0f, fsy = 0.0f, fsz = 0.0f;
         int it = 0;
-        while (it < 5 && cur == 0) {
+        while (it < 5 && !solid) {
             const bool bx = (tmx <= tmy) && (tmx <= tmz);
             const bool by = (tmx >= tmy) && (tmy <= tmz);
             const bool bz = (tmz <= tmx) && (tmz <= tmy);
@@ -316,24 +263,25 @@ __device__ __forceinline__ float3 finalize_ray(const PassArgs& a, float4 o4, flo
             tmx = fadd(tmx, fmul(tdx, fsx));
             tmy = fadd(tmy, fmul(tdy, fsy));
             tmz = fadd(tmz, fmul(tdz, fsz));
-            cur = fetch_voxel(w, vx, vy, vz, blk);
+            solid = solid_at(mv, vx, vy, vz, cid);
             it++;
         }
         lookups += 1 + it;
+        int blk;
+        const int cur = solid ? voxel_value(w, vx, vy, vz, blk) : 0;
         const float nx = -fmul((float)stx, fsx), ny = -fmul((float)sty, fsy), nz = -fmul((float)stz, fsz);
-        const float fr = fadd(fadd(fmul(fsub(tmx, tdx), fsx), fmul(fsub(tmy, tdy), fsy)),
-                              fmul(fsub(tmz, tdz), fsz));
-        // material (GetMat :145-157) and sample_radiance (:161-166)
-        const float4 m = __ldg(a.w.mats + cur);
-        const float hx = fadd(o4.x, fmul(fr, d4.x));
-        const float hy = fadd(o4.y, fmul(fr, d4.y));
-        const float hz = fadd(o4.z, fmul(fr, d4.z));
-        const float bpx = fdiv(fadd(hx, fmul(nx, 16.0f)), 16.0f);
-        const float bpy = fdiv(fadd(hy, fmul(ny, 16.0f)), 16.0f);
-        const float bpz = fdiv(fadd(hz, fmul(nz, 16.0f)), 16.0f);
-        const float3 L = sample_trilinear<Store>(a, fdiv(fadd(bpx, 0.5f), (float)w.X),
-                                                 fdiv(fadd(bpy, 0.5f), (float)w.Y),
-                                                 fdiv(fadd(bpz, 0.5f), (float)w.Z));
+        const float fr = fadd(fadd(fmul(fsub(tmx, tdx), fsx), fmul(fsub(tmy, tdy), fsy)), fmul(fsub(tmz, tdz), fsz));
+        // material (GetMat :145-157) and sample_radiance (:161-166); /16 == *0.0625 exactly
+        const float4 m = __ldg(w.mats + cur);
+        const float hx = fadd(o.x, fmul(fr, d.x));
+        const float hy = fadd(o.y, fmul(fr, d.y));
+        const float hz = fadd(o.z, fmul(fr, d.z));
+        const float bpx = fmul(fadd(hx, fmul(nx, 16.0f)), 0.0625f);
+        const float bpy = fmul(fadd(hy, fmul(ny, 16.0f)), 0.0625f);
+        const float bpz = fmul(fadd(hz, fmul(nz, 16.0f)), 0.0625f);
+        const float3 L = sample_trilinear<Store>(w, fdiv_by(fadd(bpx, 0.5f), (float)w.X, w.inv_dim[0]),
+                                                 fdiv_by(fadd(bpy, 0.5f), (float)w.Y, w.inv_dim[1]),
+                                                 fdiv_by(fadd(bpz, 0.5f), (float)w.Z, w.inv_dim[2]));
         light = make_float3(fadd(0.0f, fadd(fmul(L.x, m.x), fmul(m.x, m.w))),
                             fadd(0.0f, fadd(fmul(L.y, m.y), fmul(m.y, m.w))),
                             fadd(0.0f, fadd(fmul(L.z, m.z), fmul(m.z, m.w))));
@@ -348,7 +296,7 @@ __device__ __forceinline__ float3 finalize_ray(const PassArgs& a, float4 o4, flo
     } else {
         // sky and sun (radiance.comp:334-343); globalLightDir = normalize(0.5, 0.5, -0.9)
         const float3 gl = normalize3(make_float3(0.5f, 0.5f, -0.9f));
-        const float g = -fadd(fadd(fmul(d4.x, gl.x), fmul(d4.y, gl.y)), fmul(d4.z, gl.z));
+        const float g = -fadd(fadd(fmul(d.x, gl.x), fmul(d.y, gl.y)), fmul(d.z, gl.z));
         light = make_float3(0.0f, 0.0f, 0.0f);
         if (g > 0.95f) {
             light.x = fadd(light.x, fmul(g, fmul(0.9f, 3.0f)));
@@ -359,7 +307,7 @@ __device__ __forceinline__ float3 finalize_ray(const PassArgs& a, float4 o4, flo
         light.y = fadd(light.y, fmul(0.81f, 0.1f));
         light.z = fadd(light.z, fmul(0.92f, 0.1f));
     }
-    if (RECORD) a.hits[gr] = rec;
+    if (RECORD) w.hits[gr] = rec;
     return light;
 }
 
@@ -375,134 +323,376 @@ __device__ __forceinline__ float3 butterfly_sum(float3 v) {
 
 __device__ __forceinline__ float clamp01(float v) { return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f; }
 
-// store_probe (radiance.comp:349-354)
+// store_probe (radiance.comp:349-354): blend the clamped old value with the mean, store clamped.
 template <class Store>
-__device__ __forceinline__ void store_probe(const PassArgs& a, int g, float3 acc) {
-    const short4 q = __ldg(a.req + ((long long)g * a.size + a.shift));
-    const WorldView& w = a.w;
+__device__ __forceinline__ void store_probe(const WorldPass& w, int g, float3 acc) {
+    const short4 q = __ldg(w.req + ((long long)g * w.size + w.shift));
     if (q.x < 0 || q.y < 0 || q.z < 0 || q.x >= w.X || q.y >= w.Y || q.z >= w.Z) return;
     const int idx = q.x + w.X * (q.y + w.Y * q.z);
-    float3 old = Store::load(reinterpret_cast<const typename Store::T*>(a.prev), idx);
+    float3 old = Store::load(reinterpret_cast<const typename Store::T*>(w.prev), idx);
     old.x = old.x < 0.0f ? 0.0f : old.x; old.x = 1.0f < old.x ? 1.0f : old.x;
     old.y = old.y < 0.0f ? 0.0f : old.y; old.y = 1.0f < old.y ? 1.0f : old.y;
     old.z = old.z < 0.0f ? 0.0f : old.z; old.z = 1.0f < old.z ? 1.0f : old.z;
-    float3 nv = make_float3(fadd(fmul(old.x, a.one_minus_alpha), fmul(acc.x, a.alpha)),
-                            fadd(fmul(old.y, a.one_minus_alpha), fmul(acc.y, a.alpha)),
-                            fadd(fmul(old.z, a.one_minus_alpha), fmul(acc.z, a.alpha)));
-    nv = make_float3(clamp01(nv.x), clamp01(nv.y), clamp01(nv.z));
-    Store::store(reinterpret_cast<typename Store::T*>(a.next), idx, nv);
+    const float3 nv = make_float3(clamp01(fadd(fmul(old.x, w.one_minus_alpha), fmul(acc.x, w.alpha))),
+                                  clamp01(fadd(fmul(old.y, w.one_minus_alpha), fmul(acc.y, w.alpha))),
+                                  clamp01(fadd(fmul(old.z, w.one_minus_alpha), fmul(acc.z, w.alpha))));
+    Store::store(reinterpret_cast<typename Store::T*>(w.next), idx, nv);
 }
 
-template <class Store, bool RECORD, bool STATS>
-__global__ void __launch_bounds__(kWarps * 32)
-radiance_pass_kernel(const __grid_constant__ PassArgs a) {
-    extern __shared__ float4 smem[];
+// Subgroup mean V = sum/32 of subgroup k of workgroup g is done.  R = 32: the probe's mean is V.
+// Otherwise V goes to scratch and the last of the probe's R/32 subgroups sums them in order
+// (radiance.comp:401-407), divides by R/32 and stores.  Lane 0 only.
+template <class Store>
+__device__ __forceinline__ void subgroup_done(const WorldPass& w, int g, int k, float3 v) {
+    const int nsub = w.R >> 5;
+    if (nsub == 1) {
+        store_probe<Store>(w, g, make_float3(fadd(0.0f, v.x), fadd(0.0f, v.y), fadd(0.0f, v.z)));
+        return;
+    }
+    float4* slots = w.scratch + (long long)g * nsub;
+    __stcg(slots + k, make_float4(v.x, v.y, v.z, 0.0f));
+    __threadfence();
+    const int prior = atomicAdd(w.probe_count + g, 1);
+    if (prior != nsub - 1) return;
+    __threadfence();
+    float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+    for (int j = 0; j < nsub; j++) {
+        const float4 s = __ldcg(slots + j);
+        acc = make_float3(fadd(acc.x, s.x), fadd(acc.y, s.y), fadd(acc.z, s.z));
+    }
+    const float fn = (float)nsub;
+    acc = make_float3(fdiv_by(acc.x, fn, w.inv_nsub), fdiv_by(acc.y, fn, w.inv_nsub), fdiv_by(acc.z, fn, w.inv_nsub));
+    store_probe<Store>(w, g, acc);
+    w.probe_count[g] = 0;   // ready for the next launch
+}
+
+// Warp-uniform state of the two in-flight tasks (scalars, so nothing lands in local memory).
+struct Slots {
+    int task0, task1;
+    int issued0, issued1, done0, done1;
+    bool valid0, valid1;
+    int older;
+    __device__ __forceinline__ int task(int s) const { return s ? task1 : task0; }
+    __device__ __forceinline__ int issued(int s) const { return s ? issued1 : issued0; }
+    __device__ __forceinline__ int done(int s) const { return s ? done1 : done0; }
+    __device__ __forceinline__ bool valid(int s) const { return s ? valid1 : valid0; }
+    __device__ __forceinline__ void add_issued(int s, int v) { if (s) issued1 += v; else issued0 += v; }
+    __device__ __forceinline__ void set_valid(int s, bool v) { if (s) valid1 = v; else valid0 = v; }
+    __device__ __forceinline__ void load(int s, int t) {
+        if (s) { task1 = t; issued1 = 0; done1 = 0; valid1 = true; }
+        else { task0 = t; issued0 = 0; done0 = 0; valid0 = true; }
+    }
+    __device__ __forceinline__ bool complete(int s) const { return valid(s) && done(s) == kTaskRays; }
+};
+
+// ---------------------------------------------------------------- the kernel
+template <class Store, bool RECORD>
+__global__ void __launch_bounds__(kWarps * 32, 3)
+radiance_kernel(const __grid_constant__ LaunchArgs la) {
+    constexpr int kSlots = kRing * kTaskRays;
+    __shared__ float4 s_o[kWarps][kSlots];   // origin.xyz, .w = coarse fraction after the march
+    __shared__ float4 s_d[kWarps][kSlots];   // direction.xyz, .w = info word
+    __shared__ int s_blk[RECORD ? kWarps : 1][RECORD ? kSlots : 1];
+
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    float4* so = smem + (size_t)wib * (kSmemPerWarp / 16);
-    float4* sd = so + kPool;
-    float4* sinv = sd + kPool;
-    float* sfrac = reinterpret_cast<float*>(sinv + kPool);
-    uint32_t* sinfo = reinterpret_cast<uint32_t*>(sfrac + kPool);
+    float4* so = s_o[wib];
+    float4* sd = s_d[wib];
+    const unsigned lt_mask = (1u << lane) - 1u;
 
-    const int R = a.R;
-    const int B = a.probes_per_unit;
-    const long long n_units = ((long long)a.n_groups + B - 1) / B;
-    const long long gwarp = (long long)blockIdx.x * kWarps + wib;
-    const long long nwarps = (long long)gridDim.x * kWarps;
-    unsigned long long my_lookups = 0, my_hits = 0;
+    // current world (warp-uniform): descriptor pointer + the march's fields in registers
+    int wi = -1;
+    const WorldPass* wp = &la.single;
+    MarchView mv{0, 0, 0, 0, nullptr, nullptr};
+    float wx = 0.0f, wy = 0.0f, wz = 0.0f, max_dist = 0.0f;
+    int max_steps = 0;
+    int w_begin = 0, w_end = 0;   // task range of the current world
 
-    for (long long u = gwarp; u < n_units; u += nwarps) {
-        const long long g0 = u * B;
-        const long long g1 = min(g0 + B, (long long)a.n_groups);
-        const long long ray_end = g1 * R;
-        float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-        for (long long c0 = g0 * R; c0 < ray_end; c0 += kPool) {
-            const int n = (int)min((long long)kPool, ray_end - c0);
-            for (int i = lane; i < n; i += 32) setup_ray(a, c0 + i, so[i], sd[i], sinv[i]);
-            __syncwarp();
-            march_pool<RECORD>(a.w, so, sd, sinv, sfrac, sinfo, n, a.max_dist, a.max_steps, lane);
-            __syncwarp();
-            for (int s = 0; s < n; s += 32) {
-                const int i = s + lane;
-                const long long gr = c0 + i;
-                const int block = RECORD ? __float_as_int(so[i].w) : 0;
-                uint32_t lk;
-                float3 L = finalize_ray<Store, RECORD>(a, so[i], sd[i], sinv[i], sfrac[i], sinfo[i],
-                                                       block, gr, lk);
-                if (STATS) {
-                    my_lookups += lk;
-                    my_hits += (sinfo[i] >> 24) & 1u;
-                }
-                L = butterfly_sum(L);
-                acc.x = fadd(acc.x, fdiv(L.x, 32.0f));
-                acc.y = fadd(acc.y, fdiv(L.y, 32.0f));
-                acc.z = fadd(acc.z, fdiv(L.z, 32.0f));
-                const long long g = (c0 + s) / R;
-                const int r_last = (int)((c0 + s) - g * R) + 32;
-                if (r_last == R) {
-                    const float nsub = (float)(R / 32);
-                    acc = make_float3(fdiv(acc.x, nsub), fdiv(acc.y, nsub), fdiv(acc.z, nsub));
-                    if (lane == 0) store_probe<Store>(a, (int)g, acc);
-                    acc = make_float3(0.0f, 0.0f, 0.0f);
-                }
-            }
-            __syncwarp();
-        }
-    }
-    if (STATS) {
+    Slots sl{0, 0, 0, 0, 0, 0, false, false, 0};
+    int tb = 0, te = 0;           // grabbed task chunk [tb, te)
+    bool exhausted = false;
+    int pending = -1;             // grabbed task of another world, waiting for the slots to drain
+
+    // lane ray state.  While the warp sets up or finalizes tasks, an in-flight ray's fraction
+    // and step count are parked in the .w lanes of its shared-memory slot (free until it ends)
+    // so the march registers are dead there.
+    int my = -1;
+    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, ivx = 0, ivy = 0, ivz = 0, cx = 0, cy = 0, cz = 0, frac = 0;
+    int steps = 0;
+    unsigned long long st_lookups = 0, st_hits = 0;
+
+    auto flush_stats = [&]() {
+        unsigned long long a = st_lookups, b = st_hits;
 #pragma unroll
         for (int m = 16; m >= 1; m >>= 1) {
-            my_lookups += __shfl_xor_sync(kFull, my_lookups, m);
-            my_hits += __shfl_xor_sync(kFull, my_hits, m);
+            a += __shfl_xor_sync(kFull, a, m);
+            b += __shfl_xor_sync(kFull, b, m);
         }
-        if (lane == 0 && (my_lookups | my_hits)) {
-            atomicAdd(a.counters, my_lookups);
-            atomicAdd(a.counters + 1, my_hits);
+        if (lane == 0 && (a | b)) {
+            atomicAdd(wp->stats, a);
+            atomicAdd(wp->stats + 1, b);
+        }
+        st_lookups = st_hits = 0;
+    };
+    auto world_of = [&](int t) {
+        if (la.n_worlds == 1) return 0;
+        int lo = 0, hi = la.n_worlds - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (la.worlds[mid].task_begin <= t) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    };
+    auto next_task = [&]() -> int {
+        if (pending >= 0) return pending;
+        if (tb >= te) {
+            if (exhausted) return -1;
+            unsigned long long start = 0, k = 1;
+            if (lane == 0) {
+                const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(la.queue);
+                const long long rem = la.n_tasks - (long long)cur;
+                const long long kk = rem / (2LL * la.total_warps);
+                k = (unsigned long long)(kk < 1 ? 1 : (kk > 16 ? 16 : kk));
+                start = atomicAdd(la.queue, k);
+            }
+            start = __shfl_sync(kFull, start, 0);
+            k = __shfl_sync(kFull, k, 0);
+            if ((long long)start >= la.n_tasks) {
+                exhausted = true;
+                return -1;
+            }
+            tb = (int)start;
+            te = (int)min((long long)(start + k), la.n_tasks);
+        }
+        return tb;
+    };
+    // a ray's state: origin/direction from its slot; fraction and steps from the slot's .w
+    // lanes (0 for a fresh ray, parked values for an interrupted one)
+    auto load_ray = [&](int slot) {
+        const float4 o4 = so[slot], d4 = sd[slot];
+        ox = o4.x; oy = o4.y; oz = o4.z;
+        dx = d4.x; dy = d4.y; dz = d4.z;
+        ivx = __frcp_rn(dx); ivy = __frcp_rn(dy); ivz = __frcp_rn(dz);
+        cx = dx > 0.0f ? 16.0f : 0.0f;
+        cy = dy > 0.0f ? 16.0f : 0.0f;
+        cz = dz > 0.0f ? 16.0f : 0.0f;
+        frac = o4.w;
+        steps = __float_as_int(d4.w);
+    };
+    auto park_ray = [&]() {
+        if (my >= 0) {
+            so[my].w = frac;
+            sd[my].w = __int_as_float(steps);
+        }
+    };
+    // hand the next unissued rays (older slot first) to the lanes in `need`
+    auto assign = [&](unsigned need) {
+#pragma unroll
+        for (int j = 0; j < kRing; j++) {
+            const int s = j == 0 ? sl.older : 1 - sl.older;
+            if (!need || !sl.valid(s)) continue;
+            const int avail = kTaskRays - sl.issued(s);
+            if (avail <= 0) continue;
+            const int take = min(avail, __popc(need));
+            const int rank = __popc(need & lt_mask);
+            const bool mine = ((need >> lane) & 1u) && rank < take;
+            if (mine) my = s * kTaskRays + sl.issued(s) + rank;
+            need &= ~__ballot_sync(kFull, mine);
+            sl.add_issued(s, take);
+        }
+    };
+
+    while (true) {
+        bool progress = false;
+        // 1. fill free slots with tasks of the current world
+#pragma unroll
+        for (int s = 0; s < kRing; s++) {
+            if (sl.valid(s)) continue;
+            const int t = next_task();
+            if (t < 0) break;
+            if (t < w_begin || t >= w_end) {
+                if (sl.valid0 || sl.valid1) {   // another world: drain this one first
+                    if (pending != t) tb++;
+                    pending = t;
+                    break;
+                }
+                if (wi >= 0) flush_stats();
+                wi = world_of(t);
+                wp = la.n_worlds == 1 ? &la.single : la.worlds + wi;
+                mv.X = wp->X; mv.Y = wp->Y; mv.Z = wp->Z;
+                mv.wide = wp->cgrid_wide;
+                mv.cgrid = reinterpret_cast<const uint8_t*>(wp->cgrid);
+                mv.cbits = wp->cbits;
+                wx = fmul((float)mv.X, 16.0f); wy = fmul((float)mv.Y, 16.0f); wz = fmul((float)mv.Z, 16.0f);
+                max_dist = wp->max_dist;
+                max_steps = wp->max_steps;
+                w_begin = (int)wp->task_begin;
+                w_end = (int)(wp->task_begin + wp->n_tasks);
+            }
+            if (pending == t) pending = -1;
+            else tb++;
+            // setup: lane i builds ray i of the task
+            const long long gr = (long long)(t - w_begin) * kTaskRays + lane;
+            float3 o, d;
+            setup_ray(*wp, gr, o, d);
+            so[s * kTaskRays + lane] = make_float4(o.x, o.y, o.z, 0.0f);
+            sd[s * kTaskRays + lane] = make_float4(d.x, d.y, d.z, 0.0f);
+            if (!sl.valid(1 - s)) sl.older = s;
+            sl.load(s, t);
+            progress = true;
+        }
+        __syncwarp();
+        assign(__ballot_sync(kFull, my < 0));
+        if (my >= 0) load_ray(my);   // parked rays resume, idle lanes start fresh ones
+        if (!sl.valid0 && !sl.valid1) {
+            // no more tasks (an empty ring with a task pending cannot happen: step 1 switches
+            // world and loads it; report it rather than loop)
+            if (pending >= 0 && lane == 0) atomicOr(la.error, 2);
+            break;
+        }
+
+        // 2. march until one task has all 32 rays done (or no lane has a ray)
+        int n_active = __popc(__ballot_sync(kFull, my >= 0));
+        while (n_active > 0) {
+            bool fin = false;
+            uint32_t info = 0;
+            if (my >= 0) {
+                frac = fadd(frac, 0.5f);
+                steps++;
+                const float px = fadd(ox, fmul(dx, frac));
+                const float py = fadd(oy, fmul(dy, frac));
+                const float pz = fadd(oz, fmul(dz, frac));
+                const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
+                int cid;
+                const bool solid = solid_at(mv, ix, iy, iz, cid);
+                if (cid == 0) {
+                    // empty block: skip to its far corner (radiance.comp:215-226)
+                    const float bx = fadd((float)((ix / 16) * 16), cx);
+                    const float by = fadd((float)((iy / 16) * 16), cy);
+                    const float bz = fadd((float)((iz / 16) * 16), cz);
+                    const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
+                    const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
+                    const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
+                    frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
+                }
+                if (solid) {
+                    fin = true;
+                    info = (uint32_t)steps | (1u << 24);
+                } else if (px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz || frac >= max_dist) {
+                    fin = true;
+                    info = (uint32_t)steps;
+                } else if (steps >= max_steps) {
+                    fin = true;
+                    info = (uint32_t)steps | (1u << 25);
+                }
+                if (RECORD && fin) {
+                    int blk;
+                    const int v = voxel_value(*wp, ix, iy, iz, blk);
+                    if (solid) info |= (uint32_t)v << 16;
+                    s_blk[wib][my] = blk;
+                }
+            }
+            const unsigned fm = __ballot_sync(kFull, fin);
+            if (fm) {
+                if (fin) {
+                    so[my].w = frac;
+                    sd[my].w = __uint_as_float(info);
+                }
+                const unsigned in1 = __ballot_sync(kFull, fin && my >= kTaskRays);
+                sl.done1 += __popc(in1);
+                sl.done0 += __popc(fm & ~in1);
+                if (fin) my = -1;
+                assign(fm);
+                if (fin && my >= 0) load_ray(my);
+                n_active = __popc(__ballot_sync(kFull, my >= 0));
+                if (sl.complete(0) || sl.complete(1)) break;
+            }
+        }
+        park_ray();
+        __syncwarp();
+
+        // 3. finalize every completed task (older first)
+#pragma unroll
+        for (int j = 0; j < kRing; j++) {
+            const int s = j == 0 ? sl.older : 1 - sl.older;
+            if (!sl.complete(s)) continue;
+            const int slot = s * kTaskRays + lane;
+            const float4 o4 = so[slot], d4 = sd[slot];
+            const uint32_t info = __float_as_uint(d4.w);
+            const int t_local = sl.task(s) - w_begin;
+            const long long gr = (long long)t_local * kTaskRays + lane;
+            uint32_t lk;
+            float3 L = finalize_ray<Store, RECORD>(*wp, mv, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z),
+                                                   o4.w, info, RECORD ? s_blk[wib][slot] : 0, gr, lk);
+            st_lookups += lk;
+            st_hits += (info >> 24) & 1u;
+            L = butterfly_sum(L);
+            const float3 v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
+            const int nsub = wp->R >> 5;
+            const int g = t_local / nsub;
+            const int k = t_local - g * nsub;
+            if (lane == 0) subgroup_done<Store>(*wp, g, k, v);
+            sl.set_valid(s, false);
+            sl.older = 1 - s;
+            progress = true;
+        }
+        __syncwarp();
+        // every round loads or finishes a task; a round without progress would repeat forever
+        if (!progress) {
+            if (lane == 0) atomicOr(la.error, 1);
+            break;
+        }
+    }
+
+    if (wi >= 0) flush_stats();
+    // the last warp to finish resets the queue for the next launch
+    if (lane == 0) {
+        const unsigned long long e = atomicAdd(la.queue + 1, 1ull);
+        if (e == (unsigned long long)la.total_warps - 1) {
+            la.queue[0] = 0;
+            la.queue[1] = 0;
         }
     }
 }
 
-template <class Store, bool RECORD, bool STATS>
-cudaError_t launch_t(const PassArgs& args, int num_sms, cudaStream_t stream) {
-    auto kern = radiance_pass_kernel<Store, RECORD, STATS>;
-    const int smem = kWarps * kSmemPerWarp;
-    static bool configured = false;   // attribute set once per instantiation
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+template <class Store, bool RECORD>
+int grid_size_t(int num_sms) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long units = ((long long)args.n_groups + args.probes_per_unit - 1) / args.probes_per_unit;
-    const long long warps_needed = units;
-    long long blocks = (warps_needed + kWarps - 1) / kWarps;
-    const long long cap = (long long)num_sms * per_sm;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) return cudaSuccess;
-    kern<<<(unsigned)blocks, kWarps * 32, smem, stream>>>(args);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, radiance_kernel<Store, RECORD>, kWarps * 32, 0) !=
+            cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return num_sms * per_sm;
+}
+
+template <class Store, bool RECORD>
+cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
+    const int blocks = grid_size_t<Store, RECORD>(num_sms);
+    LaunchArgs args = a;
+    args.total_warps = blocks * kWarps;
+    radiance_kernel<Store, RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_radiance_pass(const PassArgs& args, int precision, bool record, bool stats,
-                                 int num_sms, cudaStream_t stream) {
-    if (args.n_groups <= 0) return cudaSuccess;
-#define LUMRAD_DISPATCH(STORE)                                                           \
-    if (record) return stats ? launch_t<STORE, true, true>(args, num_sms, stream)        \
-                             : launch_t<STORE, true, false>(args, num_sms, stream);      \
-    return stats ? launch_t<STORE, false, true>(args, num_sms, stream)                   \
-                 : launch_t<STORE, false, false>(args, num_sms, stream);
+int radiance_grid_size(int precision, bool record, int num_sms) {
     switch (precision) {
-        case LUMRAD_PRECISION_FP16: { LUMRAD_DISPATCH(StoreF16) }
-        case LUMRAD_PRECISION_BF16: { LUMRAD_DISPATCH(StoreBF16) }
-        default: { LUMRAD_DISPATCH(StoreF32) }
+        case LUMRAD_PRECISION_FP16: return record ? grid_size_t<StoreF16, true>(num_sms) : grid_size_t<StoreF16, false>(num_sms);
+        case LUMRAD_PRECISION_BF16: return record ? grid_size_t<StoreBF16, true>(num_sms) : grid_size_t<StoreBF16, false>(num_sms);
+        default: return record ? grid_size_t<StoreF32, true>(num_sms) : grid_size_t<StoreF32, false>(num_sms);
     }
-#undef LUMRAD_DISPATCH
+}
+
+cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream) {
+    if (args.n_tasks <= 0) return cudaSuccess;
+    switch (precision) {
+        case LUMRAD_PRECISION_FP16:
+            return record ? launch_t<StoreF16, true>(args, num_sms, stream) : launch_t<StoreF16, false>(args, num_sms, stream);
+        case LUMRAD_PRECISION_BF16:
+            return record ? launch_t<StoreBF16, true>(args, num_sms, stream) : launch_t<StoreBF16, false>(args, num_sms, stream);
+        default:
+            return record ? launch_t<StoreF32, true>(args, num_sms, stream) : launch_t<StoreF32, false>(args, num_sms, stream);
+    }
 }
 
 }  // namespace lumrad

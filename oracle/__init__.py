@@ -60,8 +60,8 @@ def load() -> C.CDLL:
         build()
     lib = C.CDLL(LIB)
     P = C.c_void_p
-    lib.oracle_pass_f32.argtypes = [P, P, C.c_int, P, P, P, P, P, C.c_int]
-    lib.oracle_pass_f64.argtypes = [P, P, C.c_int, P, P, P, P, P, C.c_int]
+    lib.oracle_pass_f32.argtypes = [P, P, C.c_int, P, P, P, P, P, P, C.c_int]
+    lib.oracle_pass_f64.argtypes = [P, P, C.c_int, P, P, P, P, P, P, C.c_int]
     lib.oracle_hash33.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, P]
     lib.oracle_hash33.restype = None
     lib.oracle_direction_table.argtypes = [C.c_int, P]
@@ -91,8 +91,10 @@ def world_struct(world) -> _Keep:
 
 def radiance_pass(world, requests: np.ndarray, rays: int = 64, max_dist: float = 128.0, blend: float = 0.01,
                   time_seed: int = 0, size: int = 1, shift: int = 0, prev: np.ndarray | None = None,
-                  precision: str = "f32", record_hits: bool = False, threads: int = 0):
-    """One pass; returns (next radiance (Z,Y,X,3), hits or None, stats dict)."""
+                  precision: str = "f32", record_hits: bool = False, threads: int = 0,
+                  ray_light: np.ndarray | None = None):
+    """One pass; returns (next radiance (Z,Y,X,3), hits or None, stats dict).
+    ray_light, if given, receives each ray's light ((groups*rays, 3), the pass's precision)."""
     lib = load()
     k = world_struct(world)
     Z, Y, X = k.grid.shape
@@ -109,7 +111,7 @@ def radiance_pass(world, requests: np.ndarray, rays: int = 64, max_dist: float =
     fn = lib.oracle_pass_f32 if precision == "f32" else lib.oracle_pass_f64
     rc = fn(C.byref(k.c), req.ctypes.data if req.size else None, req.shape[0], C.byref(p),
             prev.ctypes.data, nxt.ctypes.data, hits.ctypes.data if hits is not None else None,
-            C.byref(st), threads)
+            C.byref(st), ray_light.ctypes.data if ray_light is not None else None, threads)
     if rc != 0:
         raise ValueError("oracle rejected the arguments")
     return nxt, hits, {"probes": st.probes, "rays": st.rays, "steps": st.steps, "hits": st.hits}

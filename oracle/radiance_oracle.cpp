@@ -349,7 +349,7 @@ template <typename T> inline T clamp01(T v) { return v > (T)0 ? (v < (T)1 ? v : 
 
 template <typename T>
 int run_pass(const OracleWorld* ow, const int16_t* req, int n_req, const OracleParams* p,
-             const T* prev, T* next, OracleHit* hits, OracleStats* stats, int threads) {
+             const T* prev, T* next, OracleHit* hits, OracleStats* stats, T* ray_light_out, int threads) {
     if (!ow || !p || !prev || !next || (n_req > 0 && !req)) return -1;
     if (p->rays < 32 || p->rays % 32 != 0 || p->size < 1 || p->shift < 0 || p->shift >= p->size)
         return -1;
@@ -383,6 +383,10 @@ int run_pass(const OracleWorld* ow, const int16_t* req, int n_req, const OracleP
             if (r % 2 != 0) d = -d;
             RayOut ro;
             ray_light[r] = trace<T>(w, prev, o, d, p->max_dist, max_steps, &ro);
+            if (ray_light_out) {
+                T* lo = ray_light_out + 3 * ((size_t)g * R + r);
+                lo[0] = ray_light[r].x; lo[1] = ray_light[r].y; lo[2] = ray_light[r].z;
+            }
             const CastResult& c = ro.cast;
             tot_steps += (uint64_t)c.coarse_steps + (c.hit ? 1u + (uint64_t)ro.ref.iters : 0u);
             tot_hits += c.hit ? 1u : 0u;
@@ -450,13 +454,15 @@ int run_pass(const OracleWorld* ow, const int16_t* req, int n_req, const OracleP
 extern "C" {
 
 int oracle_pass_f32(const OracleWorld* w, const int16_t* req, int n, const OracleParams* p,
-                    const float* prev, float* next, OracleHit* hits, OracleStats* stats, int threads) {
-    return run_pass<float>(w, req, n, p, prev, next, hits, stats, threads);
+                    const float* prev, float* next, OracleHit* hits, OracleStats* stats, float* ray_light,
+                    int threads) {
+    return run_pass<float>(w, req, n, p, prev, next, hits, stats, ray_light, threads);
 }
 
 int oracle_pass_f64(const OracleWorld* w, const int16_t* req, int n, const OracleParams* p,
-                    const double* prev, double* next, OracleHit* hits, OracleStats* stats, int threads) {
-    return run_pass<double>(w, req, n, p, prev, next, hits, stats, threads);
+                    const double* prev, double* next, OracleHit* hits, OracleStats* stats, double* ray_light,
+                    int threads) {
+    return run_pass<double>(w, req, n, p, prev, next, hits, stats, ray_light, threads);
 }
 
 // hash33 of one seed (known-answer tests)
