@@ -2,17 +2,19 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include "../../include/lumrad.h"
+#include "lumrad.h"
 
 namespace lumrad {
 
-// Warps per CTA of the pass kernel.
+// Warps per CTA of the pass kernels.
 constexpr int kWarps = 8;
-// A task is one 32-ray subgroup of one probe; a warp keeps two tasks in flight.
+// A task is one 32-ray subgroup of one probe (the unit radiance.comp sums with subgroupAdd).
 constexpr int kTaskRays = 32;
-constexpr int kRing = 2;
+// Tasks per march/finalize round: the per-ray buffers between the two kernels hold this many
+// tasks' rays (32 B + 8 B per ray: 80 MiB, L2-resident on GB300).
+constexpr int kChunkTasks = 1 << 16;
 
-// One world's pass as the kernel sees it (all pointers are device pointers).
+// One world's pass as the kernels see it (all pointers are device pointers).
 //
 // The coarse march and the refine DDA only ask "is this block air" and "is this voxel solid",
 // so they read a compact copy of the world: every distinct block id is renumbered (0 stays 0)
@@ -53,17 +55,20 @@ struct LaunchArgs {
     WorldPass single;            // the world when n_worlds == 1 (passed by value)
     const WorldPass* worlds;     // device array when n_worlds > 1
     int n_worlds;
-    int total_warps;             // warps in the grid (set by the launcher)
-    long long n_tasks;
+    int total_warps;             // warps of the march grid (set by the launcher)
+    int chunk_begin, chunk_end;  // tasks of this march/finalize round (set by the launcher)
+    long long n_tasks;           // tasks of all worlds
     unsigned long long* queue;   // [0] next task, [1] warps finished; zero between launches
     int* error;                  // set non-zero if a warp's scheduler stops making progress
+    float4* ray_od;              // per ray of the round: origin (xyz), direction (xyz)
+    uint2* ray_res;              // per ray of the round: coarse fraction bits, info word
+    int* ray_blk;                // per ray of the round: block id at the last coarse step (records)
 };
 
-// Launches one pass over `n_worlds` worlds (descriptors already on the device) on `stream`.
+// Runs one pass over the worlds of `args` (descriptors already on the device when n_worlds > 1)
+// on `stream`: for each round of up to kChunkTasks tasks, the march kernel then the finalize
+// kernel.  Returns a CUDA error code.
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms,
                             cudaStream_t stream);
-
-// Number of CTAs launch_radiance uses on a device with `num_sms` SMs.
-int radiance_grid_size(int precision, bool record, int num_sms);
 
 }  // namespace lumrad

@@ -89,6 +89,11 @@ struct Context {
     std::map<int, Resident> resident;
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
+    // rays of one march/finalize round (up to kChunkTasks * 32 rays)
+    float4* d_ray_od = nullptr;
+    uint2* d_ray_res = nullptr;
+    int* d_ray_blk = nullptr;
+    size_t ray_cap = 0;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_req = nullptr;
@@ -104,6 +109,7 @@ struct Context {
     float last_ms = 0.0f;
 
     int ensure_req_capacity(size_t n);
+    int ensure_rays(long long n_tasks);
     int stage_requests(const int16_t* req, size_t n);
     int run_pass(const short4* d_req, int n, const LumRadPassParams* p);
     int check_error();

@@ -1,448 +1,67 @@
-// radiance_pass.cu — sm_103a kernel of the per-block radiance update.
+// radiance_pass.cu — sm_103a kernels of the per-block radiance update.
 //
-// Restates shaders/radiance.comp (main :361-413, trace_ray :316-346, CastRay_fast :183-291,
-// GetVoxel :121-143, sample_radiance :161-166, store_probe :349-354, hash33 :51-66).
+// Restates shaders/radiance.comp (main :361-413, trace_ray :316-346, CastRay_fast :183-291) as two
+// kernels per round of up to kChunkTasks tasks (a task = one 32-ray subgroup of one probe):
 //
-// Work decomposition.  A task is one 32-ray subgroup of one probe (the unit the shader sums
-// with subgroupAdd).  Persistent warps take tasks from a queue in guided chunks (large early,
-// single tasks at the end), so the last tasks spread over all SMs.  A warp keeps two tasks in
-// flight and runs three phases:
-//   setup     lock step, one ray per lane: hash seeds, direction, origin (into shared memory);
-//   march     a flat loop: every lane advances its ray one coarse step per iteration; a lane
-//             whose ray ends stores (fraction, info) and takes the next unissued ray of the two
-//             tasks, so short and long rays share the warp;
-//   finalize  lock step when a task's 32 rays are done: refine DDA, material, trilinear fetch
-//             of the previous radiance, shading, xor-butterfly sum.  For R = 32 the probe is
-//             blended and stored at once; otherwise the subgroup mean goes to scratch and the
-//             task that completes a probe's last subgroup sums the means in subgroup order.
+//   march_kernel     persistent warps take tasks from a queue in guided chunks (large early,
+//                    single tasks at the end).  A warp sets up a task's 32 rays in lock step
+//                    (hash seeds, direction, origin, 1/direction) into one half of a 64-ray ring in
+//                    shared memory and writes them to the round's ray buffer.  Its lanes march
+//                    in a flat loop, one coarse step per iteration; a lane whose ray ends writes
+//                    (fraction, info) and takes the next ray in ring order.  A half is set up again
+//                    as soon as its rays are handed out, so lanes never wait for each other.
+//   finalize_kernel  one warp per task, eight consecutive tasks per CTA, in lock step: refine
+//                    DDA, material, trilinear fetch of the previous radiance, shading,
+//                    xor-butterfly sum.  When R/32 divides 8 a probe's subgroups share a CTA and
+//                    their means are summed in order from shared memory; otherwise through
+//                    global scratch and a per-probe counter.
 //
-// Exactness.  All float arithmetic uses round-to-nearest intrinsics (__fadd_rn, __fmul_rn,
-// __fdiv_rn, __frcp_rn, __fsqrt_rn), which are never fused into FMA, in the shader's order.
-// Divisions by powers of two are multiplications by the exact reciprocal (identical results).
-// Hit records are bit-exact and FP32 radiance bit-identical to the CPU restatement.
-//
-// Memory.  The march and refine tests read the compact world (uint8 ids + occupancy bits,
-// L1-resident); the two tasks of a warp use 2 KiB of shared memory, leaving L1 to the data.
+// Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
+// world (uint8 ids + occupancy bits, L1-resident); the ray buffers between the kernels
+// (40 B per ray) stay in L2.
 
-#include <cuda_runtime.h>
-#include <cuda_fp16.h>
-#include <cuda_bf16.h>
-#include <stdint.h>
-#include "lumrad_internal.h"
+#include "radiance_device.cuh"
 
 namespace lumrad {
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
-// x / d where `inv` is 1/d if that is exact (d a power of two), else 0
-__device__ __forceinline__ float fdiv_by(float x, float d, float inv) { return inv != 0.0f ? fmul(x, inv) : fdiv(x, d); }
-// GLSL min/max definitions: identical NaN and signed-zero behaviour everywhere.
-__device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
-__device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
-// float -> int toward zero; PTX cvt.rzi saturates and maps NaN to 0.
-__device__ __forceinline__ int f2i(float f) { return __float2int_rz(f); }
-// SPIR-V OpSMod for a positive divisor.
-__device__ __forceinline__ int smod(int a, int b) {
-    int r = a % b;
-    return (r < 0) ? r + b : r;
-}
-// Hit records report every NaN as the canonical quiet NaN 0x7FC00000.
-__device__ __forceinline__ float canon_nan(float f) { return f == f ? f : __int_as_float(0x7FC00000); }
-
-// ---------------------------------------------------------------- radiance storage types
-struct StoreF32 {
-    typedef float4 T;
-    static __device__ __forceinline__ float3 load(const T* p, int i) {
-        float4 v = __ldg(p + i);
-        return make_float3(v.x, v.y, v.z);
-    }
-    static __device__ __forceinline__ void store(T* p, int i, float3 v) { p[i] = make_float4(v.x, v.y, v.z, 1.0f); }
-};
-struct StoreF16 {
-    typedef uint2 T;   // (r,g) (b,1) as two half2
-    static __device__ __forceinline__ float3 load(const T* p, int i) {
-        uint2 v = __ldg(p + i);
-        __half2 a = *reinterpret_cast<__half2*>(&v.x);
-        __half2 b = *reinterpret_cast<__half2*>(&v.y);
-        return make_float3(__low2float(a), __high2float(a), __low2float(b));
-    }
-    static __device__ __forceinline__ void store(T* p, int i, float3 v) {
-        __half2 a = __floats2half2_rn(v.x, v.y);
-        __half2 b = __floats2half2_rn(v.z, 1.0f);
-        uint2 o;
-        o.x = *reinterpret_cast<unsigned*>(&a);
-        o.y = *reinterpret_cast<unsigned*>(&b);
-        p[i] = o;
-    }
-};
-struct StoreBF16 {
-    typedef uint2 T;
-    static __device__ __forceinline__ float3 load(const T* p, int i) {
-        uint2 v = __ldg(p + i);
-        __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162*>(&v.x);
-        __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&v.y);
-        return make_float3(__low2float(a), __high2float(a), __low2float(b));
-    }
-    static __device__ __forceinline__ void store(T* p, int i, float3 v) {
-        __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
-        __nv_bfloat162 b = __floats2bfloat162_rn(v.z, 1.0f);
-        uint2 o;
-        o.x = *reinterpret_cast<unsigned*>(&a);
-        o.y = *reinterpret_cast<unsigned*>(&b);
-        p[i] = o;
-    }
-};
-
-// ---------------------------------------------------------------- voxel lookups
-// GetVoxel (radiance.comp:121-143) on integer voxel coordinates.  Block coordinate = ix/16
-// truncated (OpSDiv); voxel in block = ix mod 16 floored (OpSMod) = ix & 15.  The grid fetch is
-// in range iff -15 <= ix < 16*X, and then ix/16 == max(ix,0) >> 4; out of range reads block 0.
-__device__ __forceinline__ bool grid_index(int X, int Y, int Z, int ix, int iy, int iz, int& idx) {
-    const bool in = (unsigned)ix + 15u < (unsigned)(16 * X + 15) && (unsigned)iy + 15u < (unsigned)(16 * Y + 15) &&
-                    (unsigned)iz + 15u < (unsigned)(16 * Z + 15);
-    idx = (max(ix, 0) >> 4) + X * ((max(iy, 0) >> 4) + Y * (max(iz, 0) >> 4));
-    return in;
-}
-
-// What the march and refine tests read of the current world (kept in registers).
-struct MarchView {
-    int X, Y, Z;
-    int wide;                     // compact ids are uint16
-    const uint8_t* cgrid;
-    const uint32_t* cbits;
-};
-
-// Compact lookup: compact id of the block (0 iff block id 0) and whether the voxel is solid.
-__device__ __forceinline__ bool solid_at(const MarchView& m, int ix, int iy, int iz, int& cid) {
-    int idx;
-    int c = 0;
-    if (grid_index(m.X, m.Y, m.Z, ix, iy, iz, idx))
-        c = m.wide ? (int)__ldg(reinterpret_cast<const uint16_t*>(m.cgrid) + idx) : (int)__ldg(m.cgrid + idx);
-    cid = c;
-    const uint32_t word = __ldg(m.cbits + ((c << 7) | ((iz & 15) << 3) | ((iy & 15) >> 1)));
-    return (word >> (((iy & 1) << 4) | (ix & 15))) & 1u;
-}
-
-// Original lookup (voxel value and block id): block id b addresses palette slot
-// (b mod 64) + 64*(b/64) (voxel_in_palette :105-110 on the 64x64-slot image): slot b for
-// b >= 0, slot b+64 for -63 <= b < 0, nothing past the loaded slots.
-__device__ __forceinline__ int voxel_value(const WorldPass& w, int ix, int iy, int iz, int& block) {
-    int idx;
-    int b = 0;
-    if (grid_index(w.X, w.Y, w.Z, ix, iy, iz, idx)) b = __ldg(w.grid + idx);
-    block = b;
-    const int slot = b < 0 ? b + 64 : b;
-    if (b < -63 || slot >= w.n_slots) return 0;
-    return __ldg(w.pal + ((slot << 12) | ((iz & 15) << 8) | ((iy & 15) << 4) | (ix & 15)));
-}
-
-// ---------------------------------------------------------------- ray setup (:362-381)
-__device__ __forceinline__ float3 hash33(uint32_t x, uint32_t y, uint32_t z) {
-    const uint32_t k = 1103515245u;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const uint32_t nx = ((x >> 8) ^ y) * k;
-        const uint32_t ny = ((y >> 8) ^ z) * k;
-        const uint32_t nz = ((z >> 8) ^ x) * k;
-        x = nx; y = ny; z = nz;
-    }
-    const float s = 2.3283064365386963e-10f;   // 1/float(0xffffffffu) = 2^-32
-    return make_float3(fmul(__uint2float_rn(x), s), fmul(__uint2float_rn(y), s), fmul(__uint2float_rn(z), s));
-}
-
-__device__ __forceinline__ float3 normalize3(float3 v) {
-    const float dd = fadd(fadd(fmul(v.x, v.x), fmul(v.y, v.y)), fmul(v.z, v.z));
-    const float s = fdiv(1.0f, __fsqrt_rn(dd));
-    return make_float3(fmul(v.x, s), fmul(v.y, s), fmul(v.z, s));
-}
-
-// Ray r of workgroup g (global invocation id gr = g*R + r): origin and direction.
-__device__ __forceinline__ void setup_ray(const WorldPass& w, long long gr, float3& o, float3& d) {
-    const int g = (int)(gr / w.R);
-    const int r = (int)(gr - (long long)g * w.R);
-    const short4 q = __ldg(w.req + ((long long)g * w.size + w.shift));
-    uint32_t sx = (uint32_t)gr + w.seed;
-    const uint32_t sy = w.seed, sz = w.seed;
-    const float3 c = make_float3(fadd(fmul((float)q.x, 16.0f), 8.0f), fadd(fmul((float)q.y, 16.0f), 8.0f),
-                                 fadd(fmul((float)q.z, 16.0f), 8.0f));
-    const float4 f = __ldg(w.dirs + r);
-    const float3 r1 = hash33(sx, sy, sz);
-    sx++;
-    const float3 j = make_float3(fmul(0.1f, fmul(fsub(r1.x, 0.5f), 2.0f)), fmul(0.1f, fmul(fsub(r1.y, 0.5f), 2.0f)),
-                                 fmul(0.1f, fmul(fsub(r1.z, 0.5f), 2.0f)));
-    d = normalize3(make_float3(fadd(f.x, j.x), fadd(f.y, j.y), fadd(f.z, j.z)));
-    o = make_float3(fadd(c.x, fmul(d.x, 6.0f)), fadd(c.y, fmul(d.y, 6.0f)), fadd(c.z, fmul(d.z, 6.0f)));
-    const float3 r2 = hash33(sx, sy, sz);
-    o = make_float3(fadd(o.x, fmul(fsub(r2.x, 0.5f), 2.0f)), fadd(o.y, fmul(fsub(r2.y, 0.5f), 2.0f)),
-                    fadd(o.z, fmul(fsub(r2.z, 0.5f), 2.0f)));
-    if (r & 1) d = make_float3(-d.x, -d.y, -d.z);
-}
-
-// ---------------------------------------------------------------- finalize (:246-291, :316-354)
-template <class Store>
-__device__ __forceinline__ float3 sample_trilinear(const WorldPass& w, float ux, float uy, float uz) {
-    const typename Store::T* rad = reinterpret_cast<const typename Store::T*>(w.prev);
-    const int X = w.X, Y = w.Y, Z = w.Z;
-    const float u[3] = {fsub(fmul(ux, (float)X), 0.5f), fsub(fmul(uy, (float)Y), 0.5f), fsub(fmul(uz, (float)Z), 0.5f)};
-    const int n[3] = {X, Y, Z};
-    int i0[3], i1[3];
-    float t[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        const float fl = floorf(u[c]);
-        t[c] = fsub(u[c], fl);
-        const int ii = smod(f2i(fl), n[c]);
-        i0[c] = ii;
-        i1[c] = (ii + 1 == n[c]) ? 0 : ii + 1;
-    }
-    auto tex = [&](int x, int y, int z) { return Store::load(rad, x + X * (y + Y * z)); };
-    auto lerp = [](float3 p, float3 q, float s) {
-        const float r = fsub(1.0f, s);
-        return make_float3(fadd(fmul(p.x, r), fmul(q.x, s)), fadd(fmul(p.y, r), fmul(q.y, s)),
-                           fadd(fmul(p.z, r), fmul(q.z, s)));
-    };
-    const float3 c00 = lerp(tex(i0[0], i0[1], i0[2]), tex(i1[0], i0[1], i0[2]), t[0]);
-    const float3 c10 = lerp(tex(i0[0], i1[1], i0[2]), tex(i1[0], i1[1], i0[2]), t[0]);
-    const float3 c01 = lerp(tex(i0[0], i0[1], i1[2]), tex(i1[0], i0[1], i1[2]), t[0]);
-    const float3 c11 = lerp(tex(i0[0], i1[1], i1[2]), tex(i1[0], i1[1], i1[2]), t[0]);
-    return lerp(lerp(c00, c10, t[1]), lerp(c01, c11, t[1]), t[2]);
-}
-
-// info word of a marched ray: bits 0-15 coarse steps, 16-23 coarse voxel (RECORD only),
-// 24 hit, 25 stopped by the step bound.
-template <class Store, bool RECORD>
-__device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchView& mv, float3 o, float3 d,
-                                               float coarse_frac, uint32_t info, int block, long long gr,
-                                               uint32_t& lookups) {
-    const bool hit = (info >> 24) & 1u;
-    const int coarse_steps = info & 0xffff;
-    lookups = coarse_steps;
-    float3 light;
-    LumRadHit rec;
-    if (RECORD) {
-        rec.voxel[0] = rec.voxel[1] = rec.voxel[2] = 0;
-        rec.block = (int16_t)block;
-        rec.voxel_id = 0;
-        rec.flags = (hit ? LUMRAD_HIT_HIT : 0) | (((info >> 25) & 1u) ? LUMRAD_HIT_CAPPED : 0);
-        rec.coarse_steps = (uint16_t)coarse_steps;
-        rec.refine_steps = 0;
-        rec.coarse_voxel = (uint8_t)((info >> 16) & 0xff);
-        rec.fraction = canon_nan(coarse_frac);
-    }
-    if (hit) {
-        // refine DDA (radiance.comp:246-288)
-        const float back = fsub(coarse_frac, 1.5f);
-        const float bhx = fadd(o.x, fmul(d.x, back));
-        const float bhy = fadd(o.y, fmul(d.y, back));
-        const float bhz = fadd(o.z, fmul(d.z, back));
-        const int stx = d.x > 0.0f ? 1 : -1, sty = d.y > 0.0f ? 1 : -1, stz = d.z > 0.0f ? 1 : -1;
-        const float ivx = __frcp_rn(d.x), ivy = __frcp_rn(d.y), ivz = __frcp_rn(d.z);
-        const float c1x = fdiv(fsub(floorf(bhx), bhx), d.x);
-        const float c1y = fdiv(fsub(floorf(bhy), bhy), d.y);
-        const float c1z = fdiv(fsub(floorf(bhz), bhz), d.z);
-        float tmx = gmax(c1x, fadd(c1x, ivx));
-        float tmy = gmax(c1y, fadd(c1y, ivy));
-        float tmz = gmax(c1z, fadd(c1z, ivz));
-        const float tdx = fabsf(ivx), tdy = fabsf(ivy), tdz = fabsf(ivz);   // 1/|d| == |1/d|
-        int vx = f2i(bhx), vy = f2i(bhy), vz = f2i(bhz);
-        int cid;
-        bool solid = solid_at(mv, vx, vy, vz, cid);
-        float fsx = 0.0f, fsy = 0.0f, fsz = 0.0f;
-        int it = 0;
-        while (it < 5 && !solid) {
-            const bool bx = (tmx <= tmy) && (tmx <= tmz);
-            const bool by = (tmx >= tmy) && (tmy <= tmz);
-            const bool bz = (tmz <= tmx) && (tmz <= tmy);
-            fsx = bx ? 1.0f : 0.0f; fsy = by ? 1.0f : 0.0f; fsz = bz ? 1.0f : 0.0f;
-            vx += bx ? stx : 0; vy += by ? sty : 0; vz += bz ? stz : 0;
-            tmx = fadd(tmx, fmul(tdx, fsx));
-            tmy = fadd(tmy, fmul(tdy, fsy));
-            tmz = fadd(tmz, fmul(tdz, fsz));
-            solid = solid_at(mv, vx, vy, vz, cid);
-            it++;
-        }
-        lookups += 1 + it;
-        int blk;
-        const int cur = solid ? voxel_value(w, vx, vy, vz, blk) : 0;
-        const float nx = -fmul((float)stx, fsx), ny = -fmul((float)sty, fsy), nz = -fmul((float)stz, fsz);
-        const float fr = fadd(fadd(fmul(fsub(tmx, tdx), fsx), fmul(fsub(tmy, tdy), fsy)), fmul(fsub(tmz, tdz), fsz));
-        // material (GetMat :145-157) and sample_radiance (:161-166); /16 == *0.0625 exactly
-        const float4 m = __ldg(w.mats + cur);
-        const float hx = fadd(o.x, fmul(fr, d.x));
-        const float hy = fadd(o.y, fmul(fr, d.y));
-        const float hz = fadd(o.z, fmul(fr, d.z));
-        const float bpx = fmul(fadd(hx, fmul(nx, 16.0f)), 0.0625f);
-        const float bpy = fmul(fadd(hy, fmul(ny, 16.0f)), 0.0625f);
-        const float bpz = fmul(fadd(hz, fmul(nz, 16.0f)), 0.0625f);
-        const float3 L = sample_trilinear<Store>(w, fdiv_by(fadd(bpx, 0.5f), (float)w.X, w.inv_dim[0]),
-                                                 fdiv_by(fadd(bpy, 0.5f), (float)w.Y, w.inv_dim[1]),
-                                                 fdiv_by(fadd(bpz, 0.5f), (float)w.Z, w.inv_dim[2]));
-        light = make_float3(fadd(0.0f, fadd(fmul(L.x, m.x), fmul(m.x, m.w))),
-                            fadd(0.0f, fadd(fmul(L.y, m.y), fmul(m.y, m.w))),
-                            fadd(0.0f, fadd(fmul(L.z, m.z), fmul(m.z, m.w))));
-        if (RECORD) {
-            rec.voxel[0] = vx; rec.voxel[1] = vy; rec.voxel[2] = vz;
-            rec.voxel_id = (uint8_t)cur;
-            rec.refine_steps = (uint8_t)it;
-            rec.flags |= (fsx != 0.0f ? LUMRAD_HIT_STEP_X : 0) | (fsy != 0.0f ? LUMRAD_HIT_STEP_Y : 0) |
-                         (fsz != 0.0f ? LUMRAD_HIT_STEP_Z : 0);
-            rec.fraction = canon_nan(fr);
-        }
-    } else {
-        // sky and sun (radiance.comp:334-343); globalLightDir = normalize(0.5, 0.5, -0.9)
-        const float3 gl = normalize3(make_float3(0.5f, 0.5f, -0.9f));
-        const float g = -fadd(fadd(fmul(d.x, gl.x), fmul(d.y, gl.y)), fmul(d.z, gl.z));
-        light = make_float3(0.0f, 0.0f, 0.0f);
-        if (g > 0.95f) {
-            light.x = fadd(light.x, fmul(g, fmul(0.9f, 3.0f)));
-            light.y = fadd(light.y, fmul(g, fmul(0.9f, 3.0f)));
-            light.z = fadd(light.z, fmul(g, fmul(0.6f, 3.0f)));
-        }
-        light.x = fadd(light.x, fmul(0.53f, 0.1f));
-        light.y = fadd(light.y, fmul(0.81f, 0.1f));
-        light.z = fadd(light.z, fmul(0.92f, 0.1f));
-    }
-    if (RECORD) w.hits[gr] = rec;
-    return light;
-}
-
-__device__ __forceinline__ float3 butterfly_sum(float3 v) {
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-        v.x = fadd(v.x, __shfl_xor_sync(kFull, v.x, m));
-        v.y = fadd(v.y, __shfl_xor_sync(kFull, v.y, m));
-        v.z = fadd(v.z, __shfl_xor_sync(kFull, v.z, m));
-    }
-    return v;
-}
-
-__device__ __forceinline__ float clamp01(float v) { return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f; }
-
-// store_probe (radiance.comp:349-354): blend the clamped old value with the mean, store clamped.
-template <class Store>
-__device__ __forceinline__ void store_probe(const WorldPass& w, int g, float3 acc) {
-    const short4 q = __ldg(w.req + ((long long)g * w.size + w.shift));
-    if (q.x < 0 || q.y < 0 || q.z < 0 || q.x >= w.X || q.y >= w.Y || q.z >= w.Z) return;
-    const int idx = q.x + w.X * (q.y + w.Y * q.z);
-    float3 old = Store::load(reinterpret_cast<const typename Store::T*>(w.prev), idx);
-    old.x = old.x < 0.0f ? 0.0f : old.x; old.x = 1.0f < old.x ? 1.0f : old.x;
-    old.y = old.y < 0.0f ? 0.0f : old.y; old.y = 1.0f < old.y ? 1.0f : old.y;
-    old.z = old.z < 0.0f ? 0.0f : old.z; old.z = 1.0f < old.z ? 1.0f : old.z;
-    const float3 nv = make_float3(clamp01(fadd(fmul(old.x, w.one_minus_alpha), fmul(acc.x, w.alpha))),
-                                  clamp01(fadd(fmul(old.y, w.one_minus_alpha), fmul(acc.y, w.alpha))),
-                                  clamp01(fadd(fmul(old.z, w.one_minus_alpha), fmul(acc.z, w.alpha))));
-    Store::store(reinterpret_cast<typename Store::T*>(w.next), idx, nv);
-}
-
-// Subgroup mean V = sum/32 of subgroup k of workgroup g is done.  R = 32: the probe's mean is V.
-// Otherwise V goes to scratch and the last of the probe's R/32 subgroups sums them in order
-// (radiance.comp:401-407), divides by R/32 and stores.  Lane 0 only.
-template <class Store>
-__device__ __forceinline__ void subgroup_done(const WorldPass& w, int g, int k, float3 v) {
-    const int nsub = w.R >> 5;
-    if (nsub == 1) {
-        store_probe<Store>(w, g, make_float3(fadd(0.0f, v.x), fadd(0.0f, v.y), fadd(0.0f, v.z)));
-        return;
-    }
-    float4* slots = w.scratch + (long long)g * nsub;
-    __stcg(slots + k, make_float4(v.x, v.y, v.z, 0.0f));
-    __threadfence();
-    const int prior = atomicAdd(w.probe_count + g, 1);
-    if (prior != nsub - 1) return;
-    __threadfence();
-    float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-    for (int j = 0; j < nsub; j++) {
-        const float4 s = __ldcg(slots + j);
-        acc = make_float3(fadd(acc.x, s.x), fadd(acc.y, s.y), fadd(acc.z, s.z));
-    }
-    const float fn = (float)nsub;
-    acc = make_float3(fdiv_by(acc.x, fn, w.inv_nsub), fdiv_by(acc.y, fn, w.inv_nsub), fdiv_by(acc.z, fn, w.inv_nsub));
-    store_probe<Store>(w, g, acc);
-    w.probe_count[g] = 0;   // ready for the next launch
-}
-
-// Warp-uniform state of the two in-flight tasks (scalars, so nothing lands in local memory).
-struct Slots {
-    int task0, task1;
-    int issued0, issued1, done0, done1;
-    bool valid0, valid1;
-    int older;
-    __device__ __forceinline__ int task(int s) const { return s ? task1 : task0; }
-    __device__ __forceinline__ int issued(int s) const { return s ? issued1 : issued0; }
-    __device__ __forceinline__ int done(int s) const { return s ? done1 : done0; }
-    __device__ __forceinline__ bool valid(int s) const { return s ? valid1 : valid0; }
-    __device__ __forceinline__ void add_issued(int s, int v) { if (s) issued1 += v; else issued0 += v; }
-    __device__ __forceinline__ void set_valid(int s, bool v) { if (s) valid1 = v; else valid0 = v; }
-    __device__ __forceinline__ void load(int s, int t) {
-        if (s) { task1 = t; issued1 = 0; done1 = 0; valid1 = true; }
-        else { task0 = t; issued0 = 0; done0 = 0; valid0 = true; }
-    }
-    __device__ __forceinline__ bool complete(int s) const { return valid(s) && done(s) == kTaskRays; }
-};
-
-// ---------------------------------------------------------------- the kernel
-template <class Store, bool RECORD>
-__global__ void __launch_bounds__(kWarps * 32, 3)
-radiance_kernel(const __grid_constant__ LaunchArgs la) {
-    constexpr int kSlots = kRing * kTaskRays;
-    __shared__ float4 s_o[kWarps][kSlots];   // origin.xyz, .w = coarse fraction after the march
-    __shared__ float4 s_d[kWarps][kSlots];   // direction.xyz, .w = info word
-    __shared__ int s_blk[RECORD ? kWarps : 1][RECORD ? kSlots : 1];
+// ---------------------------------------------------------------- march kernel
+template <bool RECORD>
+__global__ void __launch_bounds__(kWarps * 32, 4)
+march_kernel(const __grid_constant__ LaunchArgs la) {
+    constexpr int kRingRays = 2 * kTaskRays;
+    __shared__ float4 s_ray[kWarps][3][kRingRays];    // set-up rays: origin, direction, 1/direction
+    __shared__ float4 s_park[kWarps][3][kTaskRays];   // in-flight ray state while the warp sets up
 
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    float4* so = s_o[wib];
-    float4* sd = s_d[wib];
+    float4* so = s_ray[wib][0];
+    float4* sd = s_ray[wib][1];
+    float4* si = s_ray[wib][2];
     const unsigned lt_mask = (1u << lane) - 1u;
+    const int n_round = la.chunk_end - la.chunk_begin;
 
-    // current world (warp-uniform): descriptor pointer + the march's fields in registers
-    int wi = -1;
+    // current world (warp-uniform)
     const WorldPass* wp = &la.single;
     MarchView mv{0, 0, 0, 0, nullptr, nullptr};
     float wx = 0.0f, wy = 0.0f, wz = 0.0f, max_dist = 0.0f;
     int max_steps = 0;
-    int w_begin = 0, w_end = 0;   // task range of the current world
-
-    Slots sl{0, 0, 0, 0, 0, 0, false, false, 0};
-    int tb = 0, te = 0;           // grabbed task chunk [tb, te)
+    int w_begin = 0, w_end = 0;
+    // FIFO ring: ray q of the issue order lives in ring slot q & 63; `loaded` rays have been set
+    // up, `issued` handed out; half h holds the task whose first round-relative ray is base[h]
+    int issued = 0, loaded = 0, base0 = 0, base1 = 0;
+    int tb = 0, te = 0;          // grabbed task chunk [tb, te)
     bool exhausted = false;
-    int pending = -1;             // grabbed task of another world, waiting for the slots to drain
+    int pending = -1;            // grabbed task of another world, waiting for the lanes to drain
 
-    // lane ray state.  While the warp sets up or finalizes tasks, an in-flight ray's fraction
-    // and step count are parked in the .w lanes of its shared-memory slot (free until it ends)
-    // so the march registers are dead there.
-    int my = -1;
+    // lane ray state
+    int my = -1;                 // round-relative index of the lane's ray, -1 if idle
     float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, ivx = 0, ivy = 0, ivz = 0, cx = 0, cy = 0, cz = 0, frac = 0;
     int steps = 0;
-    unsigned long long st_lookups = 0, st_hits = 0;
 
-    auto flush_stats = [&]() {
-        unsigned long long a = st_lookups, b = st_hits;
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) {
-            a += __shfl_xor_sync(kFull, a, m);
-            b += __shfl_xor_sync(kFull, b, m);
-        }
-        if (lane == 0 && (a | b)) {
-            atomicAdd(wp->stats, a);
-            atomicAdd(wp->stats + 1, b);
-        }
-        st_lookups = st_hits = 0;
-    };
-    auto world_of = [&](int t) {
-        if (la.n_worlds == 1) return 0;
-        int lo = 0, hi = la.n_worlds - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (la.worlds[mid].task_begin <= t) lo = mid; else hi = mid - 1;
-        }
-        return lo;
-    };
+    // Tasks are claimed in guided chunks: remaining / (2 * warps), clamped to [1, 16].  (Claiming
+    // the next chunk ahead of time hides the atomic's latency but holds work back from idle
+    // warps at the end; measured slower.)
     auto next_task = [&]() -> int {
         if (pending >= 0) return pending;
         if (tb >= te) {
@@ -450,112 +69,116 @@ radiance_kernel(const __grid_constant__ LaunchArgs la) {
             unsigned long long start = 0, k = 1;
             if (lane == 0) {
                 const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(la.queue);
-                const long long rem = la.n_tasks - (long long)cur;
+                const long long rem = (long long)n_round - (long long)cur;
                 const long long kk = rem / (2LL * la.total_warps);
                 k = (unsigned long long)(kk < 1 ? 1 : (kk > 16 ? 16 : kk));
                 start = atomicAdd(la.queue, k);
             }
             start = __shfl_sync(kFull, start, 0);
             k = __shfl_sync(kFull, k, 0);
-            if ((long long)start >= la.n_tasks) {
+            if ((long long)start >= (long long)n_round) {
                 exhausted = true;
                 return -1;
             }
-            tb = (int)start;
-            te = (int)min((long long)(start + k), la.n_tasks);
+            tb = la.chunk_begin + (int)start;
+            te = la.chunk_begin + (int)min((long long)(start + k), (long long)n_round);
         }
         return tb;
     };
-    // a ray's state: origin/direction from its slot; fraction and steps from the slot's .w
-    // lanes (0 for a fresh ray, parked values for an interrupted one)
-    auto load_ray = [&](int slot) {
-        const float4 o4 = so[slot], d4 = sd[slot];
-        ox = o4.x; oy = o4.y; oz = o4.z;
-        dx = d4.x; dy = d4.y; dz = d4.z;
-        ivx = __frcp_rn(dx); ivy = __frcp_rn(dy); ivz = __frcp_rn(dz);
+    auto corner = [&]() {
         cx = dx > 0.0f ? 16.0f : 0.0f;
         cy = dy > 0.0f ? 16.0f : 0.0f;
         cz = dz > 0.0f ? 16.0f : 0.0f;
-        frac = o4.w;
-        steps = __float_as_int(d4.w);
     };
-    auto park_ray = [&]() {
-        if (my >= 0) {
-            so[my].w = frac;
-            sd[my].w = __int_as_float(steps);
-        }
-    };
-    // hand the next unissued rays (older slot first) to the lanes in `need`
+    // hand the next rays in ring order to the lanes in `need`
     auto assign = [&](unsigned need) {
-#pragma unroll
-        for (int j = 0; j < kRing; j++) {
-            const int s = j == 0 ? sl.older : 1 - sl.older;
-            if (!need || !sl.valid(s)) continue;
-            const int avail = kTaskRays - sl.issued(s);
-            if (avail <= 0) continue;
-            const int take = min(avail, __popc(need));
-            const int rank = __popc(need & lt_mask);
-            const bool mine = ((need >> lane) & 1u) && rank < take;
-            if (mine) my = s * kTaskRays + sl.issued(s) + rank;
-            need &= ~__ballot_sync(kFull, mine);
-            sl.add_issued(s, take);
+        const int avail = loaded - issued;
+        const int rank = __popc(need & lt_mask);
+        if (((need >> lane) & 1u) && rank < avail) {
+            const int q = issued + rank;
+            const int slot = q & (kRingRays - 1);
+            my = ((q & kTaskRays) ? base1 : base0) + (q & (kTaskRays - 1));
+            const float4 o4 = so[slot], d4 = sd[slot], i4 = si[slot];
+            ox = o4.x; oy = o4.y; oz = o4.z;
+            dx = d4.x; dy = d4.y; dz = d4.z;
+            ivx = i4.x; ivy = i4.y; ivz = i4.z;
+            corner();
+            frac = 0.0f;
+            steps = 0;
         }
+        issued += min(avail, __popc(need));
     };
+    auto more_tasks = [&]() { return pending < 0 && !(exhausted && tb >= te); };
 
     while (true) {
-        bool progress = false;
-        // 1. fill free slots with tasks of the current world
-#pragma unroll
-        for (int s = 0; s < kRing; s++) {
-            if (sl.valid(s)) continue;
+        // 1. set up tasks into free ring halves (a half is free once its rays are handed out)
+        const bool refill = loaded - issued <= kTaskRays && (pending >= 0 || more_tasks());
+        if (refill && my >= 0) {   // park: the setup needs the registers
+            s_park[wib][0][lane] = make_float4(ox, oy, oz, frac);
+            s_park[wib][1][lane] = make_float4(dx, dy, dz, __int_as_float(steps));
+            s_park[wib][2][lane] = make_float4(ivx, ivy, ivz, 0.0f);
+        }
+        bool loaded_now = false;
+        while (refill && loaded - issued <= kTaskRays) {
             const int t = next_task();
             if (t < 0) break;
             if (t < w_begin || t >= w_end) {
-                if (sl.valid0 || sl.valid1) {   // another world: drain this one first
-                    if (pending != t) tb++;
+                const WorldPass* wq = la.n_worlds == 1 ? &la.single : la.worlds + world_of(la, t);
+                if (t >= (int)(wq->task_begin + wq->n_tasks)) {   // alignment gap between worlds
+                    if (pending == t) pending = -1; else tb++;
+                    continue;
+                }
+                if (__any_sync(kFull, my >= 0) || loaded > issued) {
+                    if (pending != t) tb++;   // another world: drain this one first
                     pending = t;
                     break;
                 }
-                if (wi >= 0) flush_stats();
-                wi = world_of(t);
-                wp = la.n_worlds == 1 ? &la.single : la.worlds + wi;
-                mv.X = wp->X; mv.Y = wp->Y; mv.Z = wp->Z;
-                mv.wide = wp->cgrid_wide;
-                mv.cgrid = reinterpret_cast<const uint8_t*>(wp->cgrid);
-                mv.cbits = wp->cbits;
+                wp = wq;
+                mv = march_view(*wp);
                 wx = fmul((float)mv.X, 16.0f); wy = fmul((float)mv.Y, 16.0f); wz = fmul((float)mv.Z, 16.0f);
                 max_dist = wp->max_dist;
                 max_steps = wp->max_steps;
                 w_begin = (int)wp->task_begin;
                 w_end = (int)(wp->task_begin + wp->n_tasks);
             }
-            if (pending == t) pending = -1;
-            else tb++;
-            // setup: lane i builds ray i of the task
-            const long long gr = (long long)(t - w_begin) * kTaskRays + lane;
+            if (pending == t) pending = -1; else tb++;
+            // lane i builds ray i of the task (subgroup k of workgroup g)
+            const int t_local = t - w_begin;
+            const int nsub = wp->R >> 5;
+            const int g = t_local / nsub;
             float3 o, d;
-            setup_ray(*wp, gr, o, d);
-            so[s * kTaskRays + lane] = make_float4(o.x, o.y, o.z, 0.0f);
-            sd[s * kTaskRays + lane] = make_float4(d.x, d.y, d.z, 0.0f);
-            if (!sl.valid(1 - s)) sl.older = s;
-            sl.load(s, t);
-            progress = true;
+            setup_ray(*wp, g, (t_local - g * nsub) * kTaskRays + lane, o, d);
+            const int base = (t - la.chunk_begin) * kTaskRays;
+            const int slot = (loaded & kTaskRays) + lane;
+            const float4 o4 = make_float4(o.x, o.y, o.z, 0.0f), d4 = make_float4(d.x, d.y, d.z, 0.0f);
+            so[slot] = o4;
+            sd[slot] = d4;
+            si[slot] = make_float4(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z), 0.0f);
+            __stcg(la.ray_od + 2 * ((long long)base + lane), o4);
+            __stcg(la.ray_od + 2 * ((long long)base + lane) + 1, d4);
+            if (loaded & kTaskRays) base1 = base; else base0 = base;
+            loaded += kTaskRays;
+            loaded_now = true;
         }
         __syncwarp();
+        if (refill && my >= 0) {
+            const float4 a = s_park[wib][0][lane], b = s_park[wib][1][lane], c = s_park[wib][2][lane];
+            ox = a.x; oy = a.y; oz = a.z; frac = a.w;
+            dx = b.x; dy = b.y; dz = b.z; steps = __float_as_int(b.w);
+            ivx = c.x; ivy = c.y; ivz = c.z;
+            corner();
+        }
+        // 2. idle lanes take rays
         assign(__ballot_sync(kFull, my < 0));
-        if (my >= 0) load_ray(my);   // parked rays resume, idle lanes start fresh ones
-        if (!sl.valid0 && !sl.valid1) {
-            // no more tasks (an empty ring with a task pending cannot happen: step 1 switches
-            // world and loads it; report it rather than loop)
-            if (pending >= 0 && lane == 0) atomicOr(la.error, 2);
+        if (!__any_sync(kFull, my >= 0)) {
+            // nothing in flight and nothing set up: no task was left (a task of another world
+            // would have been set up above, the lanes being drained)
+            if ((pending >= 0 || loaded_now) && lane == 0) atomicOr(la.error, 1);
             break;
         }
-
-        // 2. march until one task has all 32 rays done (or no lane has a ray)
-        int n_active = __popc(__ballot_sync(kFull, my >= 0));
-        while (n_active > 0) {
+        // 3. march; leave to set up more when a ring half is free and tasks may remain
+        while (true) {
             bool fin = false;
-            uint32_t info = 0;
             if (my >= 0) {
                 frac = fadd(frac, 0.5f);
                 steps++;
@@ -575,6 +198,7 @@ radiance_kernel(const __grid_constant__ LaunchArgs la) {
                     const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
                     frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
                 }
+                uint32_t info = 0;
                 if (solid) {
                     fin = true;
                     info = (uint32_t)steps | (1u << 24);
@@ -585,66 +209,25 @@ radiance_kernel(const __grid_constant__ LaunchArgs la) {
                     fin = true;
                     info = (uint32_t)steps | (1u << 25);
                 }
-                if (RECORD && fin) {
-                    int blk;
-                    const int v = voxel_value(*wp, ix, iy, iz, blk);
-                    if (solid) info |= (uint32_t)v << 16;
-                    s_blk[wib][my] = blk;
+                if (fin) {
+                    if (RECORD) {
+                        int blk;
+                        const int v = voxel_value(*wp, ix, iy, iz, blk);
+                        if (solid) info |= (uint32_t)v << 16;
+                        la.ray_blk[my] = blk;
+                    }
+                    __stcg(la.ray_res + my, make_uint2(__float_as_uint(frac), info));
+                    my = -1;
                 }
             }
             const unsigned fm = __ballot_sync(kFull, fin);
             if (fm) {
-                if (fin) {
-                    so[my].w = frac;
-                    sd[my].w = __uint_as_float(info);
-                }
-                const unsigned in1 = __ballot_sync(kFull, fin && my >= kTaskRays);
-                sl.done1 += __popc(in1);
-                sl.done0 += __popc(fm & ~in1);
-                if (fin) my = -1;
                 assign(fm);
-                if (fin && my >= 0) load_ray(my);
-                n_active = __popc(__ballot_sync(kFull, my >= 0));
-                if (sl.complete(0) || sl.complete(1)) break;
+                if (!__any_sync(kFull, my >= 0) || (loaded - issued <= kTaskRays && more_tasks())) break;
             }
-        }
-        park_ray();
-        __syncwarp();
-
-        // 3. finalize every completed task (older first)
-#pragma unroll
-        for (int j = 0; j < kRing; j++) {
-            const int s = j == 0 ? sl.older : 1 - sl.older;
-            if (!sl.complete(s)) continue;
-            const int slot = s * kTaskRays + lane;
-            const float4 o4 = so[slot], d4 = sd[slot];
-            const uint32_t info = __float_as_uint(d4.w);
-            const int t_local = sl.task(s) - w_begin;
-            const long long gr = (long long)t_local * kTaskRays + lane;
-            uint32_t lk;
-            float3 L = finalize_ray<Store, RECORD>(*wp, mv, make_float3(o4.x, o4.y, o4.z), make_float3(d4.x, d4.y, d4.z),
-                                                   o4.w, info, RECORD ? s_blk[wib][slot] : 0, gr, lk);
-            st_lookups += lk;
-            st_hits += (info >> 24) & 1u;
-            L = butterfly_sum(L);
-            const float3 v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
-            const int nsub = wp->R >> 5;
-            const int g = t_local / nsub;
-            const int k = t_local - g * nsub;
-            if (lane == 0) subgroup_done<Store>(*wp, g, k, v);
-            sl.set_valid(s, false);
-            sl.older = 1 - s;
-            progress = true;
-        }
-        __syncwarp();
-        // every round loads or finishes a task; a round without progress would repeat forever
-        if (!progress) {
-            if (lane == 0) atomicOr(la.error, 1);
-            break;
         }
     }
 
-    if (wi >= 0) flush_stats();
     // the last warp to finish resets the queue for the next launch
     if (lane == 0) {
         const unsigned long long e = atomicAdd(la.queue + 1, 1ull);
@@ -655,33 +238,100 @@ radiance_kernel(const __grid_constant__ LaunchArgs la) {
     }
 }
 
+// ---------------------------------------------------------------- finalize kernel
 template <class Store, bool RECORD>
-int grid_size_t(int num_sms) {
+__global__ void __launch_bounds__(kWarps * 32, 4)
+finalize_kernel(const __grid_constant__ LaunchArgs la) {
+    __shared__ float4 s_mean[kWarps];
+    __shared__ int s_count[kWarps];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    if (threadIdx.x < kWarps) s_count[threadIdx.x] = 0;
+    __syncthreads();
+    const int t0 = la.chunk_begin + (int)blockIdx.x * kWarps;   // worlds start at multiples of 8
+    const int t = t0 + w;
+    const WorldPass* wp = la.n_worlds == 1 ? &la.single : la.worlds + world_of(la, t0);
+    const int t_local = t - (int)wp->task_begin;
+    const bool valid = t < la.chunk_end && t_local < wp->n_tasks;
+    const int nsub = wp->R >> 5;
+    const int g = t_local / nsub;
+    const int k = t_local - g * nsub;
+    // a probe's subgroups share this CTA when R/32 divides 8 (task_begin is a multiple of 8)
+    const bool local = nsub > 1 && (kWarps % nsub) == 0 && (wp->task_begin % kWarps) == 0;
+    float3 v = make_float3(0.0f, 0.0f, 0.0f);
+    if (valid) {
+        const long long idx = (long long)(t - la.chunk_begin) * kTaskRays + lane;
+        const float4 o4 = __ldcg(la.ray_od + 2 * idx), d4 = __ldcg(la.ray_od + 2 * idx + 1);
+        const uint2 res = __ldcg(la.ray_res + idx);
+        const int blk = RECORD ? __ldcg(la.ray_blk + idx) : 0;
+        uint32_t lookups;
+        float3 L = finalize_ray<Store, RECORD>(*wp, march_view(*wp), make_float3(o4.x, o4.y, o4.z),
+                                               make_float3(d4.x, d4.y, d4.z), __uint_as_float(res.x), res.y, blk,
+                                               (long long)t_local * kTaskRays + lane, lookups);
+        L = butterfly_sum(L);
+        v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
+        // counters: lookups and hits of this task
+        unsigned a = lookups, h = (res.y >> 24) & 1u;
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) {
+            a += __shfl_xor_sync(kFull, a, m);
+            h += __shfl_xor_sync(kFull, h, m);
+        }
+        if (lane == 0) {
+            atomicAdd(wp->stats, (unsigned long long)a);
+            atomicAdd(wp->stats + 1, (unsigned long long)h);
+            if (!local) {
+                subgroup_done<Store>(*wp, g, k, v);
+            } else {
+                // the last of the probe's subgroups in this CTA sums their means in subgroup
+                // order (radiance.comp:401-407)
+                volatile float* vm = reinterpret_cast<volatile float*>(s_mean);
+                vm[4 * w] = v.x;
+                vm[4 * w + 1] = v.y;
+                vm[4 * w + 2] = v.z;
+                __threadfence_block();
+                if (atomicAdd(&s_count[w - k], 1) == nsub - 1) {
+                    __threadfence_block();
+                    float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+                    for (int j = w - k; j < w - k + nsub; j++) {
+                        const float sx = vm[4 * j], sy = vm[4 * j + 1], sz = vm[4 * j + 2];
+                        acc = make_float3(fadd(acc.x, sx), fadd(acc.y, sy), fadd(acc.z, sz));
+                    }
+                    const float fn = (float)nsub;
+                    acc = make_float3(fdiv_by(acc.x, fn, wp->inv_nsub), fdiv_by(acc.y, fn, wp->inv_nsub),
+                                      fdiv_by(acc.z, fn, wp->inv_nsub));
+                    store_probe<Store>(*wp, g, acc);
+                }
+            }
+        }
+    }
+}
+
+int march_grid(bool record, int num_sms) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, radiance_kernel<Store, RECORD>, kWarps * 32, 0) !=
-            cudaSuccess || per_sm < 1)
-        per_sm = 1;
+    const cudaError_t e = record
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<true>, kWarps * 32, 0)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<false>, kWarps * 32, 0);
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     return num_sms * per_sm;
 }
 
 template <class Store, bool RECORD>
 cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
-    const int blocks = grid_size_t<Store, RECORD>(num_sms);
+    const int blocks = march_grid(RECORD, num_sms);
     LaunchArgs args = a;
     args.total_warps = blocks * kWarps;
-    radiance_kernel<Store, RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
+    for (long long c0 = 0; c0 < a.n_tasks; c0 += kChunkTasks) {
+        args.chunk_begin = (int)c0;
+        args.chunk_end = (int)min(c0 + (long long)kChunkTasks, a.n_tasks);
+        const int n = args.chunk_end - args.chunk_begin;
+        march_kernel<RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
+        finalize_kernel<Store, RECORD><<<(n + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(args);
+    }
     return cudaGetLastError();
 }
 
 }  // namespace
-
-int radiance_grid_size(int precision, bool record, int num_sms) {
-    switch (precision) {
-        case LUMRAD_PRECISION_FP16: return record ? grid_size_t<StoreF16, true>(num_sms) : grid_size_t<StoreF16, false>(num_sms);
-        case LUMRAD_PRECISION_BF16: return record ? grid_size_t<StoreBF16, true>(num_sms) : grid_size_t<StoreBF16, false>(num_sms);
-        default: return record ? grid_size_t<StoreF32, true>(num_sms) : grid_size_t<StoreF32, false>(num_sms);
-    }
-}
 
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream) {
     if (args.n_tasks <= 0) return cudaSuccess;
