@@ -179,6 +179,30 @@ int  lumrad_get_stream(LumRadContext ctx, void** stream);
  * oldest first; *n = number written.  Synchronises. */
 int  lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n);
 
+/* ---- no-allocation pass (no counterpart in the reference) -----------------------------------
+ * One pass like lumrad_radiance_pass, for callers that may not allocate device memory while
+ * they run: engines that reserve their whole device-memory budget up front and forbid later
+ * allocations (an allocation can synchronise the device mid-frame), or hosts whose allocator
+ * owns the device heap.  The call allocates nothing; the caller passes device pointers to the
+ * inputs and the output, and every working buffer lives in one fixed array (about 8.5 MiB)
+ * compiled into this library, which each GPU that loads the library keeps until exit.
+ *   world_size  blocks per axis; X*Y*Z <= LUMRAD_NOALLOC_MAX_BLOCKS, else LUMRAD_EINVAL
+ *   d_grid      X*Y*Z int16 block ids (x-fastest)
+ *   d_palette   n_slots * 4096 uint8 voxels, voxel (x,y,z) at x + 16y + 256z
+ *   d_materials 256 * 4 floats: r, g, b, emission
+ *   d_requests  n * 4 int16 (x, y, z, w)
+ *   d_prev      X*Y*Z * 4 floats (rgb + pad), read;  d_next: same layout, written
+ *   params      rays_per_probe 32, 64, 128 or 256; size >= 1; record_hits 0
+ *   stream      a cudaStream_t (NULL = default stream); the pass is enqueued, not awaited
+ * The first call on a device looks up the array's device address; make that first call before
+ * capturing a stream into a CUDA graph.  All calls share the array: calls that overlap on the
+ * GPU (different streams, or threads) race and give wrong results. */
+#define LUMRAD_NOALLOC_MAX_BLOCKS (1 << 19)
+int  lumrad_radiance_pass_noalloc(const int* world_size, const int16_t* d_grid, const uint8_t* d_palette,
+                                  int n_slots, const float* d_materials, const int16_t* d_requests, int n,
+                                  const float* d_prev, float* d_next, const LumRadPassParams* params,
+                                  void* stream);
+
 /* Direction table used for rays_per_probe = R (sphericalFibonacci, radiance.comp:293-314):
  * R*3 floats.  cos/sin are evaluated in double and rounded to float. */
 int  lumrad_direction_table(int rays_per_probe, float* xyz);

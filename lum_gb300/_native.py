@@ -77,6 +77,8 @@ _SIGS = {
     "lumrad_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lumrad_get_kernel_times": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
     "lumrad_direction_table": (C.c_int, [C.c_int, _P]),
+    "lumrad_radiance_pass_noalloc": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.POINTER(PassParams),
+                                               _P]),
 }
 
 _lib = None

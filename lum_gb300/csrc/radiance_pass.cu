@@ -346,3 +346,212 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
 }
 
 }  // namespace lumrad
+
+// ================================================================ no-allocation entry point
+//
+// lumrad_radiance_pass_noalloc runs the same two kernels as a context's pass, but every working
+// buffer lives in one fixed array compiled into this library (g_noalloc_scratch below), so the
+// call itself never allocates device memory.  It exists for callers that may not allocate while
+// they run a frame: engines that reserve their whole device-memory budget at start-up and forbid
+// allocation afterwards (an allocation can synchronise the device and stall the frame), and hosts
+// whose own allocator owns the device heap.  Such a caller owns the inputs and outputs and passes
+// them as device pointers; the array holds the rest: the compact copy of the world, the rays of
+// one round, the direction table and the queue.
+//
+// Limits: worlds of at most LUMRAD_NOALLOC_MAX_BLOCKS blocks, 32/64/128/256 rays per probe (a
+// probe's subgroups then combine inside one CTA, so no per-probe scratch is needed), FP32
+// radiance, no hit records.  Rounds of kNoAllocRoundTasks tasks.
+
+#include "lumrad_world.h"
+#include <mutex>
+
+namespace lumrad {
+namespace {
+
+constexpr int kNoAllocMaxBlocks = LUMRAD_NOALLOC_MAX_BLOCKS;
+constexpr int kNoAllocRoundTasks = 4096;
+constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+// byte offsets of the parts of the array
+constexpr size_t kNaCgrid = 0;                                                        // uint16 per block
+constexpr size_t kNaCbits = align256(kNaCgrid + 2 * (size_t)kNoAllocMaxBlocks);      // 512 B per compact id
+constexpr size_t kNaRayOd = align256(kNaCbits + (size_t)(LUMRAD_MAX_BLOCK_SLOTS + 2) * 512);
+constexpr size_t kNaRayRes = align256(kNaRayOd + (size_t)kNoAllocRoundTasks * kTaskRays * 2 * sizeof(float4));
+constexpr size_t kNaDirs = align256(kNaRayRes + (size_t)kNoAllocRoundTasks * kTaskRays * sizeof(uint2));
+constexpr size_t kNaQueue = align256(kNaDirs + 256 * sizeof(float4));
+constexpr size_t kNaError = kNaQueue + 2 * sizeof(unsigned long long);
+constexpr size_t kNaStats = align256(kNaError + sizeof(int));
+constexpr size_t kNaBytes = align256(kNaStats + 2 * sizeof(unsigned long long));
+static_assert(kNaBytes <= (9u << 20), "no-allocation scratch must stay under 9 MiB");
+
+}  // namespace
+}  // namespace lumrad
+
+// The scratch array: one per GPU that loads this library, held until the process exits.  In host
+// code `g_noalloc_scratch` only names the symbol; its device address comes from
+// cudaGetSymbolAddress (done once per device, below).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[lumrad::kNaBytes];
+
+namespace lumrad {
+namespace {
+
+// Compact ids for the no-allocation form: 0 for block id 0 (palette slot 0), 1 + slot for a
+// non-zero id with a palette slot, n_slots + 1 (all empty) for any other id.
+__global__ void noalloc_compact_grid(const int16_t* __restrict__ grid, int W, int n_slots, uint16_t* __restrict__ cgrid) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < W; i += gridDim.x * blockDim.x) {
+        const int b = grid[i];
+        const int slot = b < 0 ? b + 64 : b;
+        const bool has = b >= -63 && slot < n_slots;
+        cgrid[i] = (uint16_t)(b == 0 ? 0 : (has ? slot + 1 : n_slots + 1));
+    }
+}
+
+// Occupancy words: entry 0 = slot 0, entry 1 + s = slot s, entry n_slots + 1 = empty.
+__global__ void noalloc_compact_bits(const uint8_t* __restrict__ pal, int n_slots, uint32_t* __restrict__ bits) {
+    const int n_words = (n_slots + 2) * 128;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += gridDim.x * blockDim.x) {
+        const int e = i >> 7, word = i & 127;
+        const int slot = e == 0 ? 0 : e - 1;
+        uint32_t v = 0;
+        if (e <= n_slots) {
+            const uint8_t* p = pal + (size_t)slot * 4096 + word * 32;
+            for (int b = 0; b < 32; b++) v |= (p[b] != 0 ? 1u : 0u) << b;
+        }
+        bits[i] = v;
+    }
+}
+
+struct NoAllocDevice {
+    bool ready = false;
+    unsigned char* base = nullptr;   // device address of g_noalloc_scratch on this device
+    int num_sms = 0;
+};
+std::mutex g_noalloc_mutex;
+NoAllocDevice g_noalloc_dev[64];
+float4 g_noalloc_dirs[4][256];       // host copies of the direction tables for R = 32, 64, 128, 256
+bool g_noalloc_dirs_ready = false;
+
+}  // namespace
+}  // namespace lumrad
+
+using namespace lumrad;
+
+extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t* d_grid, const uint8_t* d_palette,
+                                            int n_slots, const float* d_materials, const int16_t* d_requests, int n,
+                                            const float* d_prev, float* d_next, const LumRadPassParams* p,
+                                            void* stream_handle) {
+    if (!world_size || !d_grid || !d_palette || !d_materials || !d_prev || !d_next || !p || (n > 0 && !d_requests))
+        return fail(LUMRAD_EINVAL, "null argument");
+    int rc = check_params(p);
+    if (rc) return rc;
+    if (p->size < 1) return fail(LUMRAD_EINVAL, "size must be >= 1 (no adaptive slicing here)");
+    if (p->record_hits) return fail(LUMRAD_EINVAL, "hit records need lumrad_radiance_pass");
+    const int R = p->rays_per_probe;
+    if (R != 32 && R != 64 && R != 128 && R != 256) return fail(LUMRAD_EINVAL, "rays_per_probe must be 32, 64, 128 or 256");
+    for (int i = 0; i < 3; i++)
+        if (world_size[i] < 1 || world_size[i] > 2047) return fail(LUMRAD_EINVAL, "world_size must be in [1, 2047] per axis");
+    const long long W = (long long)world_size[0] * world_size[1] * world_size[2];
+    if (W > kNoAllocMaxBlocks) return fail(LUMRAD_EINVAL, "world larger than LUMRAD_NOALLOC_MAX_BLOCKS blocks");
+    if (n_slots < 1 || n_slots > LUMRAD_MAX_BLOCK_SLOTS) return fail(LUMRAD_EINVAL, "n_slots must be in [1, 4096]");
+    if (n < 0) return fail(LUMRAD_EINVAL, "negative request count");
+    const long long groups = n / p->size;
+    const long long n_tasks = groups * (R / 32);
+    if (n_tasks >= (1LL << 31)) return fail(LUMRAD_EINVAL, "pass has too many subgroups (>= 2^31)");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_handle);
+
+    // set-up, once per device: the array's device address (first call on a device; make that
+    // call before capturing a stream into a graph)
+    int dev = 0;
+    LUMRAD_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(LUMRAD_EINVAL, "device ordinal beyond 63");
+    NoAllocDevice* nd = &g_noalloc_dev[dev];
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!nd->ready) {
+            void* addr = nullptr;
+            LUMRAD_TRY(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
+            LUMRAD_TRY(cudaDeviceGetAttribute(&nd->num_sms, cudaDevAttrMultiProcessorCount, dev));
+            nd->base = static_cast<unsigned char*>(addr);
+            nd->ready = true;
+        }
+        if (!g_noalloc_dirs_ready) {
+            const int rs[4] = {32, 64, 128, 256};
+            float xyz[3 * 256];
+            for (int k = 0; k < 4; k++) {
+                fibonacci_table(rs[k], xyz);
+                for (int i = 0; i < rs[k]; i++)
+                    g_noalloc_dirs[k][i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
+            }
+            g_noalloc_dirs_ready = true;
+        }
+    }
+    unsigned char* base = nd->base;
+    uint16_t* cgrid = reinterpret_cast<uint16_t*>(base + kNaCgrid);
+    uint32_t* cbits = reinterpret_cast<uint32_t*>(base + kNaCbits);
+    float4* dirs = reinterpret_cast<float4*>(base + kNaDirs);
+    unsigned long long* queue = reinterpret_cast<unsigned long long*>(base + kNaQueue);
+    int* error = reinterpret_cast<int*>(base + kNaError);
+    unsigned long long* stats = reinterpret_cast<unsigned long long*>(base + kNaStats);
+    const int r_index = R == 32 ? 0 : R == 64 ? 1 : R == 128 ? 2 : 3;
+
+    // everything that must start at zero, and this call's inputs derived into the array
+    LUMRAD_TRY(cudaMemsetAsync(queue, 0, 2 * sizeof(unsigned long long), stream));
+    LUMRAD_TRY(cudaMemsetAsync(error, 0, sizeof(int), stream));
+    LUMRAD_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), stream));
+    LUMRAD_TRY(cudaMemcpyAsync(dirs, g_noalloc_dirs[r_index], R * sizeof(float4), cudaMemcpyHostToDevice, stream));
+    noalloc_compact_grid<<<256, 256, 0, stream>>>(d_grid, (int)W, n_slots, cgrid);
+    noalloc_compact_bits<<<256, 256, 0, stream>>>(d_palette, n_slots, cbits);
+    LUMRAD_TRY(cudaGetLastError());
+    // probes outside the list keep their value
+    LUMRAD_TRY(cudaMemcpyAsync(d_next, d_prev, (size_t)W * sizeof(float4), cudaMemcpyDeviceToDevice, stream));
+    if (n_tasks == 0) return LUMRAD_OK;
+
+    LaunchArgs la;
+    std::memset(&la, 0, sizeof la);
+    WorldPass& w = la.single;
+    w.X = world_size[0]; w.Y = world_size[1]; w.Z = world_size[2];
+    w.cgrid_wide = 1;
+    w.cgrid = cgrid;
+    w.cbits = cbits;
+    w.grid = d_grid;
+    w.pal = d_palette;
+    w.n_slots = n_slots;
+    w.mats = reinterpret_cast<const float4*>(d_materials);
+    w.prev = d_prev;
+    w.next = d_next;
+    w.req = reinterpret_cast<const short4*>(d_requests);
+    w.n_groups = (int)groups;
+    w.size = p->size;
+    w.shift = p->shift;
+    w.R = R;
+    w.max_dist = p->max_dist;
+    w.max_steps = (int)(2.0f * p->max_dist) + 2;
+    w.alpha = p->blend;
+    w.one_minus_alpha = 1.0f - p->blend;
+    w.seed = (uint32_t)p->time_seed;
+    for (int i = 0; i < 3; i++) {
+        const int v = world_size[i];
+        w.inv_dim[i] = (v & (v - 1)) == 0 ? 1.0f / (float)v : 0.0f;
+    }
+    w.inv_nsub = 1.0f / (float)(R / 32);
+    w.dirs = dirs;
+    w.stats = stats;
+    w.task_begin = 0;
+    w.n_tasks = n_tasks;
+    la.n_worlds = 1;
+    la.n_tasks = n_tasks;
+    la.queue = queue;
+    la.error = error;
+    la.ray_od = reinterpret_cast<float4*>(base + kNaRayOd);
+    la.ray_res = reinterpret_cast<uint2*>(base + kNaRayRes);
+    const int blocks = march_grid(false, nd->num_sms);
+    la.total_warps = blocks * kWarps;
+    for (long long c0 = 0; c0 < n_tasks; c0 += kNoAllocRoundTasks) {
+        la.chunk_begin = (int)c0;
+        la.chunk_end = (int)std::min(c0 + (long long)kNoAllocRoundTasks, n_tasks);
+        const int tasks = la.chunk_end - la.chunk_begin;
+        march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(la);
+        finalize_kernel<StoreF32, false><<<(tasks + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(la);
+    }
+    LUMRAD_TRY(cudaGetLastError());
+    return LUMRAD_OK;
+}
