@@ -8,7 +8,8 @@ in the shader fails the build instead of silently drifting:
 
   R1  drop `#version`, `#extension` and `precision` lines; inline the two `#include`s;
   R2  the descriptor bindings (radiance.comp:16-25) become shim resources the harness binds;
-  R3  the specialization and push constants (:27-35) become mutable globals of the same names;
+  R3  the specialization and push constants (:27-35) become mutable globals of the same names
+      (the int constant typed so that `%` on it keeps GLSL's OpSMod semantics);
   R4  `in T x` / `out T x` parameters become `T x` / `T& x`;
   R5  `#define RAYS_PER_PROBE (64)` takes the compile-time value LUMREF_R (built for 32..256);
   R6  `float max_dist = 16.0*8.0;` (the shader's TODO quality setting) reads a global;
@@ -73,8 +74,9 @@ def adapt(shader: str, consts: str) -> str:
     s = _sub(r"layout\(std430,set = 0, binding = 5\) restrict readonly buffer (\w+)\{\s*(\w+) (\w+)\[\];\s*\} (\w+);",
              _keep_lines(lambda m: f"struct {m.group(1)} {{ const {m.group(2)}* {m.group(3)}; }} {m.group(4)};"),
              s, 1)
-    # R3
-    s = _sub(r"layout\(constant_id = \d\) const (\w+) (\w+) = ([^;]+);", r"\1 \2 = \3;", s, 2)
+    # R3 (an int constant gets the shim's glsl_int type: `%` on it is OpSMod, as in SPIR-V)
+    s = _sub(r"layout\(constant_id = \d\) const int (\w+) = ([^;]+);", r"glsl_int \1 = \2;", s, 1)
+    s = _sub(r"layout\(constant_id = \d\) const float (\w+) = ([^;]+);", r"float \1 = \2;", s, 1)
     s = _sub(r"layout\(push_constant\) uniform restrict readonly (\w+)\{([^}]*)\} (\w+);",
              _keep_lines(lambda m: f"struct {m.group(1)} {{{' '.join(m.group(2).split())}}} {m.group(3)};"), s, 1)
     # R4

@@ -184,6 +184,16 @@ inline int smod(int a, int b) {
 }
 inline ivec3 operator%(ivec3 a, int s) { return ivec3(smod(a.x, s), smod(a.y, s), smod(a.z, s)); }  // OpSMod
 
+// An int specialization constant.  C++ gives `int % int` truncated semantics; GLSL's signed `%`
+// is OpSMod, so integer constants carry this type and `int % constant` follows SPIR-V.
+struct glsl_int {
+    int v;
+    glsl_int(int x) : v(x) {}
+    operator int() const { return v; }
+};
+inline int operator%(int a, glsl_int b) { return smod(a, b.v); }
+inline int operator/(int a, glsl_int b) { return a / b.v; }
+
 inline uvec3 operator>>(uvec3 a, uint s) { return uvec3(a.x >> s, a.y >> s, a.z >> s); }
 inline uvec3 operator^(uvec3 a, uvec3 b) { return uvec3(a.x ^ b.x, a.y ^ b.y, a.z ^ b.z); }
 inline uvec3 operator*(uvec3 a, uint s) { return uvec3(a.x * s, a.y * s, a.z * s); }
