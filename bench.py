@@ -9,12 +9,13 @@ Workload (one "step"): the 64x64x16-block terrain world plus 2000 random blocks 
              between steps, outside the timed region.
   e2e        the same metric through the C ABI with host buffers: each pass copies its request
              list host->device, each step reads the radiance volume back.
-  roofline   algorithmic bytes of the pass kernel per launch (3 B per grid+palette lookup,
-             16+8*12 B per hit, 8+2*12 B per probe; counts exact from the kernel's counters)
-             over the kernel's own event-timed duration, against the measured HBM copy peak.
-  cpu_baseline  the CPU oracle (OpenMP, all host cores) on a bounded sample of pass 0.
+  roofline   algorithmic bytes of one pass (3 B per grid+palette lookup, 16+8*12 B per hit,
+             8+2*12 B per probe; counts exact from the kernels' counters) over the pass kernels'
+             own event-timed duration (march + finalize), against the measured HBM copy peak.
+  cpu_baseline  the CPU oracle (port, OpenMP over all host cores) on whole steps, ~12 s.
 
---impl reference times the CPU implementation of the same workload on the host cores.
+--impl reference times the reference's implementation of the same workload on the host cores:
+Lum's radiance.comp compiled as C++ from its source (oracle/build_ref.py), one process per core.
 """
 from __future__ import annotations
 
@@ -115,20 +116,50 @@ class ClockSampler:
 
 
 def cpu_baseline(world, lists, budget_s: float = 12.0):
-    """The CPU oracle (OpenMP over probes, all host cores) on a bounded prefix of pass 0."""
+    """The CPU oracle (the port: OpenMP over workgroups, all host cores) on whole steps of the
+    workload, repeated until about `budget_s` seconds of CPU work."""
     import oracle
-    req = lists[0]
     cores = oracle.max_threads()
-    n = min(64, req.shape[0])
+    prev = np.zeros(world.grid.shape + (3,), dtype=np.float32)
+    steps = 0
     t0 = time.perf_counter()
-    oracle.radiance_pass(world, req[:n], rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=0)
-    dt = max(time.perf_counter() - t0, 1e-6)
-    n = int(min(req.shape[0], max(n, n * budget_s / dt)))
-    t0 = time.perf_counter()
-    oracle.radiance_pass(world, req[:n], rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=0)
-    dt = time.perf_counter() - t0
-    return {"value": n * RAYS / dt, "unit": "probe-rays/s", "cores": cores, "kind": "port",
-            "sample": f"first {n} probes of pass 0 ({n * RAYS} rays), one pass, {dt:.1f} s"}
+    while True:
+        cur = prev
+        for p in range(PASSES):
+            cur, _, _ = oracle.radiance_pass(world, lists[p], rays=RAYS, max_dist=MAX_DIST, blend=BLEND,
+                                             time_seed=p, prev=cur)
+        steps += 1
+        dt = time.perf_counter() - t0
+        if dt >= budget_s:
+            break
+    rays = steps * sum(l.shape[0] for l in lists) * RAYS
+    return {"value": rays / dt, "unit": "probe-rays/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} full steps (8 passes x 6554 probes x 256 rays), {dt:.1f} s"}
+
+
+def reference_runner(world):
+    """Runs a pass of the reference's own shader code (radiance.comp compiled as C++) on all host
+    cores, or, where it cannot be built, the port.  Returns (run(req, prev, seed) -> next, kind, cores)."""
+    from oracle import build_ref
+    try:
+        if not build_ref.available():
+            raise RuntimeError("no reference shader source")
+        build_ref.build(rays=(RAYS,))
+        from oracle import ref_pool
+        pool = ref_pool.RefPool(world, RAYS)
+
+        def run(req, prev, seed):
+            return pool.run_pass(req.astype(np.int8), prev, max_dist=MAX_DIST, blend=BLEND, time_seed=seed)
+        run.close = pool.close
+        return run, "reference", pool.processes
+    except Exception:
+        import oracle
+
+        def run(req, prev, seed):
+            return oracle.radiance_pass(world, req, rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=seed,
+                                        prev=prev)[0]
+        run.close = lambda: None
+        return run, "port", oracle.max_threads()
 
 
 def dist_setup(args):
@@ -146,14 +177,14 @@ def dist_setup(args):
 
 
 def run_reference(args, rank, world_size, pg):
-    """CPU implementation of the same workload (the oracle, OpenMP over all host cores)."""
+    """The reference's implementation of the same workload on the host cores: Lum's
+    radiance.comp compiled as C++ (its Vulkan path is unavailable on this machine), one process per
+    core; the port (OpenMP) where that cannot be built."""
     if rank != 0:
         return
-    import oracle
     world = worldgen.demo_world(SEED)
     lists = pass_lists(world.dims)
-    cores = oracle.max_threads()
-    n_sample = 192        # probes per pass per step: a bounded sample of each pass
+    run, kind, cores = reference_runner(world)
     prev = np.zeros(world.grid.shape + (3,), dtype=np.float32)
     t_total = 0.0
     rays_total = 0
@@ -161,23 +192,24 @@ def run_reference(args, rank, world_size, pg):
         cur = prev
         t0 = time.perf_counter()
         for p in range(PASSES):
-            cur, _, _ = oracle.radiance_pass(world, lists[p][:n_sample], rays=RAYS, max_dist=MAX_DIST,
-                                             blend=BLEND, time_seed=p, prev=cur)
+            cur = run(lists[p], cur, p)
         dt = time.perf_counter() - t0
         if step >= args.warmup:
             t_total += dt
-            rays_total += PASSES * n_sample * RAYS
+            rays_total += sum(l.shape[0] for l in lists) * RAYS
+    run.close()
     value = rays_total / t_total
+    sample = "full steps: 8 passes x 6554 probes x 256 rays"
     line = {"metric": "probe-rays/s", "value": value, "unit": "probe-rays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded terrain world)", "impl": "reference",
-            "config": dict(WORKLOAD, sample=f"first {n_sample} probes of each of the 8 passes per step"),
-            "cpu_baseline": {"value": value, "unit": "probe-rays/s", "cores": cores, "kind": "port",
-                             "sample": f"first {n_sample} probes of each pass, {PASSES} passes per step"},
+            "data": "synthetic (seeded value-noise terrain, splitmix64)", "impl": "reference",
+            "config": dict(WORKLOAD, sample=sample),
+            "cpu_baseline": {"value": value, "unit": "probe-rays/s", "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "probe-rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference's own implementation is a Vulkan compute shader (unavailable on this box); "
-                    "this arm runs the CPU restatement of it"}
+            "note": ("Lum's shaders/radiance.comp compiled as C++ from its source, one process per host core; "
+                     "its Vulkan path is unavailable on this box") if kind == "reference" else
+                    "the CPU restatement (port) of radiance.comp, OpenMP over all host cores"}
     print(json.dumps(line))
 
 
@@ -300,7 +332,7 @@ def main():
                          "ray_steps_per_s": float(np.mean(pass_steps)) / kern_avg_s},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "gpu_launches": PASSES * args.steps,
+            "gpu_launches": 2 * PASSES * args.steps,   # march + finalize per pass
         }
         print(json.dumps(line))
     rw.close()

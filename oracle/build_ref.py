@@ -116,10 +116,23 @@ def lib_path(rays: int) -> str:
     return os.path.join(OUT, f"libradiance_ref_r{rays}.so")
 
 
+def generated_source() -> str:
+    return os.path.join(OUT, "radiance_ref.cpp")
+
+
+def available() -> bool:
+    """The reference shader can be built here: from its sources, or from the C++ generated from
+    them (which travels with the repository's build outputs to machines without the sources)."""
+    return reference_present() or os.path.exists(generated_source())
+
+
 def build(rays=RAYS) -> list[str]:
-    if not reference_present():
-        raise RuntimeError(f"reference shader not found at {SHADER}")
-    src = generate()
+    if reference_present():
+        src = generate()
+    elif os.path.exists(generated_source()):
+        src = generated_source()
+    else:
+        raise RuntimeError(f"reference shader not found at {SHADER} and no generated source")
 
     def one(r):
         tmp = lib_path(r) + ".tmp"

@@ -19,6 +19,7 @@
 #pragma once
 
 #include <cmath>
+#include <csetjmp>
 #include <cstdint>
 #include <cstring>
 #include <initializer_list>
@@ -227,8 +228,11 @@ inline bvec3 greaterThanEqual(vec3 a, vec3 b) { return bvec3(a.x >= b.x, a.y >= 
 inline bool any(bvec3 b) { return b.x || b.y || b.z; }
 
 // ---------------------------------------------------------------- resources
-struct Runaway {};   // a ray whose march exceeded the fetch budget (only a NaN fraction can)
-struct Suspend {};   // unwinds one invocation at a subgroup operation or a barrier
+// An invocation is suspended at a subgroup operation or a barrier, or abandoned when its march
+// exceeds the fetch budget (only a NaN fraction can), by a longjmp back to the harness (every frame
+// it skips is trivially destructible).
+constexpr int kSuspend = 1, kRunaway = 2;
+inline std::jmp_buf g_jump;
 
 struct ShimState {
     long long block_fetches = 0;
@@ -245,7 +249,7 @@ struct sampler3D { const float* rgb = nullptr; int X = 0, Y = 0, Z = 0; };
 struct image3D { float* rgb = nullptr; int X = 0, Y = 0, Z = 0; };
 
 inline ivec4 texelFetch(const isampler3D& s, ivec3 p, int) {
-    if (++g_shim.block_fetches > g_shim.fetch_limit) throw Runaway();
+    if (++g_shim.block_fetches > g_shim.fetch_limit) std::longjmp(g_jump, kRunaway);
     g_shim.last_block = p;
     ivec4 r;
     if (p.x >= 0 && p.y >= 0 && p.z >= 0 && p.x < s.X && p.y < s.Y && p.z < s.Z)
@@ -326,13 +330,13 @@ inline int gl_SubgroupID = 0;
 inline vec3 subgroupAdd(vec3 v) {
     if (g_inv.phase == kCollect) {
         g_inv.collected[gl_SubgroupID * 32 + g_inv.lane] = v;
-        throw Suspend();
+        std::longjmp(g_jump, kSuspend);
     }
     return g_inv.sums[gl_SubgroupID];
 }
 inline bool subgroupElect() { return g_inv.lane == 0; }
 inline void barrier() {
-    if (g_inv.phase == kToBarrier) throw Suspend();
+    if (g_inv.phase == kToBarrier) std::longjmp(g_jump, kSuspend);
 }
 
 }  // namespace lumref
