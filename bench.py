@@ -165,6 +165,69 @@ def reference_runner(world):
         return run, "port", oracle.max_threads()
 
 
+BATCH_WORKLOAD = {
+    "workload": "batched radiance update: 256 independent terrain worlds, dims uniform per axis in "
+                "4x4x4..32x32x16 blocks, update lists U(1%,100%) of each world's probes, rays/probe "
+                "one of {32,64,128,256}, max_dist 128, blend 0.1, FP32",
+    "worlds": 256, "min_blocks": [4, 4, 4], "max_blocks": [32, 32, 16], "seed": SEED,
+}
+
+
+def batched_leg(local: int, steps: int, warmup: int, flush):
+    """Mixed-size workload: one autotuned batch (one graph replay per step, all 256 worlds in the
+    same persistent launches) against the plain path (one pass per world, each world alone)."""
+    import torch
+    import lum_gb300
+    mix = worldgen.mixed_worlds(n=BATCH_WORKLOAD["worlds"], seed=SEED)
+    rws = []
+    for w, req, r in mix:
+        rw = lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], device=local)
+        rw.load(w)
+        rws.append(rw)
+    rays_per_step = sum(req.shape[0] * r for _, req, r in mix)
+    tasks = sum((req.shape[0] * r // 32 + 7) // 8 * 8 for _, req, r in mix)   # 32-ray subgroups, 8-aligned
+    out = {"config": dict(BATCH_WORKLOAD, rays_per_step=rays_per_step,
+                          probes_per_step=int(sum(req.shape[0] for _, req, _ in mix)),
+                          l2="flushed between steps (256 MiB write)")}
+    with lum_gb300.RadianceBatch(rws) as b:
+        for i, (w, req, r) in enumerate(mix):
+            b.set_requests(i, req, lum_gb300.pass_params(rays=r, max_dist=128.0, blend=0.1))
+        t0 = time.perf_counter()
+        tuning = b.autotune(repeats=3)
+        out["tuning"] = dict(tuning, seconds=round(time.perf_counter() - t0, 2))
+        for k in range(warmup):
+            b.run(k)
+        b.synchronize()
+        ms = []
+        for k in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            b.run(k)
+            b.synchronize()
+            ms.append(b.last_ms())
+        st = b.stats()
+        batched = rays_per_step / (np.mean(ms) / 1000.0)
+        for k in range(warmup):
+            b.run_per_world(k)
+        b.synchronize()
+        pms = []
+        for k in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            b.run_per_world(k)
+            b.synchronize()
+            pms.append(b.last_ms())
+        plain = rays_per_step / (np.mean(pms) / 1000.0)
+    for rw in rws:
+        rw.close()
+    out.update({"value": batched, "unit": "probe-rays/s", "ms_per_step": float(np.mean(ms)),
+                "plain_value": plain, "plain_ms_per_step": float(np.mean(pms)),
+                "speedup_vs_plain": batched / plain, "steps": steps,
+                "ray_steps_per_s": st["steps"] / (ms[-1] / 1000.0),
+                "gpu_launches_per_step": 1 + 2 * -(-tasks // 65536)})
+    return out
+
+
 def dist_setup(args):
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -223,7 +286,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--legs", default="demo,batched",
+                    help="comma list of legs: demo (the headline line), batched (the mixed-size batch)")
     args = ap.parse_args()
+    legs = set(args.legs.split(","))
     rank, local, world_size, pg = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world_size, pg)
@@ -321,6 +387,10 @@ def main():
     h2d = int(sum(l.shape[0] * 8 for l in lists))
     d2h = int(world.n_blocks * 16)
 
+    batched = None
+    if "batched" in legs:
+        batched = batched_leg(local, max(3, args.steps // 2), args.warmup, flush)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(world, lists)
@@ -342,6 +412,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": 2 * PASSES * args.steps,   # march + finalize per pass
+            "batched": batched,
         }
         print(json.dumps(line))
     rw.close()

@@ -179,6 +179,43 @@ int  lumrad_get_stream(LumRadContext ctx, void** stream);
  * oldest first; *n = number written.  Synchronises. */
 int  lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n);
 
+/* ---- batches: many worlds, one launch ------------------------------------------------------
+ * The reference updates one world per frame with one dispatch and time-slices its probes
+ * (internal_render.cpp:1190-1206).  A batch updates many resident worlds (contexts on one device,
+ * one precision) of any sizes, list lengths and ray counts in one launch of the pass kernels,
+ * captured once into a CUDA graph and replayed per run.  While a context belongs to a batch, run
+ * its passes through the batch; call lumrad_batch_synchronize before reading its volume. */
+typedef void* LumRadBatch;
+
+/* Scheduling of the march queue: a warp claims remaining/(guided_div*warps) tasks at a time,
+ * at most max_chunk; march_ctas CTAs per SM (0 = as many as fit).  pass_ms: autotune's timing. */
+typedef struct {
+    int   guided_div;
+    int   max_chunk;
+    int   march_ctas;
+    float pass_ms;
+} LumRadTuning;
+
+int  lumrad_batch_create(LumRadContext const* worlds, int n_worlds, LumRadBatch* out);
+void lumrad_batch_destroy(LumRadBatch batch);
+/* World `world`'s update list (x,y,z,w int16) and parameters (size >= 1, no hit records). */
+int  lumrad_batch_set_requests(LumRadBatch batch, int world, const int16_t* requests, int n,
+                               const LumRadPassParams* params);
+/* One pass of every world in one graph replay; time_seed replaces each world's seed. */
+int  lumrad_batch_run(LumRadBatch batch, int time_seed);
+/* The same pass as one launch per world on each context's stream, waiting for each: the plain
+ * one-launch-per-world path, for comparison. */
+int  lumrad_batch_run_per_world(LumRadBatch batch, int time_seed);
+int  lumrad_batch_synchronize(LumRadBatch batch);
+/* Device time of the last lumrad_batch_run (wall time of the last lumrad_batch_run_per_world). */
+int  lumrad_batch_last_ms(LumRadBatch batch, float* ms);
+int  lumrad_batch_set_tuning(LumRadBatch batch, const LumRadTuning* tuning);
+/* Times every candidate setting (repeats runs each, after one warm-up run) on this batch, keeps
+ * the fastest and returns it.  Runs real passes; the volumes are restored afterwards. */
+int  lumrad_batch_autotune(LumRadBatch batch, int repeats, LumRadTuning* best);
+/* Counters of the last run summed over the worlds. */
+int  lumrad_batch_stats(LumRadBatch batch, LumRadPassStats* out);
+
 /* ---- no-allocation pass (no counterpart in the reference) -----------------------------------
  * One pass like lumrad_radiance_pass, for callers that may not allocate device memory while
  * they run: engines that reserve their whole device-memory budget up front and forbid later

@@ -171,6 +171,64 @@ class RadianceWorld:
         return {"probes": s.probes, "rays": s.rays, "steps": s.steps, "hits": s.hits, "gpu_ms": s.gpu_ms}
 
 
+class RadianceBatch:
+    """Many RadianceWorlds updated by one graph-replayed launch (lumrad_batch_*)."""
+
+    def __init__(self, worlds):
+        self.lib = load()
+        self.worlds = list(worlds)
+        arr = (C.c_void_p * len(self.worlds))(*[w.h.value for w in self.worlds])
+        h = C.c_void_p()
+        check(self.lib.lumrad_batch_create(arr, len(self.worlds), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lumrad_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_requests(self, i: int, requests: np.ndarray, params: PassParams) -> None:
+        req = np.ascontiguousarray(requests, dtype=np.int16)
+        check(self.lib.lumrad_batch_set_requests(self.h, i, ptr(req), req.shape[0], C.byref(params)))
+
+    def run(self, time_seed: int = 0) -> None:
+        check(self.lib.lumrad_batch_run(self.h, time_seed))
+
+    def run_per_world(self, time_seed: int = 0) -> None:
+        check(self.lib.lumrad_batch_run_per_world(self.h, time_seed))
+
+    def synchronize(self) -> None:
+        check(self.lib.lumrad_batch_synchronize(self.h))
+
+    def last_ms(self) -> float:
+        ms = C.c_float()
+        check(self.lib.lumrad_batch_last_ms(self.h, C.byref(ms)))
+        return float(ms.value)
+
+    def set_tuning(self, guided_div: int = 2, max_chunk: int = 16, march_ctas: int = 0) -> None:
+        from ._native import Tuning
+        t = Tuning(guided_div, max_chunk, march_ctas, 0.0)
+        check(self.lib.lumrad_batch_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, repeats: int = 3) -> dict:
+        from ._native import Tuning
+        t = Tuning()
+        check(self.lib.lumrad_batch_autotune(self.h, repeats, C.byref(t)))
+        return {"guided_div": t.guided_div, "max_chunk": t.max_chunk, "march_ctas": t.march_ctas,
+                "pass_ms": t.pass_ms}
+
+    def stats(self) -> dict:
+        s = PassStats()
+        check(self.lib.lumrad_batch_stats(self.h, C.byref(s)))
+        return {"probes": s.probes, "rays": s.rays, "steps": s.steps, "hits": s.hits, "gpu_ms": s.gpu_ms}
+
+
 def direction_table(rays: int) -> np.ndarray:
     out = np.zeros((rays, 3), dtype=np.float32)
     check(load().lumrad_direction_table(rays, ptr(out)))

@@ -43,6 +43,10 @@ class PassStats(C.Structure):
                 ("hits", C.c_uint64), ("gpu_ms", C.c_float)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("guided_div", C.c_int), ("max_chunk", C.c_int), ("march_ctas", C.c_int), ("pass_ms", C.c_float)]
+
+
 # LumRadHit as a numpy record (24 bytes, same layout as the C struct)
 HIT_DTYPE = np.dtype([("voxel", "<i4", (3,)), ("block", "<i2"), ("voxel_id", "u1"), ("flags", "u1"),
                       ("coarse_steps", "<u2"), ("refine_steps", "u1"), ("coarse_voxel", "u1"),
@@ -79,6 +83,16 @@ _SIGS = {
     "lumrad_direction_table": (C.c_int, [C.c_int, _P]),
     "lumrad_radiance_pass_noalloc": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.POINTER(PassParams),
                                                _P]),
+    "lumrad_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(_P)]),
+    "lumrad_batch_destroy": (None, [_P]),
+    "lumrad_batch_set_requests": (C.c_int, [_P, C.c_int, _P, C.c_int, C.POINTER(PassParams)]),
+    "lumrad_batch_run": (C.c_int, [_P, C.c_int]),
+    "lumrad_batch_run_per_world": (C.c_int, [_P, C.c_int]),
+    "lumrad_batch_synchronize": (C.c_int, [_P]),
+    "lumrad_batch_last_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "lumrad_batch_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "lumrad_batch_autotune": (C.c_int, [_P, C.c_int, C.POINTER(Tuning)]),
+    "lumrad_batch_stats": (C.c_int, [_P, C.POINTER(PassStats)]),
 }
 
 _lib = None

@@ -215,6 +215,17 @@ int DeviceWorld::ensure_hits(size_t n) {
 // (size >= 1) reading rad[cur] and writing rad[1-cur].
 int DeviceWorld::prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream,
                               WorldPass* out) {
+    int rc = fill_pass(d_req, n, p, stream, out);
+    if (rc) return rc;
+    // probes not in the list keep their value: next starts as a copy of prev
+    LUMRAD_TRY(cudaMemcpyAsync(d_rad[1 - cur], d_rad[cur], W * rad_stride, cudaMemcpyDeviceToDevice, stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
+    return LUMRAD_OK;
+}
+
+// The kernels' descriptor of a pass (inputs synced to the device, buffers sized); no copies.
+int DeviceWorld::fill_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream,
+                           WorldPass* out) {
     int rc = sync_inputs(stream);
     if (rc) return rc;
     const float4* dirs = nullptr;
@@ -259,9 +270,6 @@ int DeviceWorld::prepare_pass(const short4* d_req, int n, const LumRadPassParams
     w.n_tasks = (long long)groups * (R / 32);
     hits_recorded = p.record_hits != 0;
     hits_n = p.record_hits ? (size_t)groups * R : 0;
-    // probes not in the list keep their value: next starts as a copy of prev
-    LUMRAD_TRY(cudaMemcpyAsync(d_rad[1 - cur], d_rad[cur], W * rad_stride, cudaMemcpyDeviceToDevice, stream));
-    LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
     return LUMRAD_OK;
 }
 

@@ -63,6 +63,16 @@ struct LaunchArgs {
     float4* ray_od;              // per ray of the round: origin (xyz), direction (xyz)
     uint2* ray_res;              // per ray of the round: coarse fraction bits, info word
     int* ray_blk;                // per ray of the round: block id at the last coarse step (records)
+    // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
+    // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
+    int guided_div, max_chunk, march_ctas;
+};
+
+// Tunable scheduling of a launch (see LaunchArgs); the defaults are 2, 16 and the occupancy limit.
+struct Tuning {
+    int guided_div = 2;
+    int max_chunk = 16;
+    int march_ctas = 0;
 };
 
 // Runs one pass over the worlds of `args` (descriptors already on the device when n_worlds > 1)
@@ -70,5 +80,9 @@ struct LaunchArgs {
 // kernel.  Returns a CUDA error code.
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms,
                             cudaStream_t stream);
+
+// Start of a multi-world pass: copies every world's prev volume into its next volume and clears
+// its counters (descriptors already on the device).
+cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream);
 
 }  // namespace lumrad

@@ -72,6 +72,7 @@ struct DeviceWorld {
     int ensure_scratch(size_t groups, int R);
     int ensure_hits(size_t n);
     int prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, WorldPass* out);
+    int fill_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, WorldPass* out);
 };
 
 // A LumRadContext: one world plus its stream, events and request staging.

@@ -70,8 +70,10 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             if (lane == 0) {
                 const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(la.queue);
                 const long long rem = (long long)n_round - (long long)cur;
-                const long long kk = rem / (2LL * la.total_warps);
-                k = (unsigned long long)(kk < 1 ? 1 : (kk > 16 ? 16 : kk));
+                const long long div = la.guided_div > 0 ? la.guided_div : 2;
+                const long long cap = la.max_chunk > 0 ? la.max_chunk : 16;
+                const long long kk = rem / (div * la.total_warps);
+                k = (unsigned long long)(kk < 1 ? 1 : (kk > cap ? cap : kk));
                 start = atomicAdd(la.queue, k);
             }
             start = __shfl_sync(kFull, start, 0);
@@ -307,18 +309,19 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     }
 }
 
-int march_grid(bool record, int num_sms) {
+int march_grid(bool record, int num_sms, int ctas_per_sm = 0) {
     int per_sm = 0;
     const cudaError_t e = record
         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<true>, kWarps * 32, 0)
         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<false>, kWarps * 32, 0);
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     return num_sms * per_sm;
 }
 
 template <class Store, bool RECORD>
 cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
-    const int blocks = march_grid(RECORD, num_sms);
+    const int blocks = march_grid(RECORD, num_sms, a.march_ctas);
     LaunchArgs args = a;
     args.total_warps = blocks * kWarps;
     for (long long c0 = 0; c0 < a.n_tasks; c0 += kChunkTasks) {
@@ -343,6 +346,34 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
         default:
             return record ? launch_t<StoreF32, true>(args, num_sms, stream) : launch_t<StoreF32, false>(args, num_sms, stream);
     }
+}
+
+}  // namespace lumrad
+
+namespace lumrad {
+namespace {
+
+// Start of a batched pass: each world's next volume becomes a copy of its previous one (probes
+// not in its list keep their value) and its counters are cleared.  blockIdx.y = world.
+template <typename V>
+__global__ void prep_kernel(const WorldPass* __restrict__ worlds) {
+    const WorldPass& w = worlds[blockIdx.y];
+    const long long n = (long long)w.X * w.Y * w.Z;
+    const V* src = reinterpret_cast<const V*>(w.prev);
+    V* dst = reinterpret_cast<V*>(w.next);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x < 2) w.stats[threadIdx.x] = 0;
+}
+
+}  // namespace
+
+cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream) {
+    if (n_worlds <= 0) return cudaSuccess;
+    const dim3 grid(32, n_worlds);
+    if (precision == LUMRAD_PRECISION_FP32) prep_kernel<uint4><<<grid, 256, 0, stream>>>(d_worlds);
+    else prep_kernel<uint2><<<grid, 256, 0, stream>>>(d_worlds);
+    return cudaGetLastError();
 }
 
 }  // namespace lumrad

@@ -171,6 +171,23 @@ def probe_subset(dims: tuple[int, int, int], fraction: float, seed: int, stream:
     return np.ascontiguousarray(allp[idx])
 
 
+def mixed_worlds(n: int = 256, seed: int = 1234, max_dims=(32, 32, 16), min_dims=(4, 4, 4),
+                 rays=(32, 64, 128, 256)):
+    """The batching workload: n independent terrain worlds with dims uniform per axis in
+    [min, max], each with a seeded update list of U(1%, 100%) of its probes and rays per probe
+    drawn from `rays`.  Returns [(World, requests, rays_per_probe)]."""
+    out = []
+    u = uniform(seed, 9001, 5 * n).reshape(n, 5)
+    for i in range(n):
+        dims = tuple(int(lo + np.floor(u[i, a] * (hi - lo + 1))) for a, (lo, hi) in enumerate(zip(min_dims, max_dims)))
+        w = terrain_world(dims, seed=seed * 1000 + i, n_types=32)
+        frac = 0.01 + 0.99 * u[i, 3]
+        req = probe_subset(dims, frac, seed=seed * 1000 + i, stream=0)
+        r = int(rays[min(int(u[i, 4] * len(rays)), len(rays) - 1)])
+        out.append((w, req, r))
+    return out
+
+
 def small_world(dims=(8, 8, 8), seed: int = 1234) -> World:
     """The 8x8x8 terrain world with 32 block types."""
     return terrain_world(dims, seed=seed, n_types=32)

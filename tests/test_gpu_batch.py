@@ -1,0 +1,89 @@
+"""Batches: many worlds in one graph-replayed launch (lumrad_batch_*).
+
+Each world's result in the batch must equal the CPU oracle's for that world alone (worlds are
+independent: a ray's seed depends only on its own world's workgroup and ray index), equal the
+world run alone through its own context, and the per-world baseline path must agree too.
+"""
+import numpy as np
+import pytest
+
+from lum_gb300 import worldgen
+from tests.helpers import RTOL, random_prev, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _make(mix, precision="fp32"):
+    import lum_gb300
+    rws = []
+    for i, (w, req, r) in enumerate(mix):
+        rw = lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], precision=precision)
+        rw.load(w)
+        rw.set_radiance(random_prev(w, seed=100 + i))
+        rws.append(rw)
+    return rws
+
+
+def test_batch_matches_oracle_and_solo_runs():
+    import lum_gb300
+    import oracle
+    mix = worldgen.mixed_worlds(n=7, seed=5, max_dims=(12, 10, 8))
+    rws = _make(mix)
+    with lum_gb300.RadianceBatch(rws) as b:
+        for i, (w, req, r) in enumerate(mix):
+            b.set_requests(i, req, lum_gb300.pass_params(rays=r, max_dist=128.0, blend=0.1))
+        for seed in (3, 4):
+            b.run(seed)
+        b.synchronize()
+        got = [rw.get_radiance() for rw in rws]
+        st = b.stats()
+    for i, (w, req, r) in enumerate(mix):
+        cur = random_prev(w, seed=100 + i)
+        for seed in (3, 4):
+            cur, _, _ = oracle.radiance_pass(w, req, rays=r, max_dist=128.0, blend=0.1, time_seed=seed, prev=cur)
+        assert rel_err(got[i], cur).max() <= RTOL, (i, rel_err(got[i], cur).max())
+    assert st["rays"] == sum(req.shape[0] * r for _, req, r in mix)
+    for rw in rws:
+        rw.close()
+
+
+def test_per_world_path_and_autotune_restore():
+    import lum_gb300
+    mix = worldgen.mixed_worlds(n=5, seed=9, max_dims=(10, 10, 6))
+    a = _make(mix)
+    bws = _make(mix)
+    with lum_gb300.RadianceBatch(a) as ba, lum_gb300.RadianceBatch(bws) as bb:
+        for i, (w, req, r) in enumerate(mix):
+            p = lum_gb300.pass_params(rays=r, max_dist=200.0, blend=0.2)
+            ba.set_requests(i, req, p)
+            bb.set_requests(i, req, p)
+        best = ba.autotune(repeats=1)
+        assert best["max_chunk"] >= 1 and best["pass_ms"] > 0
+        ba.run(7)
+        bb.run_per_world(7)
+        ba.synchronize()
+        bb.synchronize()
+        for x, y in zip(a, bws):
+            assert np.array_equal(x.get_radiance(), y.get_radiance())
+    for rw in a + bws:
+        rw.close()
+
+
+def test_batch_in_the_mix_equals_alone():
+    """A world's result is identical whether it runs alone or in a batch with others."""
+    import lum_gb300
+    mix = worldgen.mixed_worlds(n=6, seed=11, max_dims=(12, 12, 6))
+    rws = _make(mix)
+    solo = _make(mix[2:3])
+    with lum_gb300.RadianceBatch(rws) as b, lum_gb300.RadianceBatch(solo) as s:
+        for i, (w, req, r) in enumerate(mix):
+            b.set_requests(i, req, lum_gb300.pass_params(rays=r, blend=0.1))
+        w, req, r = mix[2]
+        s.set_requests(0, req, lum_gb300.pass_params(rays=r, blend=0.1))
+        b.run(1)
+        s.run(1)
+        b.synchronize()
+        s.synchronize()
+        assert rws[2].get_radiance().tobytes() == solo[0].get_radiance().tobytes()
+    for rw in rws + solo:
+        rw.close()
