@@ -52,8 +52,8 @@ struct WorldPass {
 };
 
 struct LaunchArgs {
-    WorldPass single;            // the world when n_worlds == 1 (passed by value)
-    const WorldPass* worlds;     // device array when n_worlds > 1
+    WorldPass single;            // the one world, passed by value, when `worlds` is null
+    const WorldPass* worlds;     // device table of n_worlds worlds (a batch), or null
     int n_worlds;
     int total_warps;             // warps of the march grid (set by the launcher)
     int chunk_begin, chunk_end;  // tasks of this march/finalize round (set by the launcher)

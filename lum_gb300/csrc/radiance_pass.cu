@@ -125,7 +125,7 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             const int t = next_task();
             if (t < 0) break;
             if (t < w_begin || t >= w_end) {
-                const WorldPass* wq = la.n_worlds == 1 ? &la.single : la.worlds + world_of(la, t);
+                const WorldPass* wq = la.worlds ? la.worlds + world_of(la, t) : &la.single;
                 if (t >= (int)(wq->task_begin + wq->n_tasks)) {   // alignment gap between worlds
                     if (pending == t) pending = -1; else tb++;
                     continue;
@@ -252,7 +252,7 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     __syncthreads();
     const int t0 = la.chunk_begin + (int)blockIdx.x * kWarps;   // worlds start at multiples of 8
     const int t = t0 + w;
-    const WorldPass* wp = la.n_worlds == 1 ? &la.single : la.worlds + world_of(la, t0);
+    const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
     const int t_local = t - (int)wp->task_begin;
     const bool valid = t < la.chunk_end && t_local < wp->n_tasks;
     const int nsub = wp->R >> 5;

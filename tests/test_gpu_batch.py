@@ -13,10 +13,10 @@ from tests.helpers import RTOL, random_prev, rel_err
 pytestmark = pytest.mark.gpu
 
 
-def _make(mix, precision="fp32"):
+def _make(mix, precision="fp32", first=0):
     import lum_gb300
     rws = []
-    for i, (w, req, r) in enumerate(mix):
+    for i, (w, req, r) in enumerate(mix, start=first):
         rw = lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], precision=precision)
         rw.load(w)
         rw.set_radiance(random_prev(w, seed=100 + i))
@@ -74,7 +74,7 @@ def test_batch_in_the_mix_equals_alone():
     import lum_gb300
     mix = worldgen.mixed_worlds(n=6, seed=11, max_dims=(12, 12, 6))
     rws = _make(mix)
-    solo = _make(mix[2:3])
+    solo = _make(mix[2:3], first=2)
     with lum_gb300.RadianceBatch(rws) as b, lum_gb300.RadianceBatch(solo) as s:
         for i, (w, req, r) in enumerate(mix):
             b.set_requests(i, req, lum_gb300.pass_params(rays=r, blend=0.1))
