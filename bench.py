@@ -228,6 +228,89 @@ def batched_leg(local: int, steps: int, warmup: int, flush):
     return out
 
 
+SERVE_WORKLOAD = {
+    "workload": "relight serving: 64 resident terrain worlds, block counts lognormal in 8^3..64x64x32, "
+                "Poisson stream of relight requests, each editing U(1%,5%) of its world's blocks "
+                "(seeded block-type changes) and relighting the probes within 2 blocks of the edits, "
+                "64 rays/probe, max_dist 128, blend 0.1, FP32, HBM budget 120 GB",
+    "worlds": 64, "requests_per_rate": 10000, "radius": 2, "rays_per_probe": 64, "hbm_budget_gb": 120,
+    "seed": SEED,
+}
+
+
+def _serve_trace(srv, reqs, arrivals, params_of):
+    """Submits every request with its arrival time (offset into the future), serves them all and
+    returns (latencies s, rays, span s)."""
+    base = srv.now() + 0.5 + 2e-5 * len(reqs)
+    for k, (w, e) in enumerate(reqs):
+        srv.submit(w, e, params_of(k), base + float(arrivals[k]))
+    late = srv.now() > base
+    srv.run(timeout_s=600)
+    d = srv.poll(len(reqs) + 16)
+    assert len(d) == len(reqs) and (d["status"] == 0).all(), "serving trace failed"
+    lat = d["done_s"] - d["arrival_s"]
+    rays = int((d["probes"].astype(np.int64) * d["rays_per_probe"]).sum())
+    span = float(d["done_s"].max() - d["arrival_s"].min())
+    return lat, rays, span, late
+
+
+def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 10000.0, 20000.0)):
+    """Continuous batching of relight requests over 64 resident worlds, at each arrival rate and
+    saturated (every request due at once); the plain form (one request per launch, one launch
+    at a time) saturated, for comparison."""
+    import lum_gb300
+    worlds = worldgen.serving_worlds(SERVE_WORKLOAD["worlds"], seed=SEED)
+    rws = []
+    for w in worlds:
+        rw = lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], device=local)
+        rw.load(w)
+        rws.append(rw)
+    # requests: uniform world, U(1%,5%) edits
+    u = worldgen.uniform(SEED, 9301, 2 * n_requests).reshape(n_requests, 2)
+    reqs = []
+    for k in range(n_requests):
+        wi = int(u[k, 0] * len(worlds))
+        reqs.append((wi, worldgen.edit_request(worlds[wi].dims, 0.01 + 0.04 * u[k, 1], seed=SEED, stream=k)))
+
+    def params_of(k):
+        return lum_gb300.pass_params(rays=SERVE_WORKLOAD["rays_per_probe"], max_dist=128.0, blend=0.1, time_seed=k)
+
+    def summary(lat, rays, span, late):
+        return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "probe_rays_per_s": rays / span, "requests_per_s": len(lat) / span, "span_s": span,
+                "submitted_late": bool(late)}
+
+    out = {"config": dict(SERVE_WORKLOAD, world_blocks_total=int(sum(w.n_blocks for w in worlds)),
+                          l2="inputs resident; no flush (a serving loop runs warm)")}
+    budget = SERVE_WORKLOAD["hbm_budget_gb"] * 1e9
+    srv = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=3)
+    for rw in rws:
+        srv.add_world(rw)
+    # warm-up: a short saturated trace
+    _serve_trace(srv, reqs[:200], np.zeros(200), params_of)
+    sweep = []
+    for rate in rates:
+        arr = worldgen.poisson_arrivals(n_requests, rate, seed=SEED + int(rate))
+        sweep.append(dict(summary(*_serve_trace(srv, reqs, arr, params_of)), rate_per_s=rate))
+    sat = summary(*_serve_trace(srv, reqs, np.zeros(n_requests), params_of))
+    st = srv.stats()
+    srv.close()
+    plain = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=1,
+                                     max_requests_per_launch=1)
+    for rw in rws:
+        plain.add_world(rw)
+    _serve_trace(plain, reqs[:200], np.zeros(200), params_of)
+    psat = summary(*_serve_trace(plain, reqs, np.zeros(n_requests), params_of))
+    plain.close()
+    for rw in rws:
+        rw.close()
+    out.update({"value": sat["probe_rays_per_s"], "unit": "probe-rays/s", "sweep": sweep, "saturated": sat,
+                "plain_saturated": psat, "speedup_vs_plain": sat["probe_rays_per_s"] / psat["probe_rays_per_s"],
+                "launches": st["launches"], "max_requests_in_launch": st["max_requests_in_launch"],
+                "resident_gb": st["resident_bytes"] / 1e9, "peak_inflight_mb": st["peak_inflight_bytes"] / 1e6})
+    return out
+
+
 def dist_setup(args):
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -286,8 +369,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--legs", default="demo,batched",
-                    help="comma list of legs: demo (the headline line), batched (the mixed-size batch)")
+    ap.add_argument("--legs", default="demo,batched,serving",
+                    help="comma list of legs: demo (the headline line), batched (the mixed-size batch), "
+                         "serving (relight requests)")
     args = ap.parse_args()
     legs = set(args.legs.split(","))
     rank, local, world_size, pg = dist_setup(args)
@@ -390,6 +474,9 @@ def main():
     batched = None
     if "batched" in legs:
         batched = batched_leg(local, max(3, args.steps // 2), args.warmup, flush)
+    serving = None
+    if "serving" in legs:
+        serving = serving_leg(local)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -413,6 +500,7 @@ def main():
             "clocks": clocks.summary(),
             "gpu_launches": 2 * PASSES * args.steps,   # march + finalize per pass
             "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line))
     rw.close()

@@ -216,6 +216,80 @@ int  lumrad_batch_autotune(LumRadBatch batch, int repeats, LumRadTuning* best);
 /* Counters of the last run summed over the worlds. */
 int  lumrad_batch_stats(LumRadBatch batch, LumRadPassStats* out);
 
+/* ---- serving: relight requests over resident worlds ----------------------------------------
+ * The reference relights after edits by re-listing every probe near non-air blocks each frame
+ * (update_radiance, internal_render.cpp:1129-1214, after lum_set_world_block edits the grid).
+ * A server keeps many worlds (contexts on one device, one precision) resident and serves relight
+ * requests: a request edits blocks of one world and then runs one radiance pass over the probes
+ * within Chebyshev distance `radius` (settings) of its edits, in x-fastest scan order, with the
+ * request's own parameters (size 1; time_seed is the request's).  Requests are continuously
+ * batched: each launch takes, in submission order, the oldest due request of every world that
+ * has no request on the GPU, while its device bytes fit the HBM budget, and runs them all as one
+ * multi-world pass; up to `max_inflight` launches run at once on their own streams, so requests
+ * that arrive while others run are admitted as soon as a launch slot and memory are free.
+ * A world's requests run one after another in submission order, so each result is the same
+ * whether the request runs alone or among others.  Nothing runs until lumrad_server_progress
+ * or lumrad_server_run is called.  A context registered with a server belongs to it until the
+ * server is destroyed: read its volume with lumrad_server_get_radiance. */
+typedef void* LumRadServer;
+
+typedef struct {
+    int    device;
+    int    precision;             /* LUMRAD_PRECISION_*; every world must match */
+    double hbm_budget_bytes;      /* device bytes for resident worlds plus launches (0 = no limit) */
+    int    max_inflight;          /* launches on the GPU at once, 1..8 (0 = 2) */
+    int    max_requests_per_launch;   /* 0 = no limit */
+    int    radius;                /* dirty-probe radius around each edit, in blocks (0..15) */
+} LumRadServerSettings;
+
+typedef struct { int16_t x, y, z, block; } LumRadEdit;
+
+typedef struct {
+    long long request;            /* id given by lumrad_server_submit */
+    int    world;
+    int    status;                /* LUMRAD_OK, LUMRAD_ENOMEM (never fits the budget), LUMRAD_EDEVICE */
+    int    probes;                /* probes relit */
+    int    rays_per_probe;
+    double arrival_s;             /* server clock (lumrad_server_now) */
+    double start_s;               /* its launch was enqueued */
+    double done_s;                /* its launch finished on the GPU */
+} LumRadCompletion;
+
+typedef struct {
+    long long launches;
+    long long requests;           /* completed */
+    unsigned long long probes, rays;
+    double resident_bytes;        /* registered worlds */
+    double launch_bytes;          /* fixed per-slot buffers */
+    double peak_inflight_bytes;   /* largest admitted request bytes on the GPU at once */
+    int    max_requests_in_launch;
+} LumRadServerStats;
+
+int  lumrad_server_create(const LumRadServerSettings* settings, LumRadServer* out);
+void lumrad_server_destroy(LumRadServer server);
+/* Registers a loaded context; LUMRAD_ENOMEM if its device bytes do not fit the budget. */
+int  lumrad_server_add_world(LumRadServer server, LumRadContext world, int* id);
+/* Queues a request (edits in order; the last edit of a block wins).  arrival_s: when it becomes
+ * due on the server clock (< 0: now). */
+int  lumrad_server_submit(LumRadServer server, int world, const LumRadEdit* edits, int n_edits,
+                          const LumRadPassParams* params, double arrival_s, long long* request);
+/* Retires finished launches and starts new ones; never waits for the GPU. */
+int  lumrad_server_progress(LumRadServer server);
+/* Calls lumrad_server_progress until every queued request has completed, or timeout_s passes
+ * (LUMRAD_ETIMEOUT). */
+int  lumrad_server_run(LumRadServer server, double timeout_s);
+/* Takes up to cap completions (oldest first). */
+int  lumrad_server_poll(LumRadServer server, LumRadCompletion* out, int cap, int* n);
+double lumrad_server_now(LumRadServer server);
+/* The world's volume after its last completed request (waits for its launch), W*3 floats. */
+int  lumrad_server_get_radiance(LumRadServer server, int world, float* rgb);
+int  lumrad_server_stats(LumRadServer server, LumRadServerStats* out);
+/* Probes within Chebyshev distance radius of the edits of a world of world_size blocks, as
+ * (x, y, z, 0) int16 in x-fastest scan order: the request list a relight request runs.  Host
+ * only; cap 0 returns the count in *n. */
+int  lumrad_dirty_probes(const int* world_size, const LumRadEdit* edits, int n_edits, int radius,
+                         int16_t* out, int cap, int* n);
+
 /* ---- no-allocation pass (no counterpart in the reference) -----------------------------------
  * One pass like lumrad_radiance_pass, for callers that may not allocate device memory while
  * they run: engines that reserve their whole device-memory budget up front and forbid later

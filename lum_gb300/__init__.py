@@ -14,7 +14,8 @@ import numpy as np
 from ._native import (HIT_DTYPE, PRECISION, LumRadError, Material, PassParams, PassStats, Settings,
                       check, load, ptr)
 
-__all__ = ["RadianceWorld", "PassParams", "LumRadError", "HIT_DTYPE", "load", "pass_params"]
+__all__ = ["RadianceWorld", "RadianceBatch", "RadianceServer", "PassParams", "LumRadError", "HIT_DTYPE", "load",
+           "pass_params", "dirty_probes", "direction_table"]
 
 
 def pass_params(rays: int = 64, max_dist: float = 128.0, blend: float = 0.01, time_seed: int = 0,
@@ -227,6 +228,95 @@ class RadianceBatch:
         s = PassStats()
         check(self.lib.lumrad_batch_stats(self.h, C.byref(s)))
         return {"probes": s.probes, "rays": s.rays, "steps": s.steps, "hits": s.hits, "gpu_ms": s.gpu_ms}
+
+
+def _edits(edits) -> np.ndarray:
+    from ._native import EDIT_DTYPE
+    e = np.asarray(edits)
+    if e.dtype != EDIT_DTYPE:
+        e = np.ascontiguousarray(e, dtype=np.int16).reshape(-1, 4)
+        e = e.view(EDIT_DTYPE).reshape(-1)
+    return np.ascontiguousarray(e)
+
+
+class RadianceServer:
+    """Relight requests over resident worlds, continuously batched (lumrad_server_*)."""
+
+    def __init__(self, device: int = 0, precision: str = "fp32", hbm_budget_bytes: float = 0.0,
+                 max_inflight: int = 2, max_requests_per_launch: int = 0, radius: int = 2):
+        from ._native import ServerSettings
+        self.lib = load()
+        s = ServerSettings(int(device), PRECISION[precision], float(hbm_budget_bytes), int(max_inflight),
+                           int(max_requests_per_launch), int(radius))
+        h = C.c_void_p()
+        check(self.lib.lumrad_server_create(C.byref(s), C.byref(h)))
+        self.h = h
+        self.worlds = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lumrad_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_world(self, world: RadianceWorld) -> int:
+        i = C.c_int()
+        check(self.lib.lumrad_server_add_world(self.h, world.h, C.byref(i)))
+        self.worlds.append(world)
+        return int(i.value)
+
+    def submit(self, world: int, edits, params: PassParams, arrival_s: float = -1.0) -> int:
+        e = _edits(edits)
+        rid = C.c_longlong()
+        check(self.lib.lumrad_server_submit(self.h, world, e.ctypes.data if e.size else None, e.size,
+                                            C.byref(params), float(arrival_s), C.byref(rid)))
+        return int(rid.value)
+
+    def progress(self) -> None:
+        check(self.lib.lumrad_server_progress(self.h))
+
+    def run(self, timeout_s: float = 600.0) -> None:
+        check(self.lib.lumrad_server_run(self.h, float(timeout_s)))
+
+    def poll(self, cap: int = 65536) -> np.ndarray:
+        from ._native import COMPLETION_DTYPE
+        out = np.zeros(cap, dtype=COMPLETION_DTYPE)
+        n = C.c_int()
+        check(self.lib.lumrad_server_poll(self.h, out.ctypes.data, cap, C.byref(n)))
+        return out[: n.value]
+
+    def now(self) -> float:
+        return float(self.lib.lumrad_server_now(self.h))
+
+    def get_radiance(self, world: int) -> np.ndarray:
+        X, Y, Z = self.worlds[world].dims
+        out = np.empty((Z, Y, X, 3), dtype=np.float32)
+        check(self.lib.lumrad_server_get_radiance(self.h, world, ptr(out)))
+        return out
+
+    def stats(self) -> dict:
+        from ._native import ServerStats
+        s = ServerStats()
+        check(self.lib.lumrad_server_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+
+def dirty_probes(world_size, edits, radius: int = 2) -> np.ndarray:
+    """Probes within Chebyshev distance `radius` of the edits, (n, 4) int16 in scan order."""
+    e = _edits(edits)
+    ws = (C.c_int * 3)(*[int(v) for v in world_size])
+    n = C.c_int()
+    lib = load()
+    check(lib.lumrad_dirty_probes(ws, e.ctypes.data if e.size else None, e.size, radius, None, 0, C.byref(n)))
+    out = np.zeros((max(n.value, 1), 4), dtype=np.int16)
+    check(lib.lumrad_dirty_probes(ws, e.ctypes.data if e.size else None, e.size, radius, ptr(out), n.value,
+                                  C.byref(n)))
+    return out[: n.value]
 
 
 def direction_table(rays: int) -> np.ndarray:

@@ -47,6 +47,24 @@ class Tuning(C.Structure):
     _fields_ = [("guided_div", C.c_int), ("max_chunk", C.c_int), ("march_ctas", C.c_int), ("pass_ms", C.c_float)]
 
 
+class ServerSettings(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget_bytes", C.c_double),
+                ("max_inflight", C.c_int), ("max_requests_per_launch", C.c_int), ("radius", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("launches", C.c_longlong), ("requests", C.c_longlong), ("probes", C.c_uint64),
+                ("rays", C.c_uint64), ("resident_bytes", C.c_double), ("launch_bytes", C.c_double),
+                ("peak_inflight_bytes", C.c_double), ("max_requests_in_launch", C.c_int)]
+
+
+# LumRadEdit and LumRadCompletion as numpy records (same layout as the C structs)
+EDIT_DTYPE = np.dtype([("x", "<i2"), ("y", "<i2"), ("z", "<i2"), ("block", "<i2")])
+COMPLETION_DTYPE = np.dtype([("request", "<i8"), ("world", "<i4"), ("status", "<i4"), ("probes", "<i4"),
+                             ("rays_per_probe", "<i4"), ("arrival_s", "<f8"), ("start_s", "<f8"),
+                             ("done_s", "<f8")])
+assert EDIT_DTYPE.itemsize == 8 and COMPLETION_DTYPE.itemsize == 48
+
 # LumRadHit as a numpy record (24 bytes, same layout as the C struct)
 HIT_DTYPE = np.dtype([("voxel", "<i4", (3,)), ("block", "<i2"), ("voxel_id", "u1"), ("flags", "u1"),
                       ("coarse_steps", "<u2"), ("refine_steps", "u1"), ("coarse_voxel", "u1"),
@@ -93,6 +111,18 @@ _SIGS = {
     "lumrad_batch_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
     "lumrad_batch_autotune": (C.c_int, [_P, C.c_int, C.POINTER(Tuning)]),
     "lumrad_batch_stats": (C.c_int, [_P, C.POINTER(PassStats)]),
+    "lumrad_server_create": (C.c_int, [C.POINTER(ServerSettings), C.POINTER(_P)]),
+    "lumrad_server_destroy": (None, [_P]),
+    "lumrad_server_add_world": (C.c_int, [_P, _P, C.POINTER(C.c_int)]),
+    "lumrad_server_submit": (C.c_int, [_P, C.c_int, _P, C.c_int, C.POINTER(PassParams), C.c_double,
+                                       C.POINTER(C.c_longlong)]),
+    "lumrad_server_progress": (C.c_int, [_P]),
+    "lumrad_server_run": (C.c_int, [_P, C.c_double]),
+    "lumrad_server_poll": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
+    "lumrad_server_now": (C.c_double, [_P]),
+    "lumrad_server_get_radiance": (C.c_int, [_P, C.c_int, _P]),
+    "lumrad_server_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "lumrad_dirty_probes": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, C.POINTER(C.c_int)]),
 }
 
 _lib = None

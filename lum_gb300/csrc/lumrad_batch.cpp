@@ -196,6 +196,7 @@ int lumrad_batch_create(LumRadContext const* worlds, int n_worlds, LumRadBatch* 
     for (int i = 0; i < n_worlds; i++) {
         Context* c = as_ctx(worlds[i]);
         if (!c) return fail(LUMRAD_EINVAL, "null context");
+        if (int rc = check_unowned(c)) return rc;
         if (c->device != c0->device) return fail(LUMRAD_EINVAL, "the worlds of a batch must share one device");
         if (c->world.precision != c0->world.precision) return fail(LUMRAD_EINVAL, "the worlds of a batch must share one precision");
         for (int j = 0; j < i; j++)

@@ -94,46 +94,62 @@ void DeviceWorld::release() {
 
 // Renumbers the block ids present in the grid into compact ids (0 stays 0; every id whose palette
 // slot is absent shares one all-empty compact id) and builds each compact id's occupancy mask
-// from the palette as uploaded.
+// from the palette as uploaded.  Ids that appear later (edits) get the next free compact id
+// through compact_of.
 void DeviceWorld::build_compact() {
-    std::vector<int32_t> id_to_c(65536, -1);
-    std::vector<int> reps;   // representative block id of each compact id (-100000: empty)
-    auto slot_of = [&](int b) { return b >= 0 ? b : b + 64; };
-    auto has_slot = [&](int b) { return b >= -63 && slot_of(b) < n_slots; };
+    id_to_c.assign(65536, -1);
+    reps.clear();
+    empty_c = -1;
     id_to_c[0] = 0;
     reps.push_back(0);
-    int empty_c = -1;
+    n_compact = 1;
+    h_cbits.assign(128, 0u);
+    for (int k = 0; k < 4096 && n_slots > 0; k++)   // block 0 reads palette slot 0 like any other id
+        if (h_pal_dev[k]) h_cbits[k >> 5] |= 1u << (k & 31);
+    cgrid_wide = false;
+    bool assigned = false;
     for (size_t i = 0; i < W; i++) {
-        const int b = h_grid[i];
-        int32_t& c = id_to_c[(uint16_t)b];
-        if (c >= 0) continue;
-        if (has_slot(b)) {
-            c = (int32_t)reps.size();
-            reps.push_back(b);
-        } else {
-            if (empty_c < 0) {
-                empty_c = (int)reps.size();
-                reps.push_back(-100000);
-            }
-            c = empty_c;
-        }
+        if (id_to_c[(uint16_t)h_grid[i]] >= 0) continue;
+        if (compact_of(h_grid[i], &assigned) < 0) cgrid_wide = true;   // > 256 ids: uint16
     }
-    n_compact = (int)reps.size();
-    cgrid_wide = n_compact > 256;
     h_cgrid.resize(W * (cgrid_wide ? 2 : 1));
     for (size_t i = 0; i < W; i++) {
         const int32_t c = id_to_c[(uint16_t)h_grid[i]];
         if (cgrid_wide) reinterpret_cast<uint16_t*>(h_cgrid.data())[i] = (uint16_t)c;
         else h_cgrid[i] = (uint8_t)c;
     }
-    h_cbits.assign((size_t)n_compact * 128, 0u);
-    for (int c = 0; c < n_compact; c++) {
-        if (reps[c] == -100000 || !has_slot(reps[c])) continue;
-        const uint8_t* v = h_pal_dev.data() + (size_t)slot_of(reps[c]) * 4096;
+}
+
+int DeviceWorld::compact_of(int16_t b, bool* assigned) {
+    *assigned = false;
+    int32_t& c = id_to_c[(uint16_t)b];
+    if (c >= 0) return c;
+    const int slot = b >= 0 ? b : b + 64;
+    const bool has_slot = b >= -63 && slot < n_slots;
+    if (!has_slot && empty_c >= 0) return c = empty_c;
+    // past 256 ids a uint8 compact grid overflows; the id is assigned anyway (a rebuild with a
+    // uint16 grid numbers the ids in the same order)
+    const bool overflow = !cgrid_wide && n_compact >= 256;
+    if (!has_slot) empty_c = n_compact;
+    c = n_compact++;
+    reps.push_back(has_slot ? b : kEmptyRep);
+    h_cbits.resize((size_t)n_compact * 128, 0u);
+    if (has_slot) {
+        const uint8_t* v = h_pal_dev.data() + (size_t)slot * 4096;
         uint32_t* bits = h_cbits.data() + (size_t)c * 128;
         for (int k = 0; k < 4096; k++)
             if (v[k]) bits[k >> 5] |= 1u << (k & 31);
     }
+    *assigned = true;
+    return overflow ? -1 : c;
+}
+
+size_t DeviceWorld::footprint() const {
+    size_t b = W * sizeof(int16_t) + W * sizeof(uint16_t) + cbits_cap * 128 * sizeof(uint32_t) + h_pal.size() +
+               LUMRAD_MATERIALS * sizeof(float4) + 2 * W * rad_stride + scratch_cap * sizeof(float4) +
+               count_cap * sizeof(int) + 2 * sizeof(unsigned long long) + hits_cap * sizeof(LumRadHit);
+    for (auto& kv : d_dirs) b += (size_t)kv.first * sizeof(float4);
+    return b;
 }
 
 int DeviceWorld::sync_inputs(cudaStream_t stream) {
@@ -144,12 +160,15 @@ int DeviceWorld::sync_inputs(cudaStream_t stream) {
     }
     if (compact_dirty) {
         build_compact();
-        if ((size_t)n_compact > cbits_cap) {
+        // room for every id that has a palette slot (-63..-1, 1..n_slots-1), air and the empty id,
+        // so ids that edits bring in later never reallocate
+        const size_t cap = std::max<size_t>((size_t)n_compact, (size_t)n_slots + 64);
+        if (cap > cbits_cap) {
             cudaFree(d_cbits);
             d_cbits = nullptr;
             cbits_cap = 0;
-            LUMRAD_TRY(cudaMalloc(&d_cbits, (size_t)n_compact * 128 * sizeof(uint32_t)));
-            cbits_cap = (size_t)n_compact;
+            LUMRAD_TRY(cudaMalloc(&d_cbits, cap * 128 * sizeof(uint32_t)));
+            cbits_cap = cap;
         }
         LUMRAD_TRY(cudaMemcpyAsync(d_cgrid, h_cgrid.data(), h_cgrid.size(), cudaMemcpyHostToDevice, stream));
         LUMRAD_TRY(cudaMemcpyAsync(d_cbits, h_cbits.data(), h_cbits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
@@ -343,6 +362,7 @@ int Context::check_error() {
 }
 
 int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in) {
+    if (int rc = check_unowned(this)) return rc;
     LumRadPassParams p = *p_in;
     if (p.size == 0) {
         // adaptive slicing of update_radiance (internal_render.cpp:1190-1203)
@@ -404,6 +424,10 @@ void Context::release() {
 }
 
 Context* as_ctx(LumRadContext c) { return reinterpret_cast<Context*>(c); }
+
+int check_unowned(const Context* c) {
+    return c->owner ? fail(LUMRAD_ESTATE, "the context belongs to a server; use the server's calls") : LUMRAD_OK;
+}
 
 int check_params(const LumRadPassParams* p) {
     if (!p) return fail(LUMRAD_EINVAL, "params is null");
@@ -524,6 +548,7 @@ int lumrad_synchronize(LumRadContext ctx) {
 int lumrad_load_world(LumRadContext ctx, const int16_t* blocks) {
     Context* c = as_ctx(ctx);
     if (!c || !blocks) return fail(LUMRAD_EINVAL, "null argument");
+    if (int rc = check_unowned(c)) return rc;
     std::memcpy(c->world.h_grid.data(), blocks, c->world.W * sizeof(int16_t));
     c->world.grid_dirty = true;
     LUMRAD_TRY(cudaSetDevice(c->device));
@@ -533,6 +558,7 @@ int lumrad_load_world(LumRadContext ctx, const int16_t* blocks) {
 int lumrad_set_world_block(LumRadContext ctx, int x, int y, int z, int16_t block) {
     Context* c = as_ctx(ctx);
     if (!c) return fail(LUMRAD_EINVAL, "null context");
+    if (int rc = check_unowned(c)) return rc;
     DeviceWorld& w = c->world;
     if (x < 0 || y < 0 || z < 0 || x >= w.X || y >= w.Y || z >= w.Z)
         return fail(LUMRAD_EINVAL, "block coordinate out of the world");
@@ -567,6 +593,7 @@ int lumrad_load_block(LumRadContext ctx, int16_t block, const uint8_t* voxels) {
 int lumrad_upload_block_palette(LumRadContext ctx) {
     Context* c = as_ctx(ctx);
     if (!c) return fail(LUMRAD_EINVAL, "null context");
+    if (int rc = check_unowned(c)) return rc;
     DeviceWorld& w = c->world;
     LUMRAD_TRY(cudaSetDevice(c->device));
     w.h_pal_dev = w.h_pal;
@@ -586,6 +613,7 @@ int lumrad_load_materials(LumRadContext ctx, const LumRadMaterial* materials) {
 int lumrad_upload_material_palette(LumRadContext ctx) {
     Context* c = as_ctx(ctx);
     if (!c) return fail(LUMRAD_EINVAL, "null context");
+    if (int rc = check_unowned(c)) return rc;
     LUMRAD_TRY(cudaSetDevice(c->device));
     std::vector<float4> m(LUMRAD_MATERIALS);
     const auto& hm = c->world.h_mats;
@@ -632,6 +660,7 @@ int lumrad_get_radiance(LumRadContext ctx, float* rgb) {
 int lumrad_set_radiance(LumRadContext ctx, const float* rgb) {
     Context* c = as_ctx(ctx);
     if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
+    if (int rc = check_unowned(c)) return rc;
     LUMRAD_TRY(cudaSetDevice(c->device));
     DeviceWorld& w = c->world;
     if (w.precision == LUMRAD_PRECISION_FP32) {

@@ -85,4 +85,16 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
 // its counters (descriptors already on the device).
 cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream);
 
+// One block edit of a served world: worlds[world].grid[index] = block and its compact id.
+struct EditRecord {
+    int world;                   // index into the launch's world table
+    int index;                   // x + X*(y + Y*z)
+    int block;                   // new block id (int16 range)
+    int compact;                 // its compact id
+};
+
+// Writes n edits (each block at most once per launch) into the grids and compact grids of the
+// worlds of `d_worlds`.
+cudaError_t launch_apply_edits(const WorldPass* d_worlds, const EditRecord* d_edits, int n, cudaStream_t stream);
+
 }  // namespace lumrad

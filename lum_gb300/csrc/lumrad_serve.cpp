@@ -1,0 +1,632 @@
+// lumrad_serve.cpp — relight server: continuous batching of edit + relight requests over
+// resident worlds.
+//
+// In the reference an edit (lum_set_world_block, crenderer.h) changes the grid, and the next
+// frame's update_radiance (internal_render.cpp:1129-1214) re-lists every probe near non-air
+// blocks, time-sliced over frames.  The server instead relights only the probes near each edit
+// and serves many worlds at once:
+//
+//   host, per launch   take the oldest due request of each idle world (submission order) while
+//                      its device bytes fit the HBM budget; per request, dedupe its edits (last
+//                      edit of a block wins), update the host grid and compact ids, and list the
+//                      probes within `radius` of the edits; pack the world table, the edit
+//                      records and the lists into one pinned buffer
+//   device, per launch one H2D copy -> edit kernel (grid + compact grid) -> prep kernel (next =
+//                      prev) -> rounds of march + finalize over all worlds' tasks; the error word
+//                      is read back and a host callback stamps the completion time
+//
+// Up to max_inflight launches run at once on their own streams.  A world is in at most one
+// launch at a time (it is "busy" until its launch retires), so a world's requests run in order
+// and every result equals the result of the same requests run alone.
+
+#include "lumrad_world.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <vector>
+
+namespace lumrad {
+
+// Probes within Chebyshev distance r of the edits, appended to `out` in x-fastest scan order.
+// One bit per block: each (y, z) row of X blocks is ceil(X/64) words.  The edit bits are dilated
+// along x by word shifts, along y and z by ORs of 2r+1 rows / planes, and the set bits are
+// emitted in scan order.  a and b are scratch (resized here).
+void dirty_probes(int X, int Y, int Z, const LumRadEdit* e, int n, int r, std::vector<uint64_t>& a,
+                  std::vector<uint64_t>& b, std::vector<short4>& out) {
+    const size_t wpr = ((size_t)X + 63) / 64;          // words per row
+    const size_t rows = (size_t)Y * Z;
+    const size_t words = rows * wpr;
+    const size_t plane = (size_t)Y * wpr;
+    a.assign(words, 0);
+    b.assign(words, 0);
+    for (int k = 0; k < n; k++) {
+        const size_t row = (size_t)e[k].y + (size_t)Y * e[k].z;
+        a[row * wpr + (size_t)e[k].x / 64] |= 1ull << (e[k].x % 64);
+    }
+    const uint64_t last = (X % 64) ? (1ull << (X % 64)) - 1 : ~0ull;   // valid bits of a row's last word
+    // x: b = a | a shifted by 1..r either way, within each row
+    for (size_t row = 0; row < rows; row++) {
+        const uint64_t* in = a.data() + row * wpr;
+        uint64_t* o = b.data() + row * wpr;
+        for (size_t w = 0; w < wpr; w++) {
+            uint64_t v = in[w];
+            for (int s = 1; s <= r; s++) {
+                v |= in[w] << s | in[w] >> s;
+                if (w > 0) v |= in[w - 1] >> (64 - s);
+                if (w + 1 < wpr) v |= in[w + 1] << (64 - s);
+            }
+            o[w] = v;
+        }
+        o[wpr - 1] &= last;
+    }
+    // y: a = OR of b rows [y-r, y+r] within each plane
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++) {
+            uint64_t* o = a.data() + (size_t)z * plane + (size_t)y * wpr;
+            for (size_t w = 0; w < wpr; w++) o[w] = 0;
+            for (int yy = std::max(y - r, 0); yy <= std::min(y + r, Y - 1); yy++) {
+                const uint64_t* in = b.data() + (size_t)z * plane + (size_t)yy * wpr;
+                for (size_t w = 0; w < wpr; w++) o[w] |= in[w];
+            }
+        }
+    // z: b = OR of a planes [z-r, z+r]
+    for (int z = 0; z < Z; z++) {
+        uint64_t* o = b.data() + (size_t)z * plane;
+        for (size_t w = 0; w < plane; w++) o[w] = 0;
+        for (int zz = std::max(z - r, 0); zz <= std::min(z + r, Z - 1); zz++) {
+            const uint64_t* in = a.data() + (size_t)zz * plane;
+            for (size_t w = 0; w < plane; w++) o[w] |= in[w];
+        }
+    }
+    size_t count = 0;
+    for (size_t w = 0; w < words; w++) count += (size_t)__builtin_popcountll(b[w]);
+    const size_t base = out.size();
+    out.resize(base + count);
+    short4* p = out.data() + base;
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++) {
+            const uint64_t* row = b.data() + (size_t)z * plane + (size_t)y * wpr;
+            for (size_t w = 0; w < wpr; w++)
+                for (uint64_t bits = row[w]; bits; bits &= bits - 1) {
+                    p->x = (short)((int)(w * 64) + __builtin_ctzll(bits));
+                    p->y = (short)y;
+                    p->z = (short)z;
+                    p->w = 0;
+                    p++;
+                }
+        }
+}
+
+namespace {
+
+double clock_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct SRequest {
+    long long id = 0;
+    int world = 0;
+    double arrival = 0.0;
+    LumRadPassParams p{};
+    std::vector<LumRadEdit> edits;
+};
+
+struct SWorld {
+    Context* ctx = nullptr;
+    size_t bytes = 0;
+    bool busy = false;
+    int last_slot = -1;
+    std::deque<SRequest> fifo;
+    std::vector<int32_t> stamp;   // dedupe of a request's edits
+    int32_t gen = 0;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_done = nullptr;
+    uint8_t* h_pack = nullptr;
+    size_t h_cap = 0;
+    uint8_t* d_pack = nullptr;
+    size_t d_cap = 0;
+    unsigned long long* d_queue = nullptr;
+    int* d_error = nullptr;
+    int* h_error = nullptr;       // pinned
+    float4* d_ray_od = nullptr;
+    uint2* d_ray_res = nullptr;
+    bool busy = false;
+    std::vector<SRequest> reqs;
+    std::vector<int> probes;
+    double start = 0.0;
+    std::atomic<double> done{0.0};
+    size_t reserved = 0;
+};
+
+void CUDART_CB slot_done(void* p) { static_cast<Slot*>(p)->done.store(clock_s(), std::memory_order_release); }
+
+struct Server {
+    LumRadServerSettings s{};
+    int num_sms = 0;
+    double t0 = 0.0;
+    std::vector<SWorld> worlds;
+    std::vector<std::unique_ptr<Slot>> slots;
+    std::deque<LumRadCompletion> done;
+    long long next_id = 0;
+    long long pending = 0;
+    size_t resident = 0, fixed = 0, inflight = 0;
+    LumRadServerStats st{};
+    Tuning tuning;
+    // per-launch host scratch
+    std::vector<EditRecord> erec;
+    std::vector<short4> lists;
+    std::vector<uint64_t> bits_a, bits_b;
+    std::vector<int> kept;
+
+    double now() const { return clock_s() - t0; }
+    size_t budget() const { return s.hbm_budget_bytes > 0 ? (size_t)s.hbm_budget_bytes : (size_t)-1; }
+
+    // device bytes a request needs while its launch runs (upper bound, before its list is built)
+    size_t request_bytes(const SRequest& r) const {
+        const DeviceWorld& dw = worlds[r.world].ctx->world;
+        const size_t side = 2 * (size_t)s.radius + 1;
+        const size_t probes = std::min(dw.W, r.edits.size() * side * side * side);
+        return sizeof(WorldPass) + r.edits.size() * sizeof(EditRecord) + probes * sizeof(short4) + 512;
+    }
+};
+
+Server* as_server(LumRadServer h) { return reinterpret_cast<Server*>(h); }
+
+int grow_pinned(uint8_t** p, size_t* cap, size_t need) {
+    if (need <= *cap) return LUMRAD_OK;
+    const size_t c = std::max(need, *cap * 2);
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *cap = 0;
+    LUMRAD_TRY(cudaMallocHost(p, c));
+    *cap = c;
+    return LUMRAD_OK;
+}
+
+int retire(Server* sv) {
+    for (size_t k = 0; k < sv->slots.size(); k++) {
+        Slot& sl = *sv->slots[k];
+        if (!sl.busy) continue;
+        const cudaError_t q = cudaEventQuery(sl.ev_done);
+        if (q == cudaErrorNotReady) continue;
+        LUMRAD_TRY(q);
+        const int err = *sl.h_error;
+        if (err) {   // a warp's scheduler gave up: reset the slot's counters
+            LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, 2 * sizeof(unsigned long long), sl.stream));
+            LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
+            for (auto& r : sl.reqs) {
+                DeviceWorld& dw = sv->worlds[r.world].ctx->world;
+                LUMRAD_TRY(cudaMemsetAsync(dw.d_probe_count, 0, dw.count_cap * sizeof(int), sl.stream));
+            }
+            LUMRAD_TRY(cudaStreamSynchronize(sl.stream));
+        }
+        const double t_done = sl.done.load(std::memory_order_acquire) - sv->t0;
+        for (size_t j = 0; j < sl.reqs.size(); j++) {
+            const SRequest& r = sl.reqs[j];
+            LumRadCompletion c{};
+            c.request = r.id;
+            c.world = r.world;
+            c.status = err ? LUMRAD_EDEVICE : LUMRAD_OK;
+            c.probes = sl.probes[j];
+            c.rays_per_probe = r.p.rays_per_probe;
+            c.arrival_s = r.arrival;
+            c.start_s = sl.start;
+            c.done_s = t_done;
+            sv->done.push_back(c);
+            sv->worlds[r.world].busy = false;
+            sv->st.requests++;
+            sv->st.probes += (unsigned long long)sl.probes[j];
+            sv->st.rays += (unsigned long long)sl.probes[j] * (unsigned long long)r.p.rays_per_probe;
+        }
+        sv->pending -= (long long)sl.reqs.size();
+        sv->inflight -= sl.reserved;
+        sl.reserved = 0;
+        sl.reqs.clear();
+        sl.busy = false;
+    }
+    return LUMRAD_OK;
+}
+
+void complete_now(Server* sv, const SRequest& r, int status) {
+    LumRadCompletion c{};
+    c.request = r.id;
+    c.world = r.world;
+    c.status = status;
+    c.rays_per_probe = r.p.rays_per_probe;
+    c.arrival_s = r.arrival;
+    c.start_s = c.done_s = sv->now();
+    sv->done.push_back(c);
+    sv->pending--;
+}
+
+// Forms and enqueues one launch on slot `k`; *started = false if no request was due and fit.
+int launch(Server* sv, int k, bool* started) {
+    *started = false;
+    Slot& sl = *sv->slots[k];
+    const double now = sv->now();
+    const size_t budget = sv->budget();
+    // candidates: the front request of each idle world, oldest submission first
+    std::vector<int> cand;
+    for (size_t w = 0; w < sv->worlds.size(); w++) {
+        SWorld& sw = sv->worlds[w];
+        if (!sw.busy && !sw.fifo.empty() && sw.fifo.front().arrival <= now) cand.push_back((int)w);
+    }
+    if (cand.empty()) return LUMRAD_OK;
+    std::sort(cand.begin(), cand.end(),
+              [&](int a, int b) { return sv->worlds[a].fifo.front().id < sv->worlds[b].fifo.front().id; });
+    sl.reqs.clear();
+    size_t bytes = 0;
+    for (int w : cand) {
+        SWorld& sw = sv->worlds[w];
+        const size_t need = sv->request_bytes(sw.fifo.front());
+        if (budget != (size_t)-1 && sv->resident + sv->fixed + need > budget) {   // can never fit
+            complete_now(sv, sw.fifo.front(), LUMRAD_ENOMEM);
+            sw.fifo.pop_front();
+            continue;
+        }
+        if (budget != (size_t)-1 && sv->resident + sv->fixed + sv->inflight + bytes + need > budget) continue;
+        bytes += need;
+        sl.reqs.push_back(std::move(sw.fifo.front()));
+        sw.fifo.pop_front();
+        if (sv->s.max_requests_per_launch > 0 && (int)sl.reqs.size() >= sv->s.max_requests_per_launch) break;
+    }
+    const int nl = (int)sl.reqs.size();
+    if (nl == 0) return LUMRAD_OK;
+
+    // host side of each request: edits, then its dirty-probe list
+    sv->erec.clear();
+    sv->lists.clear();
+    std::vector<size_t> list_off(nl);
+    sl.probes.assign(nl, 0);
+    int rc;
+    for (int j = 0; j < nl; j++) {
+        SRequest& r = sl.reqs[j];
+        SWorld& sw = sv->worlds[r.world];
+        DeviceWorld& dw = sw.ctx->world;
+        if (++sw.gen == 0x7fffffff) {
+            std::fill(sw.stamp.begin(), sw.stamp.end(), 0);
+            sw.gen = 1;
+        }
+        sv->kept.clear();
+        for (int e = (int)r.edits.size() - 1; e >= 0; e--) {   // the last edit of a block wins
+            const LumRadEdit& ed = r.edits[e];
+            const size_t idx = (size_t)ed.x + (size_t)dw.X * ((size_t)ed.y + (size_t)dw.Y * ed.z);
+            if (sw.stamp[idx] == sw.gen) continue;
+            sw.stamp[idx] = sw.gen;
+            sv->kept.push_back(e);
+        }
+        const size_t e0 = sv->erec.size();
+        bool rebuild = false;
+        for (int e : sv->kept) {
+            const LumRadEdit& ed = r.edits[e];
+            const size_t idx = (size_t)ed.x + (size_t)dw.X * ((size_t)ed.y + (size_t)dw.Y * ed.z);
+            dw.h_grid[idx] = ed.block;
+            bool assigned = false;
+            const int c = dw.compact_of(ed.block, &assigned);
+            if (c < 0) {
+                rebuild = true;
+                continue;
+            }
+            if (assigned)   // a block id new to this world: upload its occupancy mask
+                LUMRAD_TRY(cudaMemcpyAsync(dw.d_cbits + (size_t)c * 128, dw.h_cbits.data() + (size_t)c * 128,
+                                           128 * sizeof(uint32_t), cudaMemcpyHostToDevice, sl.stream));
+            sv->erec.push_back(EditRecord{j, (int)idx, (int)ed.block, c});
+        }
+        if (rebuild) {   // more than 256 distinct ids: rebuild with a uint16 compact grid
+            sv->erec.resize(e0);
+            dw.grid_dirty = true;
+            if ((rc = dw.sync_inputs(sw.ctx->stream))) return rc;
+        }
+        list_off[j] = sv->lists.size();
+        dirty_probes(dw.X, dw.Y, dw.Z, r.edits.data(), (int)r.edits.size(), sv->s.radius, sv->bits_a, sv->bits_b,
+                     sv->lists);
+        sl.probes[j] = (int)(sv->lists.size() - list_off[j]);
+    }
+
+    // one pinned pack: world table | edit records | lists
+    const size_t off_e = align_up((size_t)nl * sizeof(WorldPass), 256);
+    const size_t off_l = align_up(off_e + sv->erec.size() * sizeof(EditRecord), 256);
+    const size_t total = off_l + sv->lists.size() * sizeof(short4);
+    if ((rc = grow_pinned(&sl.h_pack, &sl.h_cap, total))) return rc;
+    if (total > sl.d_cap) {
+        const size_t c = std::max(total, sl.d_cap * 2);
+        if (sl.d_pack) LUMRAD_TRY(cudaFreeAsync(sl.d_pack, sl.stream));
+        sl.d_pack = nullptr;
+        sl.d_cap = 0;
+        LUMRAD_TRY(cudaMallocAsync(reinterpret_cast<void**>(&sl.d_pack), c, sl.stream));
+        sl.d_cap = c;
+    }
+    WorldPass* table = reinterpret_cast<WorldPass*>(sl.h_pack);
+    const WorldPass* d_table = reinterpret_cast<const WorldPass*>(sl.d_pack);
+    const short4* d_lists = reinterpret_cast<const short4*>(sl.d_pack + off_l);
+    long long begin = 0;
+    for (int j = 0; j < nl; j++) {
+        SRequest& r = sl.reqs[j];
+        DeviceWorld& dw = sv->worlds[r.world].ctx->world;
+        LumRadPassParams p = r.p;
+        p.size = 1;
+        p.shift = 0;
+        p.record_hits = 0;
+        WorldPass w;
+        if ((rc = dw.fill_pass(d_lists + list_off[j], sl.probes[j], p, sl.stream, &w))) return rc;
+        w.task_begin = begin;
+        begin += (w.n_tasks + kWarps - 1) / kWarps * kWarps;
+        table[j] = w;
+    }
+    if (!sv->erec.empty()) std::memcpy(sl.h_pack + off_e, sv->erec.data(), sv->erec.size() * sizeof(EditRecord));
+    if (!sv->lists.empty()) std::memcpy(sl.h_pack + off_l, sv->lists.data(), sv->lists.size() * sizeof(short4));
+
+    LUMRAD_TRY(cudaMemcpyAsync(sl.d_pack, sl.h_pack, total, cudaMemcpyHostToDevice, sl.stream));
+    LUMRAD_TRY(launch_apply_edits(d_table, reinterpret_cast<const EditRecord*>(sl.d_pack + off_e),
+                                  (int)sv->erec.size(), sl.stream));
+    LUMRAD_TRY(launch_prep(d_table, nl, sv->s.precision, sl.stream));
+    LaunchArgs la;
+    std::memset(&la, 0, sizeof la);
+    la.worlds = d_table;
+    la.n_worlds = nl;
+    la.n_tasks = begin;
+    la.queue = sl.d_queue;
+    la.error = sl.d_error;
+    la.ray_od = sl.d_ray_od;
+    la.ray_res = sl.d_ray_res;
+    la.guided_div = sv->tuning.guided_div;
+    la.max_chunk = sv->tuning.max_chunk;
+    la.march_ctas = sv->tuning.march_ctas;
+    LUMRAD_TRY(launch_radiance(la, sv->s.precision, false, sv->num_sms, sl.stream));
+    LUMRAD_TRY(cudaMemcpyAsync(sl.h_error, sl.d_error, sizeof(int), cudaMemcpyDeviceToHost, sl.stream));
+    LUMRAD_TRY(cudaLaunchHostFunc(sl.stream, slot_done, &sl));
+    LUMRAD_TRY(cudaEventRecord(sl.ev_done, sl.stream));
+
+    for (int j = 0; j < nl; j++) {
+        SWorld& sw = sv->worlds[sl.reqs[j].world];
+        sw.busy = true;
+        sw.last_slot = k;
+        sw.ctx->world.cur = 1 - sw.ctx->world.cur;
+        sw.ctx->have_pass = true;
+    }
+    sl.busy = true;
+    sl.start = now;
+    sl.reserved = bytes;
+    sv->inflight += bytes;
+    sv->st.launches++;
+    sv->st.max_requests_in_launch = std::max(sv->st.max_requests_in_launch, nl);
+    sv->st.peak_inflight_bytes = std::max(sv->st.peak_inflight_bytes, (double)sv->inflight);
+    *started = true;
+    return LUMRAD_OK;
+}
+
+int progress(Server* sv) {
+    int rc = retire(sv);
+    if (rc) return rc;
+    for (size_t k = 0; k < sv->slots.size(); k++) {
+        if (sv->slots[k]->busy) continue;
+        bool started = false;
+        if ((rc = launch(sv, (int)k, &started))) return rc;
+        if (!started) break;
+    }
+    return LUMRAD_OK;
+}
+
+void destroy_server(Server* sv) {
+    cudaSetDevice(sv->s.device);
+    for (auto& slp : sv->slots) {
+        Slot& sl = *slp;
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.d_pack) cudaFreeAsync(sl.d_pack, sl.stream);
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.h_pack) cudaFreeHost(sl.h_pack);
+        if (sl.h_error) cudaFreeHost(sl.h_error);
+        cudaFree(sl.d_queue);
+        cudaFree(sl.d_error);
+        cudaFree(sl.d_ray_od);
+        cudaFree(sl.d_ray_res);
+        if (sl.ev_done) cudaEventDestroy(sl.ev_done);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    for (auto& w : sv->worlds) w.ctx->owner = nullptr;
+    delete sv;
+}
+
+}  // namespace
+}  // namespace lumrad
+
+using namespace lumrad;
+
+extern "C" {
+
+int lumrad_dirty_probes(const int* world_size, const LumRadEdit* edits, int n_edits, int radius, int16_t* out,
+                        int cap, int* n) {
+    if (!world_size || !n || (n_edits > 0 && !edits) || (cap > 0 && !out) || n_edits < 0)
+        return fail(LUMRAD_EINVAL, "bad argument");
+    const int X = world_size[0], Y = world_size[1], Z = world_size[2];
+    if (X < 1 || Y < 1 || Z < 1 || X > 2047 || Y > 2047 || Z > 2047) return fail(LUMRAD_EINVAL, "bad world size");
+    if (radius < 0 || radius > 15) return fail(LUMRAD_EINVAL, "radius must be in [0, 15]");
+    for (int k = 0; k < n_edits; k++)
+        if (edits[k].x < 0 || edits[k].y < 0 || edits[k].z < 0 || edits[k].x >= X || edits[k].y >= Y || edits[k].z >= Z)
+            return fail(LUMRAD_EINVAL, "edit outside the world");
+    std::vector<uint64_t> a, b;
+    std::vector<short4> list;
+    dirty_probes(X, Y, Z, edits, n_edits, radius, a, b, list);
+    const int total = (int)list.size();
+    if (cap > 0) std::memcpy(out, list.data(), (size_t)std::min(total, cap) * sizeof(short4));
+    *n = total;
+    return LUMRAD_OK;
+}
+
+int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
+    if (!s || !out) return fail(LUMRAD_EINVAL, "null argument");
+    *out = nullptr;
+    if (s->precision < 0 || s->precision > 2) return fail(LUMRAD_EINVAL, "unknown precision");
+    if (s->max_inflight < 0 || s->max_inflight > 8) return fail(LUMRAD_EINVAL, "max_inflight must be in [0, 8]");
+    if (s->radius < 0 || s->radius > 15) return fail(LUMRAD_EINVAL, "radius must be in [0, 15]");
+    if (s->hbm_budget_bytes < 0 || s->max_requests_per_launch < 0) return fail(LUMRAD_EINVAL, "negative limit");
+    Server* sv = new Server();
+    sv->s = *s;
+    if (sv->s.max_inflight == 0) sv->s.max_inflight = 2;
+    sv->t0 = clock_s();
+    auto attempt = [&]() -> int {
+        LUMRAD_TRY(cudaSetDevice(s->device));
+        LUMRAD_TRY(cudaDeviceGetAttribute(&sv->num_sms, cudaDevAttrMultiProcessorCount, s->device));
+        const size_t rays = (size_t)kChunkTasks * kTaskRays;
+        for (int k = 0; k < sv->s.max_inflight; k++) {
+            sv->slots.emplace_back(new Slot());
+            Slot& sl = *sv->slots.back();
+            LUMRAD_TRY(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+            LUMRAD_TRY(cudaEventCreateWithFlags(&sl.ev_done, cudaEventDisableTiming));
+            LUMRAD_TRY(cudaMalloc(&sl.d_queue, 2 * sizeof(unsigned long long)));
+            LUMRAD_TRY(cudaMalloc(&sl.d_error, sizeof(int)));
+            LUMRAD_TRY(cudaMallocHost(&sl.h_error, sizeof(int)));
+            *sl.h_error = 0;
+            LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, 2 * sizeof(unsigned long long), sl.stream));
+            LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
+            LUMRAD_TRY(cudaMalloc(&sl.d_ray_od, rays * 2 * sizeof(float4)));
+            LUMRAD_TRY(cudaMalloc(&sl.d_ray_res, rays * sizeof(uint2)));
+            LUMRAD_TRY(cudaStreamSynchronize(sl.stream));
+            sv->fixed += rays * (2 * sizeof(float4) + sizeof(uint2)) + 2 * sizeof(unsigned long long) + sizeof(int);
+        }
+        if (sv->fixed > sv->budget()) return fail(LUMRAD_ENOMEM, "the launch buffers alone exceed the HBM budget");
+        return LUMRAD_OK;
+    };
+    const int rc = attempt();
+    if (rc) {
+        const std::string msg = g_error;
+        destroy_server(sv);
+        return fail(rc, msg);
+    }
+    sv->st.launch_bytes = (double)sv->fixed;
+    *out = sv;
+    return LUMRAD_OK;
+}
+
+void lumrad_server_destroy(LumRadServer server) {
+    Server* sv = as_server(server);
+    if (sv) destroy_server(sv);
+}
+
+int lumrad_server_add_world(LumRadServer server, LumRadContext world, int* id) {
+    Server* sv = as_server(server);
+    Context* c = as_ctx(world);
+    if (!sv || !c || !id) return fail(LUMRAD_EINVAL, "null argument");
+    if (c->device != sv->s.device) return fail(LUMRAD_EINVAL, "the world is on another device");
+    if (c->world.precision != sv->s.precision) return fail(LUMRAD_EINVAL, "the world has another precision");
+    if (c->owner) return fail(LUMRAD_ESTATE, "the world already belongs to a server");
+    LUMRAD_TRY(cudaSetDevice(sv->s.device));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    DeviceWorld& dw = c->world;
+    int rc = dw.sync_inputs(c->stream);
+    if (rc) return rc;
+    // per-pass buffers at their size for 256 rays, so the serving loop never reallocates them
+    if ((rc = dw.ensure_scratch(dw.W, 256))) return rc;
+    for (int R : {32, 64, 128, 256}) {
+        const float4* d = nullptr;
+        if ((rc = dw.ensure_dirs(R, c->stream, &d))) return rc;
+    }
+    const size_t bytes = dw.footprint();
+    if (sv->resident + sv->fixed + bytes > sv->budget())
+        return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget");
+    SWorld w;
+    w.ctx = c;
+    w.bytes = bytes;
+    w.stamp.assign(dw.W, 0);
+    sv->worlds.push_back(std::move(w));
+    sv->resident += bytes;
+    sv->st.resident_bytes = (double)sv->resident;
+    c->owner = sv;
+    *id = (int)sv->worlds.size() - 1;
+    return LUMRAD_OK;
+}
+
+int lumrad_server_submit(LumRadServer server, int world, const LumRadEdit* edits, int n_edits,
+                         const LumRadPassParams* params, double arrival_s, long long* request) {
+    Server* sv = as_server(server);
+    if (!sv || !request || (n_edits > 0 && !edits) || n_edits < 0) return fail(LUMRAD_EINVAL, "bad argument");
+    if (world < 0 || world >= (int)sv->worlds.size()) return fail(LUMRAD_EINVAL, "unknown world");
+    int rc = check_params(params);
+    if (rc) return rc;
+    const DeviceWorld& dw = sv->worlds[world].ctx->world;
+    for (int k = 0; k < n_edits; k++)
+        if (edits[k].x < 0 || edits[k].y < 0 || edits[k].z < 0 || edits[k].x >= dw.X || edits[k].y >= dw.Y ||
+            edits[k].z >= dw.Z)
+            return fail(LUMRAD_EINVAL, "edit outside the world");
+    SRequest r;
+    r.id = sv->next_id++;
+    r.world = world;
+    r.arrival = arrival_s < 0.0 ? sv->now() : arrival_s;
+    r.p = *params;
+    r.edits.assign(edits, edits + n_edits);
+    sv->worlds[world].fifo.push_back(std::move(r));
+    sv->pending++;
+    *request = sv->next_id - 1;
+    return LUMRAD_OK;
+}
+
+int lumrad_server_progress(LumRadServer server) {
+    Server* sv = as_server(server);
+    if (!sv) return fail(LUMRAD_EINVAL, "null server");
+    LUMRAD_TRY(cudaSetDevice(sv->s.device));
+    return progress(sv);
+}
+
+int lumrad_server_run(LumRadServer server, double timeout_s) {
+    Server* sv = as_server(server);
+    if (!sv) return fail(LUMRAD_EINVAL, "null server");
+    LUMRAD_TRY(cudaSetDevice(sv->s.device));
+    const double deadline = clock_s() + timeout_s;
+    while (sv->pending > 0) {
+        int rc = progress(sv);
+        if (rc) return rc;
+        if (clock_s() > deadline) return fail(LUMRAD_ETIMEOUT, "requests still pending at the timeout");
+        std::this_thread::yield();
+    }
+    return LUMRAD_OK;
+}
+
+int lumrad_server_poll(LumRadServer server, LumRadCompletion* out, int cap, int* n) {
+    Server* sv = as_server(server);
+    if (!sv || !n || (cap > 0 && !out)) return fail(LUMRAD_EINVAL, "bad argument");
+    int k = 0;
+    while (k < cap && !sv->done.empty()) {
+        out[k++] = sv->done.front();
+        sv->done.pop_front();
+    }
+    *n = k;
+    return LUMRAD_OK;
+}
+
+double lumrad_server_now(LumRadServer server) {
+    Server* sv = as_server(server);
+    return sv ? sv->now() : 0.0;
+}
+
+int lumrad_server_get_radiance(LumRadServer server, int world, float* rgb) {
+    Server* sv = as_server(server);
+    if (!sv || !rgb) return fail(LUMRAD_EINVAL, "null argument");
+    if (world < 0 || world >= (int)sv->worlds.size()) return fail(LUMRAD_EINVAL, "unknown world");
+    LUMRAD_TRY(cudaSetDevice(sv->s.device));
+    SWorld& w = sv->worlds[world];
+    if (w.busy) {
+        LUMRAD_TRY(cudaEventSynchronize(sv->slots[w.last_slot]->ev_done));
+        int rc = retire(sv);
+        if (rc) return rc;
+    }
+    return lumrad_get_radiance(w.ctx, rgb);
+}
+
+int lumrad_server_stats(LumRadServer server, LumRadServerStats* out) {
+    Server* sv = as_server(server);
+    if (!sv || !out) return fail(LUMRAD_EINVAL, "null argument");
+    *out = sv->st;
+    return LUMRAD_OK;
+}
+
+}  // extern "C"

@@ -45,6 +45,10 @@ struct DeviceWorld {
     bool compact_dirty = true;
     int n_compact = 0;
     bool cgrid_wide = false;
+    std::vector<int32_t> id_to_c;         // block id (as uint16) -> compact id, -1 if not assigned
+    std::vector<int> reps;                // block id of each compact id (kEmptyRep: no voxels)
+    int empty_c = -1;                     // the shared compact id of ids without a palette slot
+    static constexpr int kEmptyRep = -100000;
 
     int16_t* d_grid = nullptr;
     void* d_cgrid = nullptr;
@@ -67,6 +71,11 @@ struct DeviceWorld {
     int init(int X, int Y, int Z, int slots, int precision, cudaStream_t stream);
     void release();
     void build_compact();
+    // Compact id of block id b, assigning the next free one (and its occupancy mask in h_cbits)
+    // if b has none yet; -1 if that needs a wider compact grid (a full rebuild).
+    int compact_of(int16_t b, bool* assigned);
+    // Device bytes this world holds.
+    size_t footprint() const;
     int sync_inputs(cudaStream_t stream);
     int ensure_dirs(int R, cudaStream_t stream, const float4** out);
     int ensure_scratch(size_t groups, int R);
@@ -81,6 +90,7 @@ struct Context {
     DeviceWorld world;
     int device = 0;
     int num_sms = 0;
+    void* owner = nullptr;                // the server this context is registered with, if any
     std::vector<int16_t> specials;        // queued (x,y,z,w)
     short4* d_req = nullptr;
     size_t req_cap = 0;
@@ -118,6 +128,8 @@ struct Context {
 };
 
 Context* as_ctx(LumRadContext c);
+// LUMRAD_ESTATE if a server owns the context (its grid and passes are the server's).
+int check_unowned(const Context* c);
 int check_params(const LumRadPassParams* p);
 void build_list(Context* c, std::vector<int16_t>& out);
 

@@ -376,6 +376,26 @@ cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, 
     return cudaGetLastError();
 }
 
+namespace {
+
+__global__ void apply_edits_kernel(const WorldPass* __restrict__ worlds, const EditRecord* __restrict__ edits, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const EditRecord e = edits[i];
+    const WorldPass& w = worlds[e.world];
+    const_cast<int16_t*>(w.grid)[e.index] = (int16_t)e.block;
+    if (w.cgrid_wide) static_cast<uint16_t*>(const_cast<void*>(w.cgrid))[e.index] = (uint16_t)e.compact;
+    else static_cast<uint8_t*>(const_cast<void*>(w.cgrid))[e.index] = (uint8_t)e.compact;
+}
+
+}  // namespace
+
+cudaError_t launch_apply_edits(const WorldPass* d_worlds, const EditRecord* d_edits, int n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    apply_edits_kernel<<<(n + 255) / 256, 256, 0, stream>>>(d_worlds, d_edits, n);
+    return cudaGetLastError();
+}
+
 }  // namespace lumrad
 
 // ================================================================ no-allocation entry point

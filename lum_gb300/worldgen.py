@@ -188,6 +188,71 @@ def mixed_worlds(n: int = 256, seed: int = 1234, max_dims=(32, 32, 16), min_dims
     return out
 
 
+_S_EDIT = 11
+
+
+def edit_request(dims, fraction: float, seed: int, stream: int, n_types: int = 32) -> np.ndarray:
+    """A relight request's edits: round(fraction * blocks) (at least 1) seeded block-type changes
+    at uniform positions (repeats allowed; the last edit of a block wins), new ids uniform in
+    0..n_types (0 digs the block out).  (n, 4) int16 rows (x, y, z, block)."""
+    X, Y, Z = dims
+    n = max(1, int(round(fraction * X * Y * Z)))
+    u = uniform(seed, _S_EDIT * 1000003 + stream, 4 * n).reshape(n, 4)
+    out = np.empty((n, 4), dtype=np.int16)
+    out[:, 0] = np.floor(u[:, 0] * X)
+    out[:, 1] = np.floor(u[:, 1] * Y)
+    out[:, 2] = np.floor(u[:, 2] * Z)
+    out[:, 3] = np.floor(u[:, 3] * (n_types + 1))
+    return out
+
+
+def apply_edits(grid: np.ndarray, edits: np.ndarray) -> np.ndarray:
+    """The grid (Z, Y, X) after the edits, applied in order."""
+    g = grid.copy()
+    for x, y, z, b in edits:
+        g[z, y, x] = b
+    return g
+
+
+def dirty_probes(dims, edits: np.ndarray, radius: int = 2) -> np.ndarray:
+    """Probes within Chebyshev distance `radius` of any edit, (n, 4) int16 (x, y, z, 0) in
+    x-fastest scan order."""
+    X, Y, Z = dims
+    mask = np.zeros((Z, Y, X), dtype=bool)
+    for x, y, z, _ in edits:
+        mask[max(z - radius, 0):z + radius + 1, max(y - radius, 0):y + radius + 1, max(x - radius, 0):x + radius + 1] = True
+    zz, yy, xx = np.nonzero(mask)
+    out = np.zeros((zz.size, 4), dtype=np.int16)
+    out[:, 0], out[:, 1], out[:, 2] = xx, yy, zz
+    return out
+
+
+def serving_worlds(n: int = 64, seed: int = 1234, lo: int = 8 ** 3, hi: int = 64 * 64 * 32):
+    """The serving workload's worlds: block counts lognormal (median sqrt(lo*hi), 2 sigma = half
+    the log range) clipped to [lo, hi]; dims X = Y = round(cbrt(2n)) in [8, 64], Z = n/(X*Y) in
+    [8, 32].  Returns [World]."""
+    u = uniform(seed, 9101, 2 * n).reshape(n, 2)
+    # Box-Muller normal from two uniforms
+    g = np.sqrt(-2.0 * np.log(np.maximum(u[:, 0], 1e-300))) * np.cos(2.0 * np.pi * u[:, 1])
+    mu = 0.5 * (np.log(lo) + np.log(hi))
+    sigma = 0.25 * (np.log(hi) - np.log(lo))
+    blocks = np.clip(np.exp(mu + sigma * g), lo, hi)
+    out = []
+    for i, b in enumerate(blocks):
+        xy = int(np.clip(round((2.0 * b) ** (1.0 / 3.0)), 8, 64))
+        z = int(np.clip(round(b / (xy * xy)), 8, 32))
+        out.append(terrain_world((xy, xy, z), seed=seed * 1000 + 500 + i, n_types=32))
+    return out
+
+
+def poisson_arrivals(n: int, rate: float, seed: int) -> np.ndarray:
+    """n arrival times (s) of a Poisson process of `rate` per second, starting at 0."""
+    u = uniform(seed, 9201, n)
+    gaps = -np.log(np.maximum(1.0 - u, 1e-300)) / rate
+    t = np.cumsum(gaps)
+    return t - t[0]
+
+
 def small_world(dims=(8, 8, 8), seed: int = 1234) -> World:
     """The 8x8x8 terrain world with 32 block types."""
     return terrain_world(dims, seed=seed, n_types=32)

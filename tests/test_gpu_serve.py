@@ -1,0 +1,179 @@
+"""Relight server (lumrad_server_*): continuously batched edit + relight requests.
+
+Each request's result must equal the CPU oracle's pass over the edited world with the request's
+dirty-probe list; a world's result must be identical alone and in a mix with other worlds'
+requests (several launches in flight); the HBM budget must gate admission without changing any
+result."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from lum_gb300 import worldgen
+from tests.helpers import RTOL, random_prev, rel_err
+
+pytestmark = pytest.mark.gpu
+
+DIMS = [(8, 8, 8), (12, 6, 5), (16, 16, 4), (5, 9, 7)]
+RAYS = [64, 32, 128, 64]
+
+
+def _worlds():
+    return [worldgen.terrain_world(d, seed=40 + i, n_types=32) for i, d in enumerate(DIMS)]
+
+
+def _requests(n_per_world, seed=1):
+    """[(world, edits, rays, time_seed)] interleaved over the worlds."""
+    out = []
+    for k in range(n_per_world):
+        for i, d in enumerate(DIMS):
+            e = worldgen.edit_request(d, 0.01 + 0.04 * ((k + i) % 3) / 2, seed=seed, stream=100 * i + k)
+            out.append((i, e, RAYS[i], 1000 * i + k))
+    return out
+
+
+def _server(worlds, which, **kw):
+    import lum_gb300
+    srv = lum_gb300.RadianceServer(**kw)
+    rws = []
+    for i in which:
+        w = worlds[i]
+        rw = lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0])
+        rw.load(w)
+        rw.set_radiance(random_prev(w, seed=200 + i))
+        srv.add_world(rw)
+        rws.append(rw)
+    return srv, rws
+
+
+def _submit(srv, reqs, which):
+    import lum_gb300
+    idx = {w: k for k, w in enumerate(which)}
+    for i, e, r, seed in reqs:
+        if i in idx:
+            srv.submit(idx[i], e, lum_gb300.pass_params(rays=r, max_dist=64.0, blend=0.1, time_seed=seed))
+
+
+def test_server_matches_oracle():
+    import oracle
+    worlds = _worlds()
+    reqs = _requests(3)
+    which = list(range(len(DIMS)))
+    srv, rws = _server(worlds, which, max_inflight=2)
+    _submit(srv, reqs, which)
+    srv.run(timeout_s=300)
+    done = srv.poll()
+    assert len(done) == len(reqs) and (done["status"] == 0).all()
+    got = [srv.get_radiance(i) for i in which]
+    for i in which:
+        w = worlds[i]
+        cur = random_prev(w, seed=200 + i)
+        grid = w.grid
+        for j, e, r, seed in reqs:
+            if j != i:
+                continue
+            grid = worldgen.apply_edits(grid, e)
+            req = worldgen.dirty_probes(w.dims, e, 2)
+            we = dataclasses.replace(w, grid=grid)
+            cur, _, _ = oracle.radiance_pass(we, req, rays=r, max_dist=64.0, blend=0.1, time_seed=seed, prev=cur)
+        err = rel_err(got[i], cur).max()
+        assert err <= RTOL, (i, err)
+        # the server's grid is the edited grid
+        for x, y, z in [(0, 0, 0), (w.dims[0] - 1, w.dims[1] - 1, w.dims[2] - 1)]:
+            assert rws[i].get_world_block(x, y, z) == grid[z, y, x]
+    # every request's probe count is its dirty list's length
+    lens = {}
+    for j, e, r, seed in reqs:
+        lens.setdefault(j, []).append(worldgen.dirty_probes(DIMS[j], e, 2).shape[0])
+    for j in which:
+        assert list(done[done["world"] == j]["probes"]) == lens[j]
+    srv.close()
+    for rw in rws:
+        rw.close()
+
+
+def test_alone_equals_mix():
+    worlds = _worlds()
+    reqs = _requests(4, seed=2)
+    mix, mix_rws = _server(worlds, [0, 1, 2, 3], max_inflight=3)
+    _submit(mix, reqs, [0, 1, 2, 3])
+    mix.run(timeout_s=300)
+    st = mix.stats()
+    assert st["requests"] == len(reqs)
+    for i in range(len(DIMS)):
+        alone, rws = _server(worlds, [i], max_inflight=1)
+        _submit(alone, reqs, [i])
+        alone.run(timeout_s=300)
+        assert alone.get_radiance(0).tobytes() == mix.get_radiance(i).tobytes(), i
+        alone.close()
+        for rw in rws:
+            rw.close()
+    mix.close()
+    for rw in mix_rws:
+        rw.close()
+
+
+def test_budget_gates_admission():
+    import lum_gb300
+    worlds = _worlds()
+    reqs = _requests(2, seed=3)
+    free, free_rws = _server(worlds, [0, 1, 2, 3])
+    _submit(free, reqs, [0, 1, 2, 3])
+    free.run(timeout_s=300)
+    st0 = free.stats()
+    assert st0["max_requests_in_launch"] == 4
+    # room for the worlds, the launch buffers and about one request at a time (a request here
+    # needs at most ~10 KB: its dirty list bound, edits and table entry)
+    headroom = 12_000
+    tight, tight_rws = _server(worlds, [0, 1, 2, 3], hbm_budget_bytes=st0["resident_bytes"] + st0["launch_bytes"] + headroom)
+    _submit(tight, reqs, [0, 1, 2, 3])
+    tight.run(timeout_s=300)
+    st1 = tight.stats()
+    assert st1["requests"] == len(reqs)
+    assert 0 < st1["peak_inflight_bytes"] <= headroom
+    assert st1["max_requests_in_launch"] < 4
+    for i in range(4):
+        assert tight.get_radiance(i).tobytes() == free.get_radiance(i).tobytes()
+    for s in (free, tight):
+        s.close()
+    for rw in free_rws + tight_rws:
+        rw.close()
+
+
+def test_request_that_never_fits_is_refused():
+    import lum_gb300
+    worlds = _worlds()
+    probe, rws = _server(worlds, [2])
+    st = probe.stats()
+    probe.close()
+    for rw in rws:
+        rw.close()
+    tiny, rws = _server(worlds, [2], hbm_budget_bytes=st["resident_bytes"] + st["launch_bytes"] + 1000)
+    before = tiny.get_radiance(0)
+    big = worldgen.edit_request(DIMS[2], 0.5, seed=9, stream=0)
+    tiny.submit(0, big, lum_gb300.pass_params(rays=64))
+    tiny.run(timeout_s=60)
+    d = tiny.poll()
+    assert len(d) == 1 and d["status"][0] == lum_gb300._native.LUMRAD_ENOMEM
+    assert tiny.get_radiance(0).tobytes() == before.tobytes()
+    x, y, z = (int(v) for v in big[-1][:3])
+    assert rws[0].get_world_block(x, y, z) == worlds[2].grid[z, y, x]
+    tiny.close()
+    for rw in rws:
+        rw.close()
+
+
+def test_owned_context_rejects_direct_calls():
+    import lum_gb300
+    worlds = _worlds()
+    srv, rws = _server(worlds, [0])
+    with pytest.raises(lum_gb300.LumRadError) as ei:
+        rws[0].radiance_pass(worldgen.all_probes(DIMS[0]), lum_gb300.pass_params())
+    assert ei.value.code == lum_gb300._native.LUMRAD_ESTATE
+    with pytest.raises(lum_gb300.LumRadError):
+        rws[0].set_world_block(0, 0, 0, 3)
+    srv.close()
+    # released by the server: direct calls work again
+    rws[0].radiance_pass(worldgen.all_probes(DIMS[0]), lum_gb300.pass_params())
+    rws[0].synchronize()
+    rws[0].close()
