@@ -142,17 +142,40 @@ int  lumrad_set_radiance(LumRadContext ctx, const float* rgb);
 
 /* ---- the pass ----------------------------------------------------------------------------- */
 /* Update list of LumInternalRenderer::update_radiance (internal_render.cpp:1142-1168):
- * blocks whose clamped 3x3x3 neighbourhood sums to > 0, then the queued special requests.
- * Writes up to `cap` entries of (x,y,z,0) into out; *n = full list length. */
+ * blocks whose clamped 3x3x3 neighbourhood sums to > 0 (scan order), then the queued special
+ * requests whose block is not already listed (request order).  Built on the device from the
+ * resident grid.  Writes up to `cap` entries of (x,y,z,w) into out; *n = full list length;
+ * the special queue is kept. */
 int  lumrad_build_update_list(LumRadContext ctx, int16_t* out, int cap, int* n);
 /* Queue one special request (specialRadianceUpdates, internal_render.cpp:1164-1168). */
 int  lumrad_request_update(LumRadContext ctx, int x, int y, int z);
 
-/* The drop-in for LumInternalRenderer::update_radiance() (internal_render.cpp:1129-1214):
- * builds the update list, uploads it and runs one pass.  With params->size == 0 the time
- * slicing adapts as the reference does (magicSize in [1,10], 1.8-2.2 ms target) and
- * time_seed/shift follow the context's frame counter. */
+/* The drop-in for one frame's radiance work in Renderer::submitFrame (renderer.cpp:436-438):
+ * shift_radiance by the stored shift, then LumInternalRenderer::update_radiance()
+ * (internal_render.cpp:1129-1214): builds the update list on the device (consuming the special
+ * requests) and runs one pass.  With params->size == 0 the time slicing adapts as the reference
+ * does (magicSize in [1,10], 1.8-2.2 ms target) and time_seed/shift follow the context's frame
+ * counter. */
 int  lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params);
+
+/* shift_radiance (internal_render.cpp:1218-1335), applied now: the volume becomes
+ * new(p) = old(p + shift) where p + shift lies inside the world, old(p) elsewhere.  A shift
+ * with |shift| >= the world's size on any axis leaves the volume unchanged (the reference
+ * returns early for x and leaves y/z undefined). */
+int  lumrad_shift_radiance(LumRadContext ctx, int dx, int dy, int dz);
+/* Renderer::setStoredRadianceShift / getStoredRadianceShift (renderer.cpp:604-609): the shift
+ * lumrad_update_radiance applies before each pass (it stays set until changed). */
+int  lumrad_set_radiance_shift(LumRadContext ctx, int dx, int dy, int dz);
+int  lumrad_get_radiance_shift(LumRadContext ctx, int* shift3);
+
+/* The radiance consumer's 8-probe gather, diffuse.frag:36-90 (sample_radiance(position,
+ * normal)): for each point (x, y, z, nx, ny, nz; position in voxel units, normal as given),
+ * trilinear weights of the 8 surrounding probes times clamp(dot(dir_to_probe, normal), 0.1, 1),
+ * each weight at least 1e-7, probe values clamped to [0, 2] (probes past the volume read 0);
+ * rgb = sum(w * probe) / sum(w).  points: n*6 floats, rgb: n*3 floats. */
+int  lumrad_gather_radiance(LumRadContext ctx, const float* points, int n, float* rgb);
+/* The same on device pointers, enqueued on the context's stream (see lumrad_get_stream). */
+int  lumrad_gather_radiance_device(LumRadContext ctx, const float* d_points, int n, float* d_rgb);
 
 /* One pass over an explicit update list of n entries (x,y,z,w) — the body of
  * radiance.comp:361-413 dispatched over n/size workgroups.  int16 coordinates. */

@@ -138,6 +138,24 @@ class RadianceWorld:
             req = req.astype(np.int16, copy=False)
             check(self.lib.lumrad_radiance_pass(self.h, ptr(req), req.shape[0], C.byref(params)))
 
+    def shift_radiance(self, dx: int, dy: int, dz: int) -> None:
+        check(self.lib.lumrad_shift_radiance(self.h, int(dx), int(dy), int(dz)))
+
+    def set_radiance_shift(self, dx: int, dy: int, dz: int) -> None:
+        check(self.lib.lumrad_set_radiance_shift(self.h, int(dx), int(dy), int(dz)))
+
+    def get_radiance_shift(self) -> tuple:
+        out = (C.c_int * 3)()
+        check(self.lib.lumrad_get_radiance_shift(self.h, out))
+        return tuple(out)
+
+    def gather(self, points: np.ndarray) -> np.ndarray:
+        """diffuse.frag's 8-probe radiance gather at (n, 6) points (position, normal)."""
+        p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 6)
+        out = np.zeros((p.shape[0], 3), dtype=np.float32)
+        check(self.lib.lumrad_gather_radiance(self.h, ptr(p), p.shape[0], ptr(out)))
+        return out
+
     def upload_requests(self, slot: int, requests: np.ndarray) -> None:
         req = np.ascontiguousarray(requests, dtype=np.int16)
         check(self.lib.lumrad_upload_requests(self.h, slot, ptr(req), req.shape[0]))

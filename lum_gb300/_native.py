@@ -99,6 +99,11 @@ _SIGS = {
     "lumrad_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lumrad_get_kernel_times": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
     "lumrad_direction_table": (C.c_int, [C.c_int, _P]),
+    "lumrad_shift_radiance": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "lumrad_set_radiance_shift": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "lumrad_get_radiance_shift": (C.c_int, [_P, _P]),
+    "lumrad_gather_radiance": (C.c_int, [_P, _P, C.c_int, _P]),
+    "lumrad_gather_radiance_device": (C.c_int, [_P, _P, C.c_int, _P]),
     "lumrad_radiance_pass_noalloc": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.POINTER(PassParams),
                                                _P]),
     "lumrad_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(_P)]),

@@ -401,6 +401,50 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     return LUMRAD_OK;
 }
 
+int Context::build_list_device(bool consume, int* n) {
+    int rc = world.sync_inputs(stream);
+    if (rc) return rc;
+    const long long W = (long long)world.W;
+    if (!list.bits) {
+        LUMRAD_TRY(cudaMalloc(&list.bits, list_scratch_words(W) * sizeof(uint32_t)));
+        LUMRAD_TRY(cudaMalloc(&list.cta_counts, list_scratch_ctas(W) * sizeof(int)));
+        LUMRAD_TRY(cudaMalloc(&list.cta_offsets, list_scratch_ctas(W) * sizeof(int)));
+        LUMRAD_TRY(cudaMalloc(&list.listed, sizeof(int)));
+        LUMRAD_TRY(cudaMalloc(&d_list_count, sizeof(int)));
+        LUMRAD_TRY(cudaMallocHost(&h_list_count, sizeof(int)));
+    }
+    const size_t ns = specials.size() / 4;
+    if ((rc = ensure_req_capacity((size_t)W + ns))) return rc;
+    if (ns > specials_cap) {
+        LUMRAD_TRY(cudaStreamSynchronize(stream));
+        cudaFree(d_specials);
+        d_specials = nullptr;
+        specials_cap = 0;
+        LUMRAD_TRY(cudaMalloc(&d_specials, std::max<size_t>(ns, 256) * sizeof(short4)));
+        specials_cap = std::max<size_t>(ns, 256);
+    }
+    if (ns) LUMRAD_TRY(cudaMemcpyAsync(d_specials, specials.data(), ns * sizeof(short4), cudaMemcpyHostToDevice, stream));
+    LUMRAD_TRY(launch_update_list(world.d_grid, world.X, world.Y, world.Z, d_specials, (int)ns, list, d_req,
+                                  d_list_count, stream));
+    LUMRAD_TRY(cudaMemcpyAsync(h_list_count, d_list_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));   // the pass's size is needed on the host
+    *n = *h_list_count;
+    if (consume) specials.clear();
+    return LUMRAD_OK;
+}
+
+// shift_radiance (internal_render.cpp:1218-1335) into the other ping-pong volume.  The reference
+// skips the copy when |shift.x| >= world_size.x and leaves larger y/z shifts undefined (a negative
+// copy extent); here any axis with |shift| >= its size leaves the volume unchanged.
+int Context::shift_volume(int dx, int dy, int dz) {
+    if (dx == 0 && dy == 0 && dz == 0) return LUMRAD_OK;
+    if (std::abs(dx) >= world.X || std::abs(dy) >= world.Y || std::abs(dz) >= world.Z) return LUMRAD_OK;
+    LUMRAD_TRY(launch_shift_radiance(world.d_rad[world.cur], world.d_rad[1 - world.cur], world.X, world.Y, world.Z, dx,
+                                     dy, dz, world.precision, stream));
+    world.cur = 1 - world.cur;
+    return LUMRAD_OK;
+}
+
 void Context::release() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
@@ -413,6 +457,14 @@ void Context::release() {
     cudaFree(d_ray_blk);
     for (auto& kv : resident) cudaFree(kv.second.ptr);
     if (h_req_pinned) cudaFreeHost(h_req_pinned);
+    cudaFree(list.bits);
+    cudaFree(list.cta_counts);
+    cudaFree(list.cta_offsets);
+    cudaFree(list.listed);
+    cudaFree(d_specials);
+    cudaFree(d_list_count);
+    if (h_list_count) cudaFreeHost(h_list_count);
+    cudaFree(d_gather);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_end) cudaEventDestroy(ev_end);
     if (ev_req) cudaEventDestroy(ev_req);
@@ -438,38 +490,6 @@ int check_params(const LumRadPassParams* p) {
     if (p->size < 0 || p->size > (1 << 20)) return fail(LUMRAD_EINVAL, "size out of range");
     if (p->size > 0 && (p->shift < 0 || p->shift >= p->size)) return fail(LUMRAD_EINVAL, "shift must be in [0, size)");
     return LUMRAD_OK;
-}
-
-// The 27-neighbour rule of update_radiance (internal_render.cpp:1142-1161) plus specials
-// (:1164-1168).  Specials are consumed, as the reference clears them.
-void build_list(Context* c, std::vector<int16_t>& out) {
-    const DeviceWorld& w = c->world;
-    const int X = w.X, Y = w.Y, Z = w.Z;
-    std::vector<uint8_t> set(w.W, 0);
-    out.clear();
-    const int16_t* g = w.h_grid.data();
-    for (int z = 0; z < Z; z++)
-        for (int y = 0; y < Y; y++)
-            for (int x = 0; x < X; x++) {
-                int sum = 0;
-                for (int dz = -1; dz <= 1; dz++) {
-                    const int tz = std::min(std::max(z + dz, 0), Z - 1);
-                    for (int dy = -1; dy <= 1; dy++) {
-                        const int ty = std::min(std::max(y + dy, 0), Y - 1);
-                        const int16_t* row = g + (size_t)X * ((size_t)ty + (size_t)Y * tz);
-                        for (int dx = -1; dx <= 1; dx++) sum += row[std::min(std::max(x + dx, 0), X - 1)];
-                    }
-                }
-                if (sum > 0) {
-                    out.insert(out.end(), {(int16_t)x, (int16_t)y, (int16_t)z, 0});
-                    set[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * z)] = 1;
-                }
-            }
-    for (size_t i = 0; i + 3 < c->specials.size(); i += 4) {
-        const int16_t* u = &c->specials[i];
-        if (!set[(size_t)u[0] + (size_t)X * ((size_t)u[1] + (size_t)Y * u[2])]) out.insert(out.end(), u, u + 4);
-    }
-    c->specials.clear();
 }
 
 }  // namespace lumrad
@@ -695,12 +715,16 @@ int lumrad_request_update(LumRadContext ctx, int x, int y, int z) {
 int lumrad_build_update_list(LumRadContext ctx, int16_t* out, int cap, int* n) {
     Context* c = as_ctx(ctx);
     if (!c || !n || (cap > 0 && !out)) return fail(LUMRAD_EINVAL, "null argument");
-    const std::vector<int16_t> specials = c->specials;   // building the list alone keeps the queue
-    std::vector<int16_t> list;
-    build_list(c, list);
-    c->specials = specials;
-    const int total = (int)(list.size() / 4);
-    if (cap > 0) std::memcpy(out, list.data(), (size_t)std::min(total, cap) * 4 * sizeof(int16_t));
+    if (int rc = check_unowned(c)) return rc;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    int total = 0;
+    int rc = c->build_list_device(false, &total);   // building the list alone keeps the queue
+    if (rc) return rc;
+    if (cap > 0 && total > 0) {
+        LUMRAD_TRY(cudaMemcpyAsync(out, c->d_req, (size_t)std::min(total, cap) * sizeof(short4), cudaMemcpyDeviceToHost,
+                                   c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    }
     *n = total;
     return LUMRAD_OK;
 }
@@ -715,11 +739,68 @@ int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
         LUMRAD_TRY(cudaEventSynchronize(c->ev_end));
         LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ev_start, c->ev_end));
     }
-    std::vector<int16_t> list;
-    build_list(c, list);
-    const size_t n = list.size() / 4;
-    if ((rc = c->stage_requests(list.data(), n))) return rc;
-    return c->run_pass(c->d_req, (int)n, params);
+    if ((rc = check_unowned(c))) return rc;
+    // a frame of Renderer::submitFrame: shift_radiance, then update_radiance (renderer.cpp:436-438)
+    if ((rc = c->shift_volume(c->shift[0], c->shift[1], c->shift[2]))) return rc;
+    int n = 0;
+    if ((rc = c->build_list_device(true, &n))) return rc;
+    return c->run_pass(c->d_req, n, params);
+}
+
+int lumrad_shift_radiance(LumRadContext ctx, int dx, int dy, int dz) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    if (int rc = check_unowned(c)) return rc;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    return c->shift_volume(dx, dy, dz);
+}
+
+int lumrad_set_radiance_shift(LumRadContext ctx, int dx, int dy, int dz) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    c->shift[0] = dx;
+    c->shift[1] = dy;
+    c->shift[2] = dz;
+    return LUMRAD_OK;
+}
+
+int lumrad_get_radiance_shift(LumRadContext ctx, int* shift) {
+    Context* c = as_ctx(ctx);
+    if (!c || !shift) return fail(LUMRAD_EINVAL, "null argument");
+    for (int i = 0; i < 3; i++) shift[i] = c->shift[i];
+    return LUMRAD_OK;
+}
+
+int lumrad_gather_radiance_device(LumRadContext ctx, const float* d_points, int n, float* d_rgb) {
+    Context* c = as_ctx(ctx);
+    if (!c || n < 0 || (n > 0 && (!d_points || !d_rgb))) return fail(LUMRAD_EINVAL, "bad argument");
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    const DeviceWorld& w = c->world;
+    LUMRAD_TRY(launch_gather(w.d_rad[w.cur], w.X, w.Y, w.Z, w.precision, d_points, n, d_rgb, c->stream));
+    return LUMRAD_OK;
+}
+
+int lumrad_gather_radiance(LumRadContext ctx, const float* points, int n, float* rgb) {
+    Context* c = as_ctx(ctx);
+    if (!c || n < 0 || (n > 0 && (!points || !rgb))) return fail(LUMRAD_EINVAL, "bad argument");
+    if (n == 0) return LUMRAD_OK;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    if ((size_t)n > c->gather_cap) {
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+        cudaFree(c->d_gather);
+        c->d_gather = nullptr;
+        c->gather_cap = 0;
+        LUMRAD_TRY(cudaMalloc(&c->d_gather, (size_t)n * 9 * sizeof(float)));
+        c->gather_cap = (size_t)n;
+    }
+    float* d_pts = c->d_gather;
+    float* d_out = c->d_gather + (size_t)n * 6;
+    LUMRAD_TRY(cudaMemcpyAsync(d_pts, points, (size_t)n * 6 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    int rc = lumrad_gather_radiance_device(ctx, d_pts, n, d_out);
+    if (rc) return rc;
+    LUMRAD_TRY(cudaMemcpyAsync(rgb, d_out, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    return LUMRAD_OK;
 }
 
 int lumrad_radiance_pass(LumRadContext ctx, const int16_t* requests, int n, const LumRadPassParams* params) {

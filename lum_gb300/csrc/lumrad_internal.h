@@ -85,6 +85,33 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
 // its counters (descriptors already on the device).
 cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream);
 
+// Device scratch of the update-list builder for a world of W blocks: ceil(W/32) flag words,
+// ceil(W/256) CTA counts and offsets, and the count of rule-listed blocks.
+struct ListScratch {
+    uint32_t* bits;
+    int* cta_counts;
+    int* cta_offsets;
+    int* listed;
+};
+size_t list_scratch_words(long long W);
+size_t list_scratch_ctas(long long W);
+
+// update_radiance's list (internal_render.cpp:1142-1168) built on the device from the int16
+// grid: rule-listed blocks in scan order, then the specials not already listed, in order.
+// out holds W + n_specials entries; *count (device) receives the list length.
+cudaError_t launch_update_list(const int16_t* grid, int X, int Y, int Z, const short4* specials, int n_specials,
+                               const ListScratch& scratch, short4* out, int* count, cudaStream_t stream);
+
+// shift_radiance (internal_render.cpp:1218-1335) from src into dst: dst(p) = src(p + shift)
+// where p + shift is inside the world, src(p) elsewhere.
+cudaError_t launch_shift_radiance(const void* src, void* dst, int X, int Y, int Z, int sx, int sy, int sz,
+                                  int precision, cudaStream_t stream);
+
+// diffuse.frag's 8-probe gather (sample_radiance(position, normal), :36-90) of n points
+// (x, y, z, nx, ny, nz in voxel units) from a radiance volume; out: n x 3 floats.
+cudaError_t launch_gather(const void* rad, int X, int Y, int Z, int precision, const float* pts, int n, float* out,
+                          cudaStream_t stream);
+
 // One block edit of a served world: worlds[world].grid[index] = block and its compact id.
 struct EditRecord {
     int world;                   // index into the launch's world table

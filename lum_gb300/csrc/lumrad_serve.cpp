@@ -250,7 +250,10 @@ void complete_now(Server* sv, const SRequest& r, int status) {
 }
 
 // Forms and enqueues one launch on slot `k`; *started = false if no request was due and fit.
-int launch(Server* sv, int k, bool* started) {
+// With `free_slots` launch slots idle, a launch takes at most 1/free_slots of the due requests,
+// so under load several launches run at once and a finished one frees its worlds while the
+// others still keep the GPU busy.
+int launch(Server* sv, int k, int free_slots, bool* started) {
     *started = false;
     Slot& sl = *sv->slots[k];
     const double now = sv->now();
@@ -266,6 +269,8 @@ int launch(Server* sv, int k, bool* started) {
               [&](int a, int b) { return sv->worlds[a].fifo.front().id < sv->worlds[b].fifo.front().id; });
     sl.reqs.clear();
     size_t bytes = 0;
+    int cap = (int)((cand.size() + (size_t)free_slots - 1) / (size_t)free_slots);
+    if (sv->s.max_requests_per_launch > 0) cap = std::min(cap, sv->s.max_requests_per_launch);
     for (int w : cand) {
         SWorld& sw = sv->worlds[w];
         const size_t need = sv->request_bytes(sw.fifo.front());
@@ -278,7 +283,7 @@ int launch(Server* sv, int k, bool* started) {
         bytes += need;
         sl.reqs.push_back(std::move(sw.fifo.front()));
         sw.fifo.pop_front();
-        if (sv->s.max_requests_per_launch > 0 && (int)sl.reqs.size() >= sv->s.max_requests_per_launch) break;
+        if ((int)sl.reqs.size() >= cap) break;
     }
     const int nl = (int)sl.reqs.size();
     if (nl == 0) return LUMRAD_OK;
@@ -408,11 +413,14 @@ int launch(Server* sv, int k, bool* started) {
 int progress(Server* sv) {
     int rc = retire(sv);
     if (rc) return rc;
-    for (size_t k = 0; k < sv->slots.size(); k++) {
+    int free_slots = 0;
+    for (auto& sl : sv->slots) free_slots += sl->busy ? 0 : 1;
+    for (size_t k = 0; k < sv->slots.size() && free_slots > 0; k++) {
         if (sv->slots[k]->busy) continue;
         bool started = false;
-        if ((rc = launch(sv, (int)k, &started))) return rc;
+        if ((rc = launch(sv, (int)k, free_slots, &started))) return rc;
         if (!started) break;
+        free_slots--;
     }
     return LUMRAD_OK;
 }

@@ -118,12 +118,27 @@ struct Context {
     int frame = 0;
     int magic_size = 1;
     float last_ms = 0.0f;
+    // radiance shift applied before each lumrad_update_radiance (Renderer::stored_radiance_shift)
+    int shift[3] = {0, 0, 0};
+    // device update-list builder
+    ListScratch list{};
+    short4* d_specials = nullptr;
+    size_t specials_cap = 0;
+    int* d_list_count = nullptr;
+    int* h_list_count = nullptr;          // pinned
+    // gather staging (host-buffer calls)
+    float* d_gather = nullptr;
+    size_t gather_cap = 0;                // points
 
     int ensure_req_capacity(size_t n);
     int ensure_rays(long long n_tasks);
     int stage_requests(const int16_t* req, size_t n);
     int run_pass(const short4* d_req, int n, const LumRadPassParams* p);
     int check_error();
+    // Builds update_radiance's list on the device into d_req; *n = its length.  The queued
+    // specials are consumed when `consume` is set.
+    int build_list_device(bool consume, int* n);
+    int shift_volume(int dx, int dy, int dz);
     void release();
 };
 
@@ -131,6 +146,5 @@ Context* as_ctx(LumRadContext c);
 // LUMRAD_ESTATE if a server owns the context (its grid and passes are the server's).
 int check_unowned(const Context* c);
 int check_params(const LumRadPassParams* p);
-void build_list(Context* c, std::vector<int16_t>& out);
 
 }  // namespace lumrad

@@ -1,0 +1,272 @@
+// radiance_aux.cu — the device work either side of the radiance pass:
+//
+//   update list   the probes update_radiance relights each frame (internal_render.cpp:1142-1168):
+//                 every block whose clamped 3x3x3 neighbourhood has a positive id sum, in scan
+//                 order, then each special request whose block is not already listed, in request
+//                 order.  Four launches: flag (one bit per block, ballot) + per-CTA counts, a
+//                 single-CTA scan of the counts, an order-preserving write, and the specials.
+//   scroll        shift_radiance (internal_render.cpp:1218-1335): new(p) = old(p + shift) where
+//                 p + shift is inside the world, old(p) elsewhere; one pass into the other
+//                 ping-pong volume.
+//   gather        the 8-probe consumer read of diffuse.frag:36-90 (sample_radiance(position,
+//                 normal)): trilinear weights times a clamped directional weight over the 8
+//                 surrounding probes, probe values clamped to [0, 2].
+//
+// All FP32 arithmetic is written out in the shader's order with round-to-nearest intrinsics (no
+// contraction), so results are reproducible bit for bit.
+
+#include "radiance_device.cuh"
+
+#include <algorithm>
+
+namespace lumrad {
+namespace {
+
+constexpr int kListCta = 256;      // blocks per CTA of the list kernels (8 warps)
+constexpr int kScanCta = 1024;
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__global__ void __launch_bounds__(kListCta)
+list_flags_kernel(const int16_t* __restrict__ grid, int X, int Y, int Z, long long W, uint32_t* __restrict__ bits,
+                  int* __restrict__ cta_counts) {
+    __shared__ int s_cnt[kListCta / 32];
+    const long long i = (long long)blockIdx.x * kListCta + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool flag = false;
+    if (i < W) {
+        const int x = (int)(i % X);
+        const long long q = i / X;
+        const int y = (int)(q % Y);
+        const int z = (int)(q / Y);
+        int sum = 0;   // sum of the 27 clamped neighbours' ids (internal_render.cpp:1147-1156)
+        for (int dz = -1; dz <= 1; dz++) {
+            const int tz = clampi(z + dz, 0, Z - 1);
+            for (int dy = -1; dy <= 1; dy++) {
+                const int ty = clampi(y + dy, 0, Y - 1);
+                const int16_t* row = grid + (size_t)X * ((size_t)ty + (size_t)Y * tz);
+                for (int dx = -1; dx <= 1; dx++) sum += __ldg(row + clampi(x + dx, 0, X - 1));
+            }
+        }
+        flag = sum > 0;
+    }
+    const unsigned b = __ballot_sync(kFull, flag);
+    const long long word = i >> 5;
+    if (lane == 0) {
+        if (word < (W + 31) / 32) bits[word] = b;
+        s_cnt[warp] = __popc(b);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int w = 0; w < kListCta / 32; w++) c += s_cnt[w];
+        cta_counts[blockIdx.x] = c;
+    }
+}
+
+// Exclusive scan of `v` over the CTA (kScanCta threads); returns the CTA total through *total.
+__device__ __forceinline__ int cta_exclusive_scan(int v, int* s_warp, int* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = s_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += t;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    const int excl = x - v + (warp > 0 ? s_warp[warp - 1] : 0);
+    *total = s_warp[31];
+    __syncthreads();   // s_warp is reused by the next call
+    return excl;
+}
+
+__global__ void __launch_bounds__(kScanCta)
+list_scan_kernel(const int* __restrict__ counts, int n, int* __restrict__ offsets, int* __restrict__ total) {
+    __shared__ int s_warp[32];
+    int carry = 0;
+    for (int base = 0; base < n; base += kScanCta) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? counts[i] : 0;
+        int chunk = 0;
+        const int excl = cta_exclusive_scan(v, s_warp, &chunk);
+        if (i < n) offsets[i] = carry + excl;
+        carry += chunk;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kListCta)
+list_write_kernel(const uint32_t* __restrict__ bits, const int* __restrict__ offsets, int X, int Y, long long W,
+                  short4* __restrict__ out) {
+    __shared__ int s_pre[kListCta / 32];
+    const long long words = (W + 31) / 32;
+    if (threadIdx.x < kListCta / 32) {
+        const long long wi = (long long)blockIdx.x * (kListCta / 32) + threadIdx.x;
+        s_pre[threadIdx.x] = wi < words ? __popc(bits[wi]) : 0;
+    }
+    __syncthreads();
+    const long long i = (long long)blockIdx.x * kListCta + threadIdx.x;
+    if (i >= W) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t b = bits[i >> 5];
+    if (!((b >> lane) & 1u)) return;
+    int pos = offsets[blockIdx.x] + __popc(b & ((1u << lane) - 1u));
+    for (int w = 0; w < warp; w++) pos += s_pre[w];
+    const int x = (int)(i % X);
+    const long long q = i / X;
+    out[pos] = make_short4((short)x, (short)(q % Y), (short)(q / Y), 0);
+}
+
+// Specials in request order, each unless its block is already listed (duplicates are kept, as
+// in the reference: `set` only marks rule-listed blocks).
+__global__ void __launch_bounds__(kScanCta)
+list_specials_kernel(const short4* __restrict__ sp, int ns, const uint32_t* __restrict__ bits, int X, int Y,
+                     const int* __restrict__ listed, short4* __restrict__ out, int* __restrict__ count) {
+    __shared__ int s_warp[32];
+    int carry = *listed;
+    for (int base = 0; base < ns; base += kScanCta) {
+        const int i = base + threadIdx.x;
+        int keep = 0;
+        short4 s = make_short4(0, 0, 0, 0);
+        if (i < ns) {
+            s = sp[i];
+            const long long idx = (long long)s.x + (long long)X * ((long long)s.y + (long long)Y * s.z);
+            keep = ((bits[idx >> 5] >> (idx & 31)) & 1u) ? 0 : 1;
+        }
+        int chunk = 0;
+        const int excl = cta_exclusive_scan(keep, s_warp, &chunk);
+        if (keep) out[carry + excl] = s;
+        carry += chunk;
+    }
+    if (threadIdx.x == 0) *count = carry;
+}
+
+template <typename V>
+__global__ void shift_kernel(const V* __restrict__ src, V* __restrict__ dst, int X, int Y, int Z, int sx, int sy,
+                             int sz, long long W) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % X);
+        const long long q = i / X;
+        const int y = (int)(q % Y), z = (int)(q / Y);
+        const int qx = x + sx, qy = y + sy, qz = z + sz;
+        const bool inside = qx >= 0 && qx < X && qy >= 0 && qy < Y && qz >= 0 && qz < Z;
+        dst[i] = inside ? src[(size_t)qx + (size_t)X * ((size_t)qy + (size_t)Y * qz)] : src[i];
+    }
+}
+
+// sample_probe (diffuse.frag:25-33): texelFetch at the clamped probe (outside the volume reads 0,
+// the robust-access definition), clamped to [0, 2].
+template <class Store>
+__device__ __forceinline__ float3 gather_probe(const typename Store::T* rad, int X, int Y, int Z, int px, int py,
+                                               int pz) {
+    px = clampi(px, 0, X);
+    py = clampi(py, 0, Y);
+    pz = clampi(pz, 0, Z);
+    float3 v = make_float3(0.0f, 0.0f, 0.0f);
+    if (px < X && py < Y && pz < Z) v = Store::load(rad, (int)((size_t)px + (size_t)X * ((size_t)py + (size_t)Y * pz)));
+    return make_float3(gmin(gmax(v.x, 0.0f), 2.0f), gmin(gmax(v.y, 0.0f), 2.0f), gmin(gmax(v.z, 0.0f), 2.0f));
+}
+
+template <class Store>
+__global__ void gather_kernel(const typename Store::T* __restrict__ rad, int X, int Y, int Z,
+                              const float* __restrict__ pts, int n, float* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float* q = pts + 6 * (size_t)k;
+    const float px = q[0], py = q[1], pz = q[2], nx = q[3], ny = q[4], nz = q[5];
+    // zero probe: clamp(ivec3(floor(position - 8.0)) / 16, 0, world_size)   (:42)
+    const int zx = clampi(f2i(floorf(fsub(px, 8.0f))) / 16, 0, X);
+    const int zy = clampi(f2i(floorf(fsub(py, 8.0f))) / 16, 0, Y);
+    const int zz = clampi(f2i(floorf(fsub(pz, 8.0f))) / 16, 0, Z);
+    const float cx = fadd(fmul((float)zx, 16.0f), 8.0f);   // (:43)
+    const float cy = fadd(fmul((float)zy, 16.0f), 8.0f);
+    const float cz = fadd(fmul((float)zz, 16.0f), 8.0f);
+    // alpha = clamp((position - zero_probe_pos) / 16, 0, 1)   (:45); x/16 == x*0.0625 exactly
+    const float ax = gmin(gmax(fmul(fsub(px, cx), 0.0625f), 0.0f), 1.0f);
+    const float ay = gmin(gmax(fmul(fsub(py, cy), 0.0625f), 0.0f), 1.0f);
+    const float az = gmin(gmax(fmul(fsub(pz, cz), 0.0625f), 0.0f), 1.0f);
+    float tw = 0.0f, tr = 0.0f, tg = 0.0f, tb = 0.0f;
+#pragma unroll 1
+    for (int i = 0; i < 8; i++) {
+        const int ox = i & 1, oy = (i >> 1) & 1, oz = (i >> 2) & 1;   // (:50)
+        const float fx = (float)ox, fy = (float)oy, fz = (float)oz;
+        const float3 ptp = make_float3(fsub(fadd(cx, fmul(fx, 16.0f)), px), fsub(fadd(cy, fmul(fy, 16.0f)), py),
+                                       fsub(fadd(cz, fmul(fz, 16.0f)), pz));   // (:55-57)
+        const float3 dir = normalize3(ptp);   // (:58)
+        // mix(1 - alpha, alpha, offset) = (1-alpha)*(1-offset) + alpha*offset   (:60)
+        const float tx = fadd(fmul(fsub(1.0f, ax), fsub(1.0f, fx)), fmul(ax, fx));
+        const float ty = fadd(fmul(fsub(1.0f, ay), fsub(1.0f, fy)), fmul(ay, fy));
+        const float tz = fadd(fmul(fsub(1.0f, az), fsub(1.0f, fz)), fmul(az, fz));
+        float w = fmul(fmul(tx, ty), tz);   // (:61)
+        const float d = fadd(fadd(fmul(dir.x, nx), fmul(dir.y, ny)), fmul(dir.z, nz));
+        w = fmul(w, gmin(gmax(d, 0.1f), 1.0f));   // (:70-74)
+        const float3 c = gather_probe<Store>(rad, X, Y, Z, zx + ox, zy + oy, zz + oz);   // (:81)
+        w = gmax(1e-7f, w);   // (:84)
+        tw = fadd(tw, w);
+        tr = fadd(tr, fmul(w, c.x));
+        tg = fadd(tg, fmul(w, c.y));
+        tb = fadd(tb, fmul(w, c.z));
+    }
+    out[3 * (size_t)k] = fdiv(tr, tw);   // (:89)
+    out[3 * (size_t)k + 1] = fdiv(tg, tw);
+    out[3 * (size_t)k + 2] = fdiv(tb, tw);
+}
+
+}  // namespace
+
+cudaError_t launch_update_list(const int16_t* grid, int X, int Y, int Z, const short4* specials, int n_specials,
+                               const ListScratch& s, short4* out, int* count, cudaStream_t stream) {
+    const long long W = (long long)X * Y * Z;
+    const int ctas = (int)((W + kListCta - 1) / kListCta);
+    list_flags_kernel<<<ctas, kListCta, 0, stream>>>(grid, X, Y, Z, W, s.bits, s.cta_counts);
+    list_scan_kernel<<<1, kScanCta, 0, stream>>>(s.cta_counts, ctas, s.cta_offsets, s.listed);
+    list_write_kernel<<<ctas, kListCta, 0, stream>>>(s.bits, s.cta_offsets, X, Y, W, out);
+    list_specials_kernel<<<1, kScanCta, 0, stream>>>(specials, n_specials, s.bits, X, Y, s.listed, out, count);
+    return cudaGetLastError();
+}
+
+size_t list_scratch_words(long long W) { return (size_t)((W + 31) / 32); }
+size_t list_scratch_ctas(long long W) { return (size_t)((W + kListCta - 1) / kListCta); }
+
+cudaError_t launch_shift_radiance(const void* src, void* dst, int X, int Y, int Z, int sx, int sy, int sz,
+                                  int precision, cudaStream_t stream) {
+    const long long W = (long long)X * Y * Z;
+    const int blocks = (int)std::min<long long>((W + 255) / 256, 152LL * 16);
+    if (precision == LUMRAD_PRECISION_FP32)
+        shift_kernel<uint4><<<blocks, 256, 0, stream>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), X, Y,
+                                                        Z, sx, sy, sz, W);
+    else
+        shift_kernel<uint2><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(src), static_cast<uint2*>(dst), X, Y,
+                                                        Z, sx, sy, sz, W);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const void* rad, int X, int Y, int Z, int precision, const float* pts, int n, float* out,
+                          cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (n + 255) / 256;
+    switch (precision) {
+        case LUMRAD_PRECISION_FP16:
+            gather_kernel<StoreF16><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(rad), X, Y, Z, pts, n, out);
+            break;
+        case LUMRAD_PRECISION_BF16:
+            gather_kernel<StoreBF16><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(rad), X, Y, Z, pts, n, out);
+            break;
+        default:
+            gather_kernel<StoreF32><<<blocks, 256, 0, stream>>>(static_cast<const float4*>(rad), X, Y, Z, pts, n, out);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace lumrad

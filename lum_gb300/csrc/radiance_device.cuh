@@ -10,8 +10,6 @@
 #include <cuda/atomic>
 #include "lumrad_internal.h"
 
-#include "lumrad_internal.h"
-
 namespace lumrad {
 namespace {
 

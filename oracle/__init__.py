@@ -67,6 +67,8 @@ def load() -> C.CDLL:
     lib.oracle_direction_table.argtypes = [C.c_int, P]
     lib.oracle_trace_ray.argtypes = [P, P, P, P, C.c_float, P, P]
     lib.oracle_update_list.argtypes = [P, P, C.c_int, P, C.c_int, P]
+    lib.oracle_shift.argtypes = [C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int]
+    lib.oracle_gather.argtypes = [C.c_int, C.c_int, C.c_int, P, P, C.c_int, P]
     lib.oracle_max_threads.restype = C.c_int
     _lib = lib
     return lib
@@ -157,6 +159,24 @@ def update_list(world, specials: np.ndarray | None = None) -> np.ndarray:
     if rc != 0:
         raise ValueError("special request outside the world")
     return out[: n.value]
+
+
+def shift_radiance(volume: np.ndarray, shift) -> np.ndarray:
+    """shift_radiance (internal_render.cpp:1218-1335) of a (Z, Y, X, 3) float32 volume; returns a copy."""
+    v = np.ascontiguousarray(volume, dtype=np.float32).copy()
+    Z, Y, X, _ = v.shape
+    load().oracle_shift(X, Y, Z, v.ctypes.data, int(shift[0]), int(shift[1]), int(shift[2]))
+    return v
+
+
+def gather(volume: np.ndarray, points: np.ndarray) -> np.ndarray:
+    """diffuse.frag:24-90's 8-probe gather of a (Z, Y, X, 3) float32 volume at (n, 6) points."""
+    v = np.ascontiguousarray(volume, dtype=np.float32)
+    p = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 6)
+    out = np.zeros((p.shape[0], 3), dtype=np.float32)
+    Z, Y, X, _ = v.shape
+    load().oracle_gather(X, Y, Z, v.ctypes.data, p.ctypes.data, p.shape[0], out.ctypes.data)
+    return out
 
 
 def max_threads() -> int:

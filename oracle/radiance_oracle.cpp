@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 #include <algorithm>
@@ -504,6 +505,83 @@ int oracle_trace_ray(const OracleWorld* ow, const float* prev, const float* o3, 
         } else {
             hit->fraction = canon(ro.cast.fraction);
         }
+    }
+    return 0;
+}
+
+// shift_radiance (internal_render.cpp:1218-1335): the two image copies amount to
+// new(p) = old(p + shift) for p in the destination box [dst, dst + world - |shift|), where
+// dst = shift >= 0 ? 0 : -shift per axis, and old(p) elsewhere.  The reference returns early
+// only for |shift.x| >= world.x; a larger y or z shift gives it a negative extent, which is
+// defined here as no change.  vol: W*3 floats, updated in place.
+int oracle_shift(int X, int Y, int Z, float* vol, int sx, int sy, int sz) {
+    if (std::abs(sx) >= X || std::abs(sy) >= Y || std::abs(sz) >= Z) return 0;
+    const int off[3] = {sx, sy, sz}, size[3] = {X, Y, Z};
+    int src[3], dst[3], ext[3];
+    for (int a = 0; a < 3; a++) {
+        src[a] = off[a] >= 0 ? off[a] : 0;     // process_axis (:1234-1251)
+        dst[a] = off[a] >= 0 ? 0 : -off[a];
+        ext[a] = size[a] - std::abs(off[a]);   // intersection_size (:1268)
+    }
+    std::vector<float> tmp((size_t)ext[0] * ext[1] * ext[2] * 3);
+    for (int z = 0; z < ext[2]; z++)           // copy to temp (:1299-1301)
+        for (int y = 0; y < ext[1]; y++)
+            for (int x = 0; x < ext[0]; x++)
+                for (int c = 0; c < 3; c++)
+                    tmp[(((size_t)z * ext[1] + y) * ext[0] + x) * 3 + c] =
+                        vol[(((size_t)(z + src[2]) * Y + (y + src[1])) * X + (x + src[0])) * 3 + c];
+    for (int z = 0; z < ext[2]; z++)           // copy back at dst (:1312-1316)
+        for (int y = 0; y < ext[1]; y++)
+            for (int x = 0; x < ext[0]; x++)
+                for (int c = 0; c < 3; c++)
+                    vol[(((size_t)(z + dst[2]) * Y + (y + dst[1])) * X + (x + dst[0])) * 3 + c] =
+                        tmp[(((size_t)z * ext[1] + y) * ext[0] + x) * 3 + c];
+    return 0;
+}
+
+// The radiance consumer's gather, diffuse.frag:24-90 (sample_probe + sample_radiance(position,
+// normal)) at n points (x, y, z, nx, ny, nz) of a W*3 float volume; out: n*3 floats.
+// texelFetch past the volume reads 0 (the probe index is clamped to [0, world_size], one past
+// the last probe).  ivec3(floor(...)) converts like f2i; '/' on ints is OpSDiv (truncation).
+int oracle_gather(int X, int Y, int Z, const float* vol, const float* pts, int n, float* out) {
+    auto clampi = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi); };
+    auto probe = [&](int px, int py, int pz) -> V3 {   // sample_probe (:25-33)
+        px = clampi(px, 0, X); py = clampi(py, 0, Y); pz = clampi(pz, 0, Z);
+        V3 v{0.0f, 0.0f, 0.0f};
+        if (px < X && py < Y && pz < Z) {
+            const float* t = vol + (((size_t)pz * Y + py) * X + px) * 3;
+            v = V3{t[0], t[1], t[2]};
+        }
+        return V3{gmin(gmax(v.x, 0.0f), 2.0f), gmin(gmax(v.y, 0.0f), 2.0f), gmin(gmax(v.z, 0.0f), 2.0f)};
+    };
+    for (int k = 0; k < n; k++) {
+        const float* q = pts + 6 * (size_t)k;
+        const V3 pos{q[0], q[1], q[2]}, nrm{q[3], q[4], q[5]};
+        const int zx = clampi(f2i(std::floor(pos.x - 8.0f)) / 16, 0, X);   // (:42)
+        const int zy = clampi(f2i(std::floor(pos.y - 8.0f)) / 16, 0, Y);
+        const int zz = clampi(f2i(std::floor(pos.z - 8.0f)) / 16, 0, Z);
+        const V3 zp{(float)zx * 16.0f + 8.0f, (float)zy * 16.0f + 8.0f, (float)zz * 16.0f + 8.0f};   // (:43)
+        const V3 d = (pos - zp) * 0.0625f;   // (pos - zero_probe_pos) / 16.0, exact as * 1/16
+        const V3 alpha{gmin(gmax(d.x, 0.0f), 1.0f), gmin(gmax(d.y, 0.0f), 1.0f), gmin(gmax(d.z, 0.0f), 1.0f)};
+        float tw = 0.0f;
+        V3 tc{0.0f, 0.0f, 0.0f};
+        for (int i = 0; i < 8; i++) {
+            const int ox = i & 1, oy = (i >> 1) & 1, oz = (i >> 2) & 1;   // (:50)
+            const V3 off{(float)ox, (float)oy, (float)oz};
+            const V3 pp = zp + off * 16.0f;   // (:55)
+            const V3 dir = normalize3(pp - pos);   // (:57-58)
+            const V3 one{1.0f, 1.0f, 1.0f};
+            const V3 tri = (one - alpha) * (one - off) + alpha * off;   // mix(1-alpha, alpha, offset) (:60)
+            float w = (tri.x * tri.y) * tri.z;   // (:61)
+            w = w * gmin(gmax(dot3(dir, nrm), 0.1f), 1.0f);   // (:70-74)
+            const V3 c = probe(zx + ox, zy + oy, zz + oz);   // (:81)
+            w = gmax(1e-7f, w);   // (:84)
+            tw = tw + w;
+            tc = tc + V3{w * c.x, w * c.y, w * c.z};
+        }
+        out[3 * (size_t)k] = tc.x / tw;   // (:89)
+        out[3 * (size_t)k + 1] = tc.y / tw;
+        out[3 * (size_t)k + 2] = tc.z / tw;
     }
     return 0;
 }

@@ -117,7 +117,8 @@ def test_budget_gates_admission():
     import lum_gb300
     worlds = _worlds()
     reqs = _requests(2, seed=3)
-    free, free_rws = _server(worlds, [0, 1, 2, 3])
+    # one launch slot: a launch takes every due request (with more slots they are split)
+    free, free_rws = _server(worlds, [0, 1, 2, 3], max_inflight=1)
     _submit(free, reqs, [0, 1, 2, 3])
     free.run(timeout_s=300)
     st0 = free.stats()
@@ -125,7 +126,8 @@ def test_budget_gates_admission():
     # room for the worlds, the launch buffers and about one request at a time (a request here
     # needs at most ~10 KB: its dirty list bound, edits and table entry)
     headroom = 12_000
-    tight, tight_rws = _server(worlds, [0, 1, 2, 3], hbm_budget_bytes=st0["resident_bytes"] + st0["launch_bytes"] + headroom)
+    tight, tight_rws = _server(worlds, [0, 1, 2, 3], max_inflight=1,
+                               hbm_budget_bytes=st0["resident_bytes"] + st0["launch_bytes"] + headroom)
     _submit(tight, reqs, [0, 1, 2, 3])
     tight.run(timeout_s=300)
     st1 = tight.stats()
