@@ -311,6 +311,21 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
     return out
 
 
+def max_over_ranks(v: float, pg, device) -> float:
+    """The largest of every rank's v: the slowest replica sets the job's time."""
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: float, world_size: int, seconds: float) -> float:
+    """Whole-job throughput of replicas: every rank processes units_per_rank in `seconds` (the max)."""
+    return world_size * units_per_rank / seconds
+
+
 def dist_setup(args):
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -439,12 +454,9 @@ def main():
         torch.cuda.synchronize()
         if pg:
             pg.barrier()
-    total_ms = float(sum(step_ms))
-    if pg:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world_size * args.steps * rays_per_step / (total_ms / 1000.0)
+    dev = f"cuda:{local}"
+    total_ms = max_over_ranks(float(sum(step_ms)), pg, dev)
+    value = job_value(args.steps * rays_per_step, world_size, total_ms / 1000.0)
 
     hbm_peak, peak_kind = load_peaks()
     bytes_per_launch = float(np.mean(pass_bytes))
@@ -467,7 +479,7 @@ def main():
             rw2.radiance_pass(lists[p], params(p))
         rw2.get_radiance()
         e2e_s += time.perf_counter() - t0
-    e2e_value = world_size * args.steps * rays_per_step / e2e_s
+    e2e_value = job_value(args.steps * rays_per_step, world_size, max_over_ranks(e2e_s, pg, dev))
     h2d = int(sum(l.shape[0] * 8 for l in lists))
     d2h = int(world.n_blocks * 16)
 
