@@ -202,6 +202,37 @@ int  lumrad_get_stream(LumRadContext ctx, void** stream);
  * oldest first; *n = number written.  Synchronises. */
 int  lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n);
 
+/* ---- producers: voxel models blockified into the world (blockify + map) ---------------------
+ * Each frame the reference turns its animated voxel models into temporary palette blocks
+ * (Renderer::submitFrame, renderer.cpp:428-455): start_blockify / blockify_mesh / end_blockify
+ * (internal_render.cpp:977-1070), exec_copies (:1375-1476) and map_mesh + shaders/map.comp
+ * (:1484-1520).  lumrad_blockify does one frame of that: from the loaded (origin) world, every
+ * block under a mesh's AABB whose id is below static_blocks gets the next temporary slot
+ * (static_blocks, static_blocks+1, ... in mesh order, z-y-x within a mesh) holding a copy of the
+ * static block's voxels; slots from static_blocks up are cleared first; then each mesh's non-zero
+ * voxels are written into the temporary blocks through the inverse of its transform.  Passes
+ * after the call read the blockified world and palette; the origin world is kept, and the next
+ * lumrad_blockify (or any change of the origin world or palette) starts from it again.
+ * LUMRAD_ENOMEM if the temporary slots would pass max_block_types (the world is left as it was).
+ * Meshes are processed in the given order, so a later mesh's voxels win where meshes overlap
+ * (the reference sorts them by camera distance, renderer.cpp:407-414).  The reference's map.comp
+ * hard-codes 15 static blocks (its default static_block_palette_size); here it is the argument. */
+typedef struct {
+    float rot[4];           /* rotation quaternion x, y, z, w (glm::quat, MeshTransform.rot) */
+    float shift[3];         /* translation in voxels (MeshTransform.shift) */
+} LumRadMeshTransform;
+
+/* A voxel model (InternalMeshModel::voxels): sx*sy*sz uint8 material ids, x-fastest (the .vox
+ * model layout, load_stuff.cpp:376-385).  *model receives its index. */
+int  lumrad_load_model(LumRadContext ctx, const uint8_t* voxels, int sx, int sy, int sz, int* model);
+int  lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models,
+                     const LumRadMeshTransform* transforms, int n_meshes);
+/* The grid the next pass reads (blockified, or the origin world), X*Y*Z int16 x-fastest. */
+int  lumrad_get_world(LumRadContext ctx, int16_t* blocks);
+/* The device palette as the next pass reads it: max_block_types * 4096 uint8, slot-major,
+ * voxel (x,y,z) at x + 16y + 256z. */
+int  lumrad_get_block_palette(LumRadContext ctx, uint8_t* voxels);
+
 /* ---- batches: many worlds, one launch ------------------------------------------------------
  * The reference updates one world per frame with one dispatch and time-slices its probes
  * (internal_render.cpp:1190-1206).  A batch updates many resident worlds (contexts on one device,

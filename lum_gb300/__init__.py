@@ -138,6 +138,37 @@ class RadianceWorld:
             req = req.astype(np.int16, copy=False)
             check(self.lib.lumrad_radiance_pass(self.h, ptr(req), req.shape[0], C.byref(params)))
 
+    def load_model(self, voxels_zyx: np.ndarray) -> int:
+        """A voxel model given as a (sz, sy, sx) uint8 array (x-fastest in memory); returns its index."""
+        v = np.ascontiguousarray(voxels_zyx, dtype=np.uint8)
+        sz, sy, sx = v.shape
+        i = C.c_int()
+        check(self.lib.lumrad_load_model(self.h, ptr(v), sx, sy, sz, C.byref(i)))
+        return int(i.value)
+
+    def blockify(self, static_blocks: int, meshes) -> None:
+        """meshes: [(model index, (qx, qy, qz, qw), (sx, sy, sz))] in processing order."""
+        from ._native import MeshTransform
+        n = len(meshes)
+        models = (C.c_int * max(n, 1))(*[int(m[0]) for m in meshes])
+        tr = (MeshTransform * max(n, 1))()
+        for k, (_, q, s) in enumerate(meshes):
+            tr[k].rot[:] = [float(v) for v in q]
+            tr[k].shift[:] = [float(v) for v in s]
+        check(self.lib.lumrad_blockify(self.h, int(static_blocks), models, tr, n))
+
+    def get_world(self) -> np.ndarray:
+        X, Y, Z = self.dims
+        out = np.empty((Z, Y, X), dtype=np.int16)
+        check(self.lib.lumrad_get_world(self.h, ptr(out)))
+        return out
+
+    def get_block_palette(self) -> np.ndarray:
+        """(max_block_types, 16, 16, 16) uint8 indexed [slot, z, y, x]."""
+        out = np.empty((self.max_block_types, 16, 16, 16), dtype=np.uint8)
+        check(self.lib.lumrad_get_block_palette(self.h, ptr(out)))
+        return out
+
     def shift_radiance(self, dx: int, dy: int, dz: int) -> None:
         check(self.lib.lumrad_shift_radiance(self.h, int(dx), int(dy), int(dz)))
 

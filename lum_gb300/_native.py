@@ -38,6 +38,10 @@ class PassParams(C.Structure):
                 ("record_hits", C.c_int)]
 
 
+class MeshTransform(C.Structure):
+    _fields_ = [("rot", C.c_float * 4), ("shift", C.c_float * 3)]
+
+
 class PassStats(C.Structure):
     _fields_ = [("probes", C.c_uint64), ("rays", C.c_uint64), ("steps", C.c_uint64),
                 ("hits", C.c_uint64), ("gpu_ms", C.c_float)]
@@ -99,6 +103,10 @@ _SIGS = {
     "lumrad_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "lumrad_get_kernel_times": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
     "lumrad_direction_table": (C.c_int, [C.c_int, _P]),
+    "lumrad_load_model": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "lumrad_blockify": (C.c_int, [_P, C.c_int, _P, _P, C.c_int]),
+    "lumrad_get_world": (C.c_int, [_P, _P]),
+    "lumrad_get_block_palette": (C.c_int, [_P, _P]),
     "lumrad_shift_radiance": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
     "lumrad_set_radiance_shift": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
     "lumrad_get_radiance_shift": (C.c_int, [_P, _P]),

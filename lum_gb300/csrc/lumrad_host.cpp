@@ -83,6 +83,8 @@ int DeviceWorld::init(int X_, int Y_, int Z_, int slots, int precision_, cudaStr
 }
 
 void DeviceWorld::release() {
+    cudaFree(d_slot_of);
+    d_slot_of = nullptr;
     cudaFree(d_grid); cudaFree(d_cgrid); cudaFree(d_cbits); cudaFree(d_pal); cudaFree(d_mats);
     cudaFree(d_rad[0]); cudaFree(d_rad[1]); cudaFree(d_scratch); cudaFree(d_probe_count); cudaFree(d_stats);
     cudaFree(d_hits);
@@ -96,7 +98,7 @@ void DeviceWorld::release() {
 // slot is absent shares one all-empty compact id) and builds each compact id's occupancy mask
 // from the palette as uploaded.  Ids that appear later (edits) get the next free compact id
 // through compact_of.
-void DeviceWorld::build_compact() {
+void DeviceWorld::build_compact(const int16_t* g) {
     id_to_c.assign(65536, -1);
     reps.clear();
     empty_c = -1;
@@ -109,12 +111,12 @@ void DeviceWorld::build_compact() {
     cgrid_wide = false;
     bool assigned = false;
     for (size_t i = 0; i < W; i++) {
-        if (id_to_c[(uint16_t)h_grid[i]] >= 0) continue;
-        if (compact_of(h_grid[i], &assigned) < 0) cgrid_wide = true;   // > 256 ids: uint16
+        if (id_to_c[(uint16_t)g[i]] >= 0) continue;
+        if (compact_of(g[i], &assigned) < 0) cgrid_wide = true;   // > 256 ids: uint16
     }
     h_cgrid.resize(W * (cgrid_wide ? 2 : 1));
     for (size_t i = 0; i < W; i++) {
-        const int32_t c = id_to_c[(uint16_t)h_grid[i]];
+        const int32_t c = id_to_c[(uint16_t)g[i]];
         if (cgrid_wide) reinterpret_cast<uint16_t*>(h_cgrid.data())[i] = (uint16_t)c;
         else h_cgrid[i] = (uint8_t)c;
     }
@@ -153,6 +155,11 @@ size_t DeviceWorld::footprint() const {
 }
 
 int DeviceWorld::sync_inputs(cudaStream_t stream) {
+    // a changed origin world or palette replaces the blockified frame (the next blockify rebuilds it)
+    if (!h_cur.empty() && (grid_dirty || compact_dirty)) {
+        h_cur.clear();
+        grid_dirty = true;
+    }
     if (grid_dirty) {
         LUMRAD_TRY(cudaMemcpyAsync(d_grid, h_grid.data(), W * sizeof(int16_t), cudaMemcpyHostToDevice, stream));
         grid_dirty = false;
@@ -465,6 +472,8 @@ void Context::release() {
     cudaFree(d_list_count);
     if (h_list_count) cudaFreeHost(h_list_count);
     cudaFree(d_gather);
+    for (auto& m : models) cudaFree(m.d_vox);
+    models.clear();
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_end) cudaEventDestroy(ev_end);
     if (ev_req) cudaEventDestroy(ev_req);

@@ -112,6 +112,22 @@ cudaError_t launch_shift_radiance(const void* src, void* dst, int X, int Y, int 
 cudaError_t launch_gather(const void* rad, int X, int Y, int Z, int precision, const float* pts, int n, float* out,
                           cudaStream_t stream);
 
+// One mesh of map.comp: column-major inverse transform (float), the dispatch origin in world
+// voxels (pco.shift) and the dispatch size in voxels (a multiple of 4 per axis).
+struct MapArgs {
+    float inv[16];
+    int shift[3];
+    int dims[3];
+};
+// exec_copies' static-to-temporary block copies: (src slot, dst slot) pairs.
+cudaError_t launch_palette_copies(uint8_t* pal, const int2* copies, int n, cudaStream_t stream);
+// map.comp for one mesh (model voxels x-fastest, mx*my*mz bytes) into the palette.
+cudaError_t launch_map(const int16_t* grid, int X, int Y, int Z, uint8_t* pal, int n_slots, int static_blocks,
+                       const uint8_t* model, int mx, int my, int mz, const MapArgs& a, cudaStream_t stream);
+// Occupancy masks (128 words per compact id) from the device palette; slot_of[c] = -1: empty.
+cudaError_t launch_compact_bits(const uint8_t* pal, const int* slot_of, int n_compact, uint32_t* cbits,
+                                cudaStream_t stream);
+
 // One block edit of a served world: worlds[world].grid[index] = block and its compact id.
 struct EditRecord {
     int world;                   // index into the launch's world table

@@ -67,10 +67,15 @@ struct DeviceWorld {
     size_t hits_cap = 0, hits_n = 0;
     bool hits_recorded = false;
     std::map<int, float4*> d_dirs;
+    // blockify: the frame's grid with temporary blocks (empty when not blockified)
+    std::vector<int16_t> h_cur;
+    int* d_slot_of = nullptr;             // palette slot of each compact id (-1: none)
+    size_t slot_of_cap = 0;
 
     int init(int X, int Y, int Z, int slots, int precision, cudaStream_t stream);
     void release();
-    void build_compact();
+    void build_compact() { build_compact(h_grid.data()); }
+    void build_compact(const int16_t* g);   // compact ids of grid g (W ids)
     // Compact id of block id b, assigning the next free one (and its occupancy mask in h_cbits)
     // if b has none yet; -1 if that needs a wider compact grid (a full rebuild).
     int compact_of(int16_t b, bool* assigned);
@@ -120,6 +125,9 @@ struct Context {
     float last_ms = 0.0f;
     // radiance shift applied before each lumrad_update_radiance (Renderer::stored_radiance_shift)
     int shift[3] = {0, 0, 0};
+    // voxel models for blockify / map (InternalMeshModel::voxels)
+    struct Model { int sx = 0, sy = 0, sz = 0; uint8_t* d_vox = nullptr; };
+    std::vector<Model> models;
     // device update-list builder
     ListScratch list{};
     short4* d_specials = nullptr;

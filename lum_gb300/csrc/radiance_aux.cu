@@ -223,7 +223,95 @@ __global__ void gather_kernel(const typename Store::T* __restrict__ rad, int X, 
     out[3 * (size_t)k + 2] = fdiv(tb, tw);
 }
 
+// exec_copies' block copies (internal_render.cpp:1446-1451): palette slot dst = slot src, one CTA
+// of 256 threads x 16 bytes per copy.
+__global__ void __launch_bounds__(256) palette_copy_kernel(uint8_t* __restrict__ pal, const int2* __restrict__ copies) {
+    const int2 c = copies[blockIdx.x];
+    const uint4* src = reinterpret_cast<const uint4*>(pal + (size_t)c.x * 4096);
+    uint4* dst = reinterpret_cast<uint4*>(pal + (size_t)c.y * 4096);
+    dst[threadIdx.x] = src[threadIdx.x];
+}
+
+// map.comp:33-67 for one mesh.  Invocation g covers world voxel g + 0.5 + shift; the model voxel is
+// inverse_trans * (world_voxel, 1) truncated; a non-zero model voxel is written into the
+// temporary block (id >= static_blocks) that holds the world voxel.  Truncation maps world voxels
+// in (-1, 0) and [-15, -1] of an axis onto block 0 (the reference races there); invocations with a
+// negative world coordinate run in the first launch and the others in the second, so the
+// non-negative ones win.
+__global__ void map_kernel(const int16_t* __restrict__ grid, int X, int Y, int Z, uint8_t* __restrict__ pal,
+                           int n_slots, int static_blocks, const uint8_t* __restrict__ model, int mx, int my, int mz,
+                           MapArgs a, int negative_pass) {
+    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int gz = blockIdx.z * blockDim.z + threadIdx.z;
+    if (gx >= a.dims[0] || gy >= a.dims[1] || gz >= a.dims[2]) return;
+    // world_voxel = vec3(g) / 1.0 + vec3(0.5) + vec3(shift)   (:37-40)
+    const float wx = fadd(fadd((float)gx, 0.5f), (float)a.shift[0]);
+    const float wy = fadd(fadd((float)gy, 0.5f), (float)a.shift[1]);
+    const float wz = fadd(fadd((float)gz, 0.5f), (float)a.shift[2]);
+    const int neg = (wx < 0.0f || wy < 0.0f || wz < 0.0f) ? 1 : 0;
+    if (neg != negative_pass) return;
+    const int ix = f2i(wx), iy = f2i(wy), iz = f2i(wz);   // (:41)
+    // model_voxel = (inverse_trans * vec4(world_voxel, 1)).xyz, column by column   (:47-48)
+    const float* m = a.inv;   // column-major m[4*col + row]
+    const float vx = fadd(fadd(fadd(fmul(m[0], wx), fmul(m[4], wy)), fmul(m[8], wz)), m[12]);
+    const float vy = fadd(fadd(fadd(fmul(m[1], wx), fmul(m[5], wy)), fmul(m[9], wz)), m[13]);
+    const float vz = fadd(fadd(fadd(fmul(m[2], wx), fmul(m[6], wy)), fmul(m[10], wz)), m[14]);
+    const int px = f2i(vx), py = f2i(vy), pz = f2i(vz);
+    // target block = iworld / 16 (OpSDiv); out of range reads block 0   (:50-52)
+    const int bx = ix / 16, by = iy / 16, bz = iz / 16;
+    int id = 0;
+    if (bx >= 0 && by >= 0 && bz >= 0 && bx < X && by < Y && bz < Z)
+        id = grid[(size_t)bx + (size_t)X * ((size_t)by + (size_t)Y * bz)];
+    if (id < static_blocks) return;   // (:59)
+    int v = 0;
+    if (px >= 0 && py >= 0 && pz >= 0 && px < mx && py < my && pz < mz)
+        v = model[(size_t)px + (size_t)mx * ((size_t)py + (size_t)my * pz)];   // (:60)
+    if (v == 0 || id >= n_slots) return;   // the palette image ends at its last slot
+    pal[((size_t)id << 12) | (smod(iz, 16) << 8) | (smod(iy, 16) << 4) | smod(ix, 16)] = (uint8_t)v;   // (:54,62)
+}
+
+// Occupancy masks of compact ids from the device palette: CTA c, thread w -> word w of id c.
+__global__ void __launch_bounds__(128) compact_bits_kernel(const uint8_t* __restrict__ pal, const int* __restrict__ slot_of,
+                                                           uint32_t* __restrict__ cbits) {
+    const int c = blockIdx.x, w = threadIdx.x;
+    const int slot = slot_of[c];
+    uint32_t bits = 0;
+    if (slot >= 0) {
+        const uint4* p = reinterpret_cast<const uint4*>(pal + (size_t)slot * 4096 + 32 * w);
+        const uint4 a = p[0], b = p[1];
+        const uint32_t words[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+            if ((words[k >> 2] >> (8 * (k & 3))) & 0xffu) bits |= 1u << k;
+    }
+    cbits[(size_t)c * 128 + w] = bits;
+}
+
 }  // namespace
+
+cudaError_t launch_palette_copies(uint8_t* pal, const int2* copies, int n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    palette_copy_kernel<<<n, 256, 0, stream>>>(pal, copies);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_map(const int16_t* grid, int X, int Y, int Z, uint8_t* pal, int n_slots, int static_blocks,
+                       const uint8_t* model, int mx, int my, int mz, const MapArgs& a, cudaStream_t stream) {
+    if (a.dims[0] <= 0 || a.dims[1] <= 0 || a.dims[2] <= 0) return cudaSuccess;
+    const dim3 block(4, 4, 4);   // local_size 4x4x4 (:32)
+    const dim3 grid_dim((a.dims[0] + 3) / 4, (a.dims[1] + 3) / 4, (a.dims[2] + 3) / 4);
+    for (int pass = 1; pass >= 0; pass--)
+        map_kernel<<<grid_dim, block, 0, stream>>>(grid, X, Y, Z, pal, n_slots, static_blocks, model, mx, my, mz, a, pass);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_bits(const uint8_t* pal, const int* slot_of, int n_compact, uint32_t* cbits,
+                                cudaStream_t stream) {
+    if (n_compact <= 0) return cudaSuccess;
+    compact_bits_kernel<<<n_compact, 128, 0, stream>>>(pal, slot_of, cbits);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_update_list(const int16_t* grid, int X, int Y, int Z, const short4* specials, int n_specials,
                                const ListScratch& s, short4* out, int* count, cudaStream_t stream) {

@@ -69,6 +69,7 @@ def load() -> C.CDLL:
     lib.oracle_update_list.argtypes = [P, P, C.c_int, P, C.c_int, P]
     lib.oracle_shift.argtypes = [C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int]
     lib.oracle_gather.argtypes = [C.c_int, C.c_int, C.c_int, P, P, C.c_int, P]
+    lib.oracle_blockify.argtypes = [C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, C.c_int]
     lib.oracle_max_threads.restype = C.c_int
     _lib = lib
     return lib
@@ -177,6 +178,27 @@ def gather(volume: np.ndarray, points: np.ndarray) -> np.ndarray:
     Z, Y, X, _ = v.shape
     load().oracle_gather(X, Y, Z, v.ctypes.data, p.ctypes.data, p.shape[0], out.ctypes.data)
     return out
+
+
+def blockify(grid: np.ndarray, palette: np.ndarray, static_blocks: int, models, meshes):
+    """One frame of blockify + exec_copies + map (internal_render.cpp:977-1070,1375-1520, map.comp).
+    grid (Z,Y,X) int16, palette (n_slots,16,16,16) uint8 [slot,z,y,x], models: list of (sz,sy,sx)
+    uint8 arrays, meshes: [(model, quat xyzw, shift xyz)].  Returns (grid, palette) or None when
+    the temporary slots run out."""
+    g = np.ascontiguousarray(grid, dtype=np.int16).copy()
+    p = np.ascontiguousarray(palette, dtype=np.uint8).copy()
+    Z, Y, X = g.shape
+    n = len(meshes)
+    arrs = [np.ascontiguousarray(models[m[0]], dtype=np.uint8) for m in meshes]
+    ptrs = (C.c_void_p * max(n, 1))(*[a.ctypes.data for a in arrs])
+    msize = np.array([[a.shape[2], a.shape[1], a.shape[0]] for a in arrs] or [[1, 1, 1]], dtype=np.int32)
+    rot = np.array([m[1] for m in meshes] or [[0, 0, 0, 1]], dtype=np.float32)
+    sh = np.array([m[2] for m in meshes] or [[0, 0, 0]], dtype=np.float32)
+    rc = load().oracle_blockify(X, Y, Z, g.ctypes.data, p.ctypes.data, p.shape[0], int(static_blocks), ptrs,
+                                msize.ctypes.data, rot.ctypes.data, sh.ctypes.data, n)
+    if rc == -2:
+        return None
+    return g, p
 
 
 def max_threads() -> int:

@@ -21,6 +21,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
+#include <limits>
+#include <utility>
 #include <cstring>
 #include <vector>
 #include <algorithm>
@@ -582,6 +584,115 @@ int oracle_gather(int X, int Y, int Z, const float* vol, const float* pts, int n
         out[3 * (size_t)k] = tc.x / tw;   // (:89)
         out[3 * (size_t)k + 1] = tc.y / tw;
         out[3 * (size_t)k + 2] = tc.z / tw;
+    }
+    return 0;
+}
+
+// One frame of the model producers: start_blockify / blockify_mesh (internal_render.cpp:977-1070),
+// exec_copies' palette part (:1375-1451) and map_mesh + shaders/map.comp (:1484-1520, map.comp:33-67).
+// grid: W ids, updated in place to the blockified world; pal: n_slots*4096 voxels, updated in place.
+// models: voxel arrays x-fastest with sizes msize[3*i..]; rot: 4 floats (x,y,z,w) and shift: 3 floats
+// per mesh.  Returns -2 when the temporary slots run past n_slots (nothing changed), 0 otherwise.
+// Definitions where the reference is undefined: a negative static id gets an empty temporary block;
+// map invocations with a negative world coordinate (which truncation aliases into block 0) write
+// before all others; meshes in order; glm's inverse of [R|s] is [R^T | -R^T s] in double.
+int oracle_blockify(int X, int Y, int Z, int16_t* grid, uint8_t* pal, int n_slots, int static_blocks,
+                    const uint8_t* const* models, const int* msize, const float* rot, const float* shift, int n) {
+    struct Box { float mn[3], mx[3]; };
+    auto rotation = [](const float* q, float r[3][3]) {   // glm::mat3_cast, r[col][row]
+        const float x = q[0], y = q[1], z = q[2], w = q[3];
+        r[0][0] = 1.0f - 2.0f * (y * y + z * z); r[0][1] = 2.0f * (x * y + w * z); r[0][2] = 2.0f * (x * z - w * y);
+        r[1][0] = 2.0f * (x * y - w * z); r[1][1] = 1.0f - 2.0f * (x * x + z * z); r[1][2] = 2.0f * (y * z + w * x);
+        r[2][0] = 2.0f * (x * z + w * y); r[2][1] = 2.0f * (y * z - w * x); r[2][2] = 1.0f - 2.0f * (x * x + y * y);
+    };
+    auto aabb = [](const float r[3][3], const float* t, const int* size) {   // get_shift (:988-1012)
+        const float b[3] = {(float)(size[0] - 1), (float)(size[1] - 1), (float)(size[2] - 1)};
+        Box box;
+        for (int a = 0; a < 3; a++) { box.mn[a] = std::numeric_limits<float>::max(); box.mx[a] = std::numeric_limits<float>::lowest(); }
+        for (int k = 0; k < 8; k++) {
+            // the corner order of get_shift: 0, y, yz, z, x, xy, xyz, xz
+            static const int sel[8][3] = {{0,0,0},{0,1,0},{0,1,1},{0,0,1},{1,0,0},{1,1,0},{1,1,1},{1,0,1}};
+            const float c[3] = {sel[k][0] ? b[0] : 0.0f, sel[k][1] ? b[1] : 0.0f, sel[k][2] ? b[2] : 0.0f};
+            for (int a = 0; a < 3; a++) {
+                // glm dmat4 * dvec4: (m0*v0 + m1*v1) + (m2*v2 + m3*v3), in double
+                const double p = ((double)r[0][a] * (double)c[0] + (double)r[1][a] * (double)c[1]) +
+                                 ((double)r[2][a] * (double)c[2] + (double)t[a] * 1.0);
+                const float f = (float)p;
+                box.mn[a] = gmin(box.mn[a], f);
+                box.mx[a] = gmax(box.mx[a], f);
+            }
+        }
+        return box;
+    };
+    const size_t W = (size_t)X * Y * Z;
+    std::vector<int16_t> cur(grid, grid + W);
+    std::vector<std::pair<int, int>> copies;
+    int counter = static_blocks;
+    const int ws[3] = {X, Y, Z};
+    for (int i = 0; i < n; i++) {
+        float r[3][3];
+        rotation(rot + 4 * i, r);
+        const Box box = aabb(r, shift + 3 * i, msize + 3 * i);
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(std::max(((int)box.mn[a] - 1) / 16, 0), ws[a] - 1);
+            hi[a] = std::min(std::max(((int)box.mx[a] + 1) / 16, 0), ws[a] - 1);
+        }
+        for (int z = lo[2]; z <= hi[2]; z++)
+            for (int y = lo[1]; y <= hi[1]; y++)
+                for (int x = lo[0]; x <= hi[0]; x++) {
+                    int16_t& b = cur[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * z)];
+                    if (b < static_blocks) {
+                        if (counter >= n_slots || counter > 32767) return -2;
+                        if (b > 0) copies.push_back({b, counter});
+                        b = (int16_t)counter++;
+                    }
+                }
+    }
+    std::memcpy(grid, cur.data(), W * sizeof(int16_t));
+    std::memset(pal + (size_t)static_blocks * 4096, 0, (size_t)(n_slots - static_blocks) * 4096);
+    for (auto& cp : copies) std::memcpy(pal + (size_t)cp.second * 4096, pal + (size_t)cp.first * 4096, 4096);
+    for (int i = 0; i < n; i++) {
+        float r[3][3];
+        rotation(rot + 4 * i, r);
+        const float* t = shift + 3 * i;
+        const int* size = msize + 3 * i;
+        const Box box = aabb(r, t, size);
+        int org[3], dims[3];
+        for (int a = 0; a < 3; a++) {
+            org[a] = (int)std::floor(box.mn[a]);
+            dims[a] = ((int)std::ceil(box.mx[a]) - org[a] + 3) / 4 * 4;
+        }
+        float inv[3][4];   // rows of [R^T | -R^T t]
+        for (int row = 0; row < 3; row++) {
+            for (int col = 0; col < 3; col++) inv[row][col] = r[row][col];
+            inv[row][3] = (float)(-(((double)r[row][0] * t[0] + (double)r[row][1] * t[1]) + (double)r[row][2] * t[2]));
+        }
+        for (int negative_pass = 1; negative_pass >= 0; negative_pass--)
+            for (int gz = 0; gz < dims[2]; gz++)
+                for (int gy = 0; gy < dims[1]; gy++)
+                    for (int gx = 0; gx < dims[0]; gx++) {
+                        const float wv[3] = {((float)gx + 0.5f) + (float)org[0], ((float)gy + 0.5f) + (float)org[1],
+                                             ((float)gz + 0.5f) + (float)org[2]};
+                        const bool neg = wv[0] < 0.0f || wv[1] < 0.0f || wv[2] < 0.0f;
+                        if ((neg ? 1 : 0) != negative_pass) continue;
+                        int iw[3], im[3];
+                        for (int a = 0; a < 3; a++) {
+                            iw[a] = f2i(wv[a]);
+                            const float mv = ((inv[a][0] * wv[0] + inv[a][1] * wv[1]) + inv[a][2] * wv[2]) + inv[a][3];
+                            im[a] = f2i(mv);
+                        }
+                        const int bx = iw[0] / 16, by = iw[1] / 16, bz = iw[2] / 16;
+                        int id = 0;
+                        if (bx >= 0 && by >= 0 && bz >= 0 && bx < X && by < Y && bz < Z)
+                            id = cur[(size_t)bx + (size_t)X * ((size_t)by + (size_t)Y * bz)];
+                        if (id < static_blocks) continue;
+                        int v = 0;
+                        if (im[0] >= 0 && im[1] >= 0 && im[2] >= 0 && im[0] < size[0] && im[1] < size[1] && im[2] < size[2])
+                            v = models[i][(size_t)im[0] + (size_t)size[0] * ((size_t)im[1] + (size_t)size[1] * im[2])];
+                        if (v == 0 || id >= n_slots) continue;
+                        pal[(size_t)id * 4096 + smod(iw[0], 16) + 16 * smod(iw[1], 16) + 256 * smod(iw[2], 16)] = (uint8_t)v;
+                    }
     }
     return 0;
 }

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from lum_gb300 import worldgen
-from tests.helpers import random_prev
+from tests.helpers import RTOL, random_prev, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -118,3 +118,71 @@ def test_gather_matches_oracle(precision):
         got = rw.gather(pts)
         ref = oracle.gather(rw.get_radiance(), pts)
     assert got.tobytes() == ref.tobytes()
+
+
+def _quat(seed):
+    q = np.random.default_rng(seed).normal(size=4)
+    return tuple((q / np.linalg.norm(q)).astype(np.float32))
+
+
+def _models():
+    rng = np.random.default_rng(21)
+    a = (rng.random((12, 9, 14)) < 0.6) * rng.integers(1, 256, (12, 9, 14))
+    b = (rng.random((5, 20, 7)) < 0.8) * rng.integers(1, 256, (5, 20, 7))
+    return [a.astype(np.uint8), b.astype(np.uint8)]
+
+
+def test_blockify_matches_oracle():
+    """Blockified grid and palette bit for bit, then a pass over the blockified world equals the
+    oracle's pass on the oracle's blockified world."""
+    import lum_gb300
+    import oracle
+    w = worldgen.terrain_world((8, 7, 6), seed=12, n_types=20)
+    models = _models()
+    meshes = [(0, _quat(1), (20.3, 17.9, 30.2)),
+              (1, _quat(2), (64.0, 40.5, 9.0)),
+              (0, (0.0, 0.0, 0.0, 1.0), (-6.5, 3.0, -2.0)),   # partly below the world: aliasing into block 0
+              (1, _quat(3), (25.0, 30.0, 20.0))]              # overlaps the first mesh
+    static = w.palette.shape[0]
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=200) as rw:
+        rw.load(w)
+        ids = [rw.load_model(m) for m in models]
+        assert ids == [0, 1]
+        rw.blockify(static, meshes)
+        got_g, got_p = rw.get_world(), rw.get_block_palette()
+        pal = np.zeros((200, 16, 16, 16), np.uint8)
+        pal[:static] = w.palette
+        ref_g, ref_p = oracle.blockify(w.grid, pal, static, models, meshes)
+        assert np.array_equal(got_g, ref_g)
+        assert np.array_equal(got_p, ref_p)
+        assert got_g.max() > static   # temporary blocks were made
+        # a pass over the blockified world
+        req = worldgen.all_probes(w.dims)
+        prev = random_prev(w)
+        rw.set_radiance(prev)
+        p = lum_gb300.pass_params(rays=64, max_dist=128.0, blend=0.1, time_seed=3, record_hits=True)
+        rw.radiance_pass(req, p)
+        got = rw.get_radiance()
+        hits = rw.get_hits()
+        wb = worldgen.World(grid=ref_g, palette=ref_p, materials=w.materials)
+        ref, ref_hits, _ = oracle.radiance_pass(wb, req, rays=64, max_dist=128.0, blend=0.1, time_seed=3, prev=prev,
+                                                record_hits=True)
+        assert hits.tobytes() == ref_hits.tobytes()
+        assert rel_err(got, ref).max() <= RTOL
+        # the next frame starts from the origin world again
+        rw.blockify(static, [])
+        assert np.array_equal(rw.get_world(), w.grid)
+        pal2 = rw.get_block_palette()
+        assert np.array_equal(pal2[:static], w.palette) and not pal2[static:].any()
+
+
+def test_blockify_out_of_slots_leaves_the_world():
+    import lum_gb300
+    w = worldgen.terrain_world((6, 6, 4), seed=13, n_types=8)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=12) as rw:
+        rw.load(w)
+        m = rw.load_model(np.ones((40, 40, 40), np.uint8))
+        with pytest.raises(lum_gb300.LumRadError) as ei:
+            rw.blockify(9, [(m, (0.0, 0.0, 0.0, 1.0), (1.0, 1.0, 1.0))])
+        assert ei.value.code == lum_gb300._native.LUMRAD_ENOMEM
+        assert np.array_equal(rw.get_world(), w.grid)

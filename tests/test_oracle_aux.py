@@ -78,3 +78,35 @@ def test_gather_closed_forms():
     # (index clamped to world_size) every probe reads 0
     far = np.array([[-500, -500, -500, 0, 1, 0], [5000, 5000, 5000, 1, 0, 0]], dtype=np.float32)
     assert np.array_equal(oracle.gather(vol, far), np.array([[2, 2, 2], [0, 0, 0]], np.float32))
+
+
+def test_blockify_identity_places_the_model():
+    """A solid 8^3 model at shift (16,16,16): the 2x2x2 blocks under its AABB get temporary slots
+    2..9 in z-y-x order; block (1,1,1) (id 1) is copied from static slot 1; the model's voxels land
+    in voxels 0..7 of block (1,1,1)'s slot."""
+    grid = np.zeros((4, 4, 4), np.int16)
+    grid[1, 1, 1] = 1
+    pal = np.zeros((16, 16, 16, 16), np.uint8)
+    pal[1] = 3
+    model = np.full((8, 8, 8), 7, np.uint8)
+    g, p = oracle.blockify(grid, pal, 2, [model], [(0, (0, 0, 0, 1), (16, 16, 16))])
+    want = grid.copy()
+    slot = 2
+    for z in range(2):
+        for y in range(2):
+            for x in range(2):
+                want[z, y, x] = slot
+                slot += 1
+    assert np.array_equal(g, want)
+    expect = np.zeros_like(pal)
+    expect[1] = 3
+    expect[9] = 3
+    expect[9, 0:8, 0:8, 0:8] = 7
+    assert np.array_equal(p, expect)
+
+
+def test_blockify_runs_out_of_slots():
+    grid = np.zeros((4, 4, 4), np.int16)
+    pal = np.zeros((5, 16, 16, 16), np.uint8)
+    model = np.ones((20, 20, 20), np.uint8)
+    assert oracle.blockify(grid, pal, 2, [model], [(0, (0, 0, 0, 1), (8, 8, 8))]) is None
