@@ -17,7 +17,9 @@
 // identity, shift * rotate = [R | s] exactly; the AABB of the model's corners through
 // dmat4 * vec4 (pairwise sums (m0*v0 + m1*v1) + (m2*v2 + m3*v3) in double, rounded to float).
 // The inverse of [R | s] is the rigid inverse [R^T | -R^T s] in double rounded to float (glm's
-// general inverse agrees up to the double rounding).
+// general inverse agrees up to the double rounding).  Where several map invocations target one
+// palette voxel (the reference races), the result is as if the invocations ran one after another
+// in linear order (x fastest) and the meshes in order.
 
 #include "lumrad_world.h"
 
@@ -104,6 +106,7 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
     if (int rc = check_unowned(c)) return rc;
     DeviceWorld& w = c->world;
     if (static_blocks < 1 || static_blocks > w.n_slots) return fail(LUMRAD_EINVAL, "static_blocks must be in [1, max_block_types]");
+    if (n_meshes >= (1 << 23)) return fail(LUMRAD_EINVAL, "too many meshes");
     for (int i = 0; i < n_meshes; i++)
         if (models[i] < 0 || models[i] >= (int)c->models.size()) return fail(LUMRAD_EINVAL, "unknown model");
     LUMRAD_TRY(cudaSetDevice(c->device));
@@ -140,6 +143,36 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
                 }
     }
 
+    // map dispatches of every mesh (checked before anything reaches the device)
+    std::vector<MapArgs> margs(n_meshes);
+    for (int i = 0; i < n_meshes; i++) {
+        float r[3][3];
+        quat_to_mat(transforms[i].rot, r);
+        const float* s = transforms[i].shift;
+        const Context::Model& m = c->models[models[i]];
+        const int size[3] = {m.sx, m.sy, m.sz};
+        const Box box = model_aabb(r, s, size);
+        MapArgs& a = margs[i];
+        double invocations = 1.0;
+        for (int k = 0; k < 3; k++) {
+            const int mn = (int)std::floor(box.mn[k]);   // ivec3(floor(min)), ivec3(ceil(max)) (:1500-1501)
+            const int mx = (int)std::ceil(box.mx[k]);
+            a.shift[k] = mn;
+            a.dims[k] = (mx - mn + 3) / 4 * 4;   // (map_area + 3) / 4 groups of 4 (:1512)
+            invocations *= (double)a.dims[k];
+        }
+        if (invocations >= 4294967296.0) return fail(LUMRAD_EINVAL, "a mesh covers more than 2^32 world voxels");
+        // inverse [R^T | -R^T s], column-major
+        for (int col = 0; col < 3; col++)
+            for (int row = 0; row < 3; row++) a.inv[4 * col + row] = r[row][col];
+        for (int row = 0; row < 3; row++) {
+            const double t = ((double)r[row][0] * s[0] + (double)r[row][1] * s[1]) + (double)r[row][2] * s[2];
+            a.inv[12 + row] = (float)(-t);
+            a.inv[4 * row + 3] = 0.0f;
+        }
+        a.inv[15] = 1.0f;
+    }
+
     // exec_copies (device): temporary part of the palette cleared, block copies, world upload
     const size_t tmp_bytes = (size_t)(w.n_slots - static_blocks) * 4096;
     if (tmp_bytes) LUMRAD_TRY(cudaMemsetAsync(w.d_pal + (size_t)static_blocks * 4096, 0, tmp_bytes, c->stream));
@@ -152,33 +185,26 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
     }
     LUMRAD_TRY(cudaMemcpyAsync(w.d_grid, cur.data(), w.W * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream));
 
-    // map (device), mesh by mesh
-    for (int i = 0; i < n_meshes; i++) {
-        float r[3][3];
-        quat_to_mat(transforms[i].rot, r);
-        const float* s = transforms[i].shift;
-        const Context::Model& m = c->models[models[i]];
-        const int size[3] = {m.sx, m.sy, m.sz};
-        const Box box = model_aabb(r, s, size);
-        MapArgs a;
-        for (int k = 0; k < 3; k++) {
-            const int mn = (int)std::floor(box.mn[k]);   // ivec3(floor(min)), ivec3(ceil(max)) (:1500-1501)
-            const int mx = (int)std::ceil(box.mx[k]);
-            a.shift[k] = mn;
-            a.dims[k] = (mx - mn + 3) / 4 * 4;   // (map_area + 3) / 4 groups of 4 (:1512)
+    // map (device), mesh by mesh; writes claimed in the owner words, then resolved
+    const size_t n_tmp = (size_t)(w.n_slots - static_blocks) * 4096;
+    if (n_meshes > 0 && n_tmp > 0) {
+        if (n_tmp > c->map_owner_cap) {
+            LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+            cudaFree(c->d_map_owner);
+            c->d_map_owner = nullptr;
+            c->map_owner_cap = 0;
+            LUMRAD_TRY(cudaMalloc(&c->d_map_owner, n_tmp * sizeof(unsigned long long)));
+            c->map_owner_cap = n_tmp;
         }
-        // inverse [R^T | -R^T s], column-major
-        for (int col = 0; col < 3; col++)
-            for (int row = 0; row < 3; row++) a.inv[4 * col + row] = r[row][col];
-        for (int row = 0; row < 3; row++) {
-            const double t = ((double)r[row][0] * s[0] + (double)r[row][1] * s[1]) + (double)r[row][2] * s[2];
-            a.inv[12 + row] = (float)(-t);
-            a.inv[4 * row + 3] = 0.0f;
-        }
-        a.inv[15] = 1.0f;
-        LUMRAD_TRY(launch_map(w.d_grid, w.X, w.Y, w.Z, w.d_pal, w.n_slots, static_blocks, m.d_vox, m.sx, m.sy, m.sz, a,
-                              c->stream));
+        LUMRAD_TRY(cudaMemsetAsync(c->d_map_owner, 0, n_tmp * sizeof(unsigned long long), c->stream));
     }
+    for (int i = 0; i < n_meshes && n_tmp > 0; i++) {
+        const Context::Model& m = c->models[models[i]];
+        LUMRAD_TRY(launch_map(w.d_grid, w.X, w.Y, w.Z, w.n_slots, static_blocks, m.d_vox, m.sx, m.sy, m.sz, margs[i], i,
+                              c->d_map_owner, c->stream));
+    }
+    if (n_meshes > 0 && n_tmp > 0)
+        LUMRAD_TRY(launch_map_resolve(w.d_pal + (size_t)static_blocks * 4096, c->d_map_owner, n_tmp, c->stream));
 
     // compact world of the blockified grid; occupancy masks from the device palette
     w.build_compact(cur.data());

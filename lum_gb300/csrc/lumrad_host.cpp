@@ -474,6 +474,7 @@ void Context::release() {
     cudaFree(d_gather);
     for (auto& m : models) cudaFree(m.d_vox);
     models.clear();
+    cudaFree(d_map_owner);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_end) cudaEventDestroy(ev_end);
     if (ev_req) cudaEventDestroy(ev_req);

@@ -121,9 +121,13 @@ struct MapArgs {
 };
 // exec_copies' static-to-temporary block copies: (src slot, dst slot) pairs.
 cudaError_t launch_palette_copies(uint8_t* pal, const int2* copies, int n, cudaStream_t stream);
-// map.comp for one mesh (model voxels x-fastest, mx*my*mz bytes) into the palette.
-cudaError_t launch_map(const int16_t* grid, int X, int Y, int Z, uint8_t* pal, int n_slots, int static_blocks,
-                       const uint8_t* model, int mx, int my, int mz, const MapArgs& a, cudaStream_t stream);
+// map.comp for mesh `mesh` (model voxels x-fastest, mx*my*mz bytes): each write is claimed in
+// owner (one 64-bit word per voxel of the palette slots from static_blocks up, zero at the start
+// of a frame); launch_map_resolve then writes the winners into those slots.
+cudaError_t launch_map(const int16_t* grid, int X, int Y, int Z, int n_slots, int static_blocks, const uint8_t* model,
+                       int mx, int my, int mz, const MapArgs& a, int mesh, unsigned long long* owner,
+                       cudaStream_t stream);
+cudaError_t launch_map_resolve(uint8_t* pal_tmp, const unsigned long long* owner, size_t n, cudaStream_t stream);
 // Occupancy masks (128 words per compact id) from the device palette; slot_of[c] = -1: empty.
 cudaError_t launch_compact_bits(const uint8_t* pal, const int* slot_of, int n_compact, uint32_t* cbits,
                                 cudaStream_t stream);

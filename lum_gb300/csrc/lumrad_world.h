@@ -128,6 +128,8 @@ struct Context {
     // voxel models for blockify / map (InternalMeshModel::voxels)
     struct Model { int sx = 0, sy = 0, sz = 0; uint8_t* d_vox = nullptr; };
     std::vector<Model> models;
+    unsigned long long* d_map_owner = nullptr;   // one word per voxel of the temporary palette slots
+    size_t map_owner_cap = 0;
     // device update-list builder
     ListScratch list{};
     short4* d_specials = nullptr;

@@ -233,14 +233,16 @@ __global__ void __launch_bounds__(256) palette_copy_kernel(uint8_t* __restrict__
 }
 
 // map.comp:33-67 for one mesh.  Invocation g covers world voxel g + 0.5 + shift; the model voxel is
-// inverse_trans * (world_voxel, 1) truncated; a non-zero model voxel is written into the
-// temporary block (id >= static_blocks) that holds the world voxel.  Truncation maps world voxels
-// in (-1, 0) and [-15, -1] of an axis onto block 0 (the reference races there); invocations with a
-// negative world coordinate run in the first launch and the others in the second, so the
-// non-negative ones win.
-__global__ void map_kernel(const int16_t* __restrict__ grid, int X, int Y, int Z, uint8_t* __restrict__ pal,
-                           int n_slots, int static_blocks, const uint8_t* __restrict__ model, int mx, int my, int mz,
-                           MapArgs a, int negative_pass) {
+// inverse_trans * (world_voxel, 1) truncated; a non-zero model voxel goes to the temporary block
+// (id >= static_blocks) that holds the world voxel.  Truncation sends world voxels in (-1, 1) to
+// coordinate 0 and those in [-15, -1] onto block 0's far side, so several invocations can target
+// one palette voxel (the reference races there).  Writes are resolved as if the invocations ran
+// one after another in linear order (x fastest) and the meshes in order: each invocation
+// atomicMax-es (mesh, invocation, value) into the target's 64-bit owner word; a resolve pass
+// writes the winning values.
+__global__ void map_kernel(const int16_t* __restrict__ grid, int X, int Y, int Z, int n_slots, int static_blocks,
+                           const uint8_t* __restrict__ model, int mx, int my, int mz, MapArgs a,
+                           unsigned long long* __restrict__ owner, unsigned long long mesh_key) {
     const int gx = blockIdx.x * blockDim.x + threadIdx.x;
     const int gy = blockIdx.y * blockDim.y + threadIdx.y;
     const int gz = blockIdx.z * blockDim.z + threadIdx.z;
@@ -249,10 +251,8 @@ __global__ void map_kernel(const int16_t* __restrict__ grid, int X, int Y, int Z
     const float wx = fadd(fadd((float)gx, 0.5f), (float)a.shift[0]);
     const float wy = fadd(fadd((float)gy, 0.5f), (float)a.shift[1]);
     const float wz = fadd(fadd((float)gz, 0.5f), (float)a.shift[2]);
-    const int neg = (wx < 0.0f || wy < 0.0f || wz < 0.0f) ? 1 : 0;
-    if (neg != negative_pass) return;
     const int ix = f2i(wx), iy = f2i(wy), iz = f2i(wz);   // (:41)
-    // model_voxel = (inverse_trans * vec4(world_voxel, 1)).xyz, column by column   (:47-48)
+    // model_voxel = (inverse_trans * vec4(world_voxel, 1)).xyz, columns summed in order   (:47-48)
     const float* m = a.inv;   // column-major m[4*col + row]
     const float vx = fadd(fadd(fadd(fmul(m[0], wx), fmul(m[4], wy)), fmul(m[8], wz)), m[12]);
     const float vy = fadd(fadd(fadd(fmul(m[1], wx), fmul(m[5], wy)), fmul(m[9], wz)), m[13]);
@@ -263,12 +263,23 @@ __global__ void map_kernel(const int16_t* __restrict__ grid, int X, int Y, int Z
     int id = 0;
     if (bx >= 0 && by >= 0 && bz >= 0 && bx < X && by < Y && bz < Z)
         id = grid[(size_t)bx + (size_t)X * ((size_t)by + (size_t)Y * bz)];
-    if (id < static_blocks) return;   // (:59)
+    if (id < static_blocks || id >= n_slots) return;   // (:59); the palette ends at its last slot
     int v = 0;
     if (px >= 0 && py >= 0 && pz >= 0 && px < mx && py < my && pz < mz)
         v = model[(size_t)px + (size_t)mx * ((size_t)py + (size_t)my * pz)];   // (:60)
-    if (v == 0 || id >= n_slots) return;   // the palette image ends at its last slot
-    pal[((size_t)id << 12) | (smod(iz, 16) << 8) | (smod(iy, 16) << 4) | smod(ix, 16)] = (uint8_t)v;   // (:54,62)
+    if (v == 0) return;
+    const unsigned long long lin =
+        (unsigned long long)gx + (unsigned long long)a.dims[0] * ((unsigned long long)gy + (unsigned long long)a.dims[1] * gz);
+    const size_t t = ((size_t)(id - static_blocks) << 12) | (smod(iz, 16) << 8) | (smod(iy, 16) << 4) | smod(ix, 16);
+    atomicMax(owner + t, mesh_key | (lin << 8) | (unsigned long long)v);   // (:54,62)
+}
+
+__global__ void map_resolve_kernel(uint8_t* __restrict__ pal_tmp, const unsigned long long* __restrict__ owner,
+                                   size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const unsigned long long o = owner[i];
+        if (o) pal_tmp[i] = (uint8_t)(o & 0xffu);
+    }
 }
 
 // Occupancy masks of compact ids from the device palette: CTA c, thread w -> word w of id c.
@@ -296,13 +307,21 @@ cudaError_t launch_palette_copies(uint8_t* pal, const int2* copies, int n, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_map(const int16_t* grid, int X, int Y, int Z, uint8_t* pal, int n_slots, int static_blocks,
-                       const uint8_t* model, int mx, int my, int mz, const MapArgs& a, cudaStream_t stream) {
+cudaError_t launch_map(const int16_t* grid, int X, int Y, int Z, int n_slots, int static_blocks, const uint8_t* model,
+                       int mx, int my, int mz, const MapArgs& a, int mesh, unsigned long long* owner,
+                       cudaStream_t stream) {
     if (a.dims[0] <= 0 || a.dims[1] <= 0 || a.dims[2] <= 0) return cudaSuccess;
     const dim3 block(4, 4, 4);   // local_size 4x4x4 (:32)
     const dim3 grid_dim((a.dims[0] + 3) / 4, (a.dims[1] + 3) / 4, (a.dims[2] + 3) / 4);
-    for (int pass = 1; pass >= 0; pass--)
-        map_kernel<<<grid_dim, block, 0, stream>>>(grid, X, Y, Z, pal, n_slots, static_blocks, model, mx, my, mz, a, pass);
+    map_kernel<<<grid_dim, block, 0, stream>>>(grid, X, Y, Z, n_slots, static_blocks, model, mx, my, mz, a, owner,
+                                               (unsigned long long)(mesh + 1) << 40);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_map_resolve(uint8_t* pal_tmp, const unsigned long long* owner, size_t n, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    map_resolve_kernel<<<blocks, 256, 0, stream>>>(pal_tmp, owner, n);
     return cudaGetLastError();
 }
 

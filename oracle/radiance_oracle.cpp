@@ -594,8 +594,9 @@ int oracle_gather(int X, int Y, int Z, const float* vol, const float* pts, int n
 // models: voxel arrays x-fastest with sizes msize[3*i..]; rot: 4 floats (x,y,z,w) and shift: 3 floats
 // per mesh.  Returns -2 when the temporary slots run past n_slots (nothing changed), 0 otherwise.
 // Definitions where the reference is undefined: a negative static id gets an empty temporary block;
-// map invocations with a negative world coordinate (which truncation aliases into block 0) write
-// before all others; meshes in order; glm's inverse of [R|s] is [R^T | -R^T s] in double.
+// map invocations that target one palette voxel (truncation aliases world voxels near and below 0
+// into block 0) run one after another in linear order, x fastest, and the meshes in order; glm's
+// inverse of [R|s] is [R^T | -R^T s] in double.
 int oracle_blockify(int X, int Y, int Z, int16_t* grid, uint8_t* pal, int n_slots, int static_blocks,
                     const uint8_t* const* models, const int* msize, const float* rot, const float* shift, int n) {
     struct Box { float mn[3], mx[3]; };
@@ -668,14 +669,11 @@ int oracle_blockify(int X, int Y, int Z, int16_t* grid, uint8_t* pal, int n_slot
             for (int col = 0; col < 3; col++) inv[row][col] = r[row][col];
             inv[row][3] = (float)(-(((double)r[row][0] * t[0] + (double)r[row][1] * t[1]) + (double)r[row][2] * t[2]));
         }
-        for (int negative_pass = 1; negative_pass >= 0; negative_pass--)
-            for (int gz = 0; gz < dims[2]; gz++)
+        for (int gz = 0; gz < dims[2]; gz++)
                 for (int gy = 0; gy < dims[1]; gy++)
                     for (int gx = 0; gx < dims[0]; gx++) {
                         const float wv[3] = {((float)gx + 0.5f) + (float)org[0], ((float)gy + 0.5f) + (float)org[1],
                                              ((float)gz + 0.5f) + (float)org[2]};
-                        const bool neg = wv[0] < 0.0f || wv[1] < 0.0f || wv[2] < 0.0f;
-                        if ((neg ? 1 : 0) != negative_pass) continue;
                         int iw[3], im[3];
                         for (int a = 0; a < 3; a++) {
                             iw[a] = f2i(wv[a]);
