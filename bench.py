@@ -387,6 +387,7 @@ def main():
     ap.add_argument("--legs", default="demo,batched,serving",
                     help="comma list of legs: demo (the headline line), batched (the mixed-size batch), "
                          "serving (relight requests)")
+    ap.add_argument("--serve-requests", type=int, default=10000, help="requests per arrival rate (serving leg)")
     args = ap.parse_args()
     legs = set(args.legs.split(","))
     rank, local, world_size, pg = dist_setup(args)
@@ -398,6 +399,16 @@ def main():
     import lum_gb300
 
     torch.cuda.set_device(local)
+    if "demo" not in legs:   # a diagnostics run of other legs only (profiling); not the headline line
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+        out = {"diagnostics": True}
+        if "batched" in legs:
+            out["batched"] = batched_leg(local, max(3, args.steps // 2), args.warmup, flush)
+        if "serving" in legs:
+            out["serving"] = serving_leg(local, n_requests=args.serve_requests)
+        if rank == 0:
+            print(json.dumps(out))
+        return
     world = worldgen.demo_world(SEED)
     lists = pass_lists(world.dims)
     probes_per_step = sum(l.shape[0] for l in lists)
@@ -488,7 +499,7 @@ def main():
         batched = batched_leg(local, max(3, args.steps // 2), args.warmup, flush)
     serving = None
     if "serving" in legs:
-        serving = serving_leg(local)
+        serving = serving_leg(local, n_requests=args.serve_requests)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
