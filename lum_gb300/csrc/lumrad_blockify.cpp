@@ -212,28 +212,17 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
     if (cap > w.cbits_cap) {
         LUMRAD_TRY(cudaStreamSynchronize(c->stream));
         cudaFree(w.d_cbits);
+        cudaFree(w.d_cslot);
         w.d_cbits = nullptr;
+        w.d_cslot = nullptr;
         w.cbits_cap = 0;
         LUMRAD_TRY(cudaMalloc(&w.d_cbits, cap * 128 * sizeof(uint32_t)));
+        LUMRAD_TRY(cudaMalloc(&w.d_cslot, cap * sizeof(int)));
         w.cbits_cap = cap;
     }
-    if ((size_t)w.n_compact > w.slot_of_cap) {
-        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
-        cudaFree(w.d_slot_of);
-        w.d_slot_of = nullptr;
-        w.slot_of_cap = 0;
-        LUMRAD_TRY(cudaMalloc(&w.d_slot_of, cap * sizeof(int)));
-        w.slot_of_cap = cap;
-    }
-    std::vector<int> slot_of(w.n_compact);
-    for (int k = 0; k < w.n_compact; k++) {
-        const int b = w.reps[k];
-        const int slot = b >= 0 ? b : b + 64;
-        slot_of[k] = (b != DeviceWorld::kEmptyRep && b >= -63 && slot < w.n_slots) ? slot : -1;
-    }
-    LUMRAD_TRY(cudaMemcpyAsync(w.d_slot_of, slot_of.data(), slot_of.size() * sizeof(int), cudaMemcpyHostToDevice,
+    LUMRAD_TRY(cudaMemcpyAsync(w.d_cslot, w.h_cslot.data(), w.h_cslot.size() * sizeof(int), cudaMemcpyHostToDevice,
                                c->stream));
-    LUMRAD_TRY(launch_compact_bits(w.d_pal, w.d_slot_of, w.n_compact, w.d_cbits, c->stream));
+    LUMRAD_TRY(launch_compact_bits(w.d_pal, w.d_cslot, w.n_compact, w.d_cbits, c->stream));
     LUMRAD_TRY(cudaMemcpyAsync(w.d_cgrid, w.h_cgrid.data(), w.h_cgrid.size(), cudaMemcpyHostToDevice, c->stream));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));   // host vectors are reused by the next call
     w.h_cur.swap(cur);

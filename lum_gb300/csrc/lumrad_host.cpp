@@ -83,14 +83,12 @@ int DeviceWorld::init(int X_, int Y_, int Z_, int slots, int precision_, cudaStr
 }
 
 void DeviceWorld::release() {
-    cudaFree(d_slot_of);
-    d_slot_of = nullptr;
-    cudaFree(d_grid); cudaFree(d_cgrid); cudaFree(d_cbits); cudaFree(d_pal); cudaFree(d_mats);
+    cudaFree(d_grid); cudaFree(d_cgrid); cudaFree(d_cbits); cudaFree(d_cslot); cudaFree(d_pal); cudaFree(d_mats);
     cudaFree(d_rad[0]); cudaFree(d_rad[1]); cudaFree(d_scratch); cudaFree(d_probe_count); cudaFree(d_stats);
     cudaFree(d_hits);
     for (auto& kv : d_dirs) cudaFree(kv.second);
     d_dirs.clear();
-    d_grid = nullptr; d_cgrid = nullptr; d_cbits = nullptr; d_pal = nullptr; d_mats = nullptr;
+    d_grid = nullptr; d_cgrid = nullptr; d_cbits = nullptr; d_cslot = nullptr; d_pal = nullptr; d_mats = nullptr;
     d_rad[0] = d_rad[1] = nullptr; d_scratch = nullptr; d_probe_count = nullptr; d_stats = nullptr; d_hits = nullptr;
 }
 
@@ -108,6 +106,7 @@ void DeviceWorld::build_compact(const int16_t* g) {
     h_cbits.assign(128, 0u);
     for (int k = 0; k < 4096 && n_slots > 0; k++)   // block 0 reads palette slot 0 like any other id
         if (h_pal_dev[k]) h_cbits[k >> 5] |= 1u << (k & 31);
+    h_cslot.assign(1, n_slots > 0 ? 0 : -1);
     cgrid_wide = false;
     bool assigned = false;
     for (size_t i = 0; i < W; i++) {
@@ -135,6 +134,7 @@ int DeviceWorld::compact_of(int16_t b, bool* assigned) {
     if (!has_slot) empty_c = n_compact;
     c = n_compact++;
     reps.push_back(has_slot ? b : kEmptyRep);
+    h_cslot.push_back(has_slot ? slot : -1);
     h_cbits.resize((size_t)n_compact * 128, 0u);
     if (has_slot) {
         const uint8_t* v = h_pal_dev.data() + (size_t)slot * 4096;
@@ -147,7 +147,7 @@ int DeviceWorld::compact_of(int16_t b, bool* assigned) {
 }
 
 size_t DeviceWorld::footprint() const {
-    size_t b = W * sizeof(int16_t) + W * sizeof(uint16_t) + cbits_cap * 128 * sizeof(uint32_t) + h_pal.size() +
+    size_t b = W * sizeof(int16_t) + W * sizeof(uint16_t) + cbits_cap * (128 * sizeof(uint32_t) + sizeof(int)) + h_pal.size() +
                LUMRAD_MATERIALS * sizeof(float4) + 2 * W * rad_stride + scratch_cap * sizeof(float4) +
                count_cap * sizeof(int) + 2 * sizeof(unsigned long long) + hits_cap * sizeof(LumRadHit);
     for (auto& kv : d_dirs) b += (size_t)kv.first * sizeof(float4);
@@ -172,14 +172,18 @@ int DeviceWorld::sync_inputs(cudaStream_t stream) {
         const size_t cap = std::max<size_t>((size_t)n_compact, (size_t)n_slots + 64);
         if (cap > cbits_cap) {
             cudaFree(d_cbits);
+            cudaFree(d_cslot);
             d_cbits = nullptr;
+            d_cslot = nullptr;
             cbits_cap = 0;
             LUMRAD_TRY(cudaMalloc(&d_cbits, cap * 128 * sizeof(uint32_t)));
+            LUMRAD_TRY(cudaMalloc(&d_cslot, cap * sizeof(int)));
             cbits_cap = cap;
         }
         LUMRAD_TRY(cudaMemcpyAsync(d_cgrid, h_cgrid.data(), h_cgrid.size(), cudaMemcpyHostToDevice, stream));
         LUMRAD_TRY(cudaMemcpyAsync(d_cbits, h_cbits.data(), h_cbits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                                    stream));
+        LUMRAD_TRY(cudaMemcpyAsync(d_cslot, h_cslot.data(), h_cslot.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
         LUMRAD_TRY(cudaStreamSynchronize(stream));   // host vectors may be rebuilt by the next call
         compact_dirty = false;
     }
@@ -267,6 +271,7 @@ int DeviceWorld::fill_pass(const short4* d_req, int n, const LumRadPassParams& p
     w.cgrid_wide = cgrid_wide ? 1 : 0;
     w.cgrid = d_cgrid;
     w.cbits = d_cbits;
+    w.cslot = d_cslot;
     w.grid = d_grid;
     w.pal = d_pal;
     w.n_slots = n_slots;

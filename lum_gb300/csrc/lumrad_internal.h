@@ -26,6 +26,7 @@ struct WorldPass {
     int cgrid_wide;              // 0: uint8 compact ids, 1: uint16
     const void* cgrid;           // X*Y*Z compact ids, x-fastest
     const uint32_t* cbits;       // 128 words per compact id
+    const int* cslot;            // palette slot of each compact id (-1: none), or null: read the grid
     const int16_t* grid;         // X*Y*Z block ids
     const uint8_t* pal;          // n_slots * 4096 voxels, voxel (x,y,z) at x + 16y + 256z
     int n_slots;

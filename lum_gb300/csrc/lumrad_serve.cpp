@@ -322,9 +322,12 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
                 rebuild = true;
                 continue;
             }
-            if (assigned)   // a block id new to this world: upload its occupancy mask
+            if (assigned) {   // a block id new to this world: upload its occupancy mask and slot
                 LUMRAD_TRY(cudaMemcpyAsync(dw.d_cbits + (size_t)c * 128, dw.h_cbits.data() + (size_t)c * 128,
                                            128 * sizeof(uint32_t), cudaMemcpyHostToDevice, sl.stream));
+                LUMRAD_TRY(cudaMemcpyAsync(dw.d_cslot + c, dw.h_cslot.data() + c, sizeof(int), cudaMemcpyHostToDevice,
+                                           sl.stream));
+            }
             sv->erec.push_back(EditRecord{j, (int)idx, (int)ed.block, c});
         }
         if (rebuild) {   // more than 256 distinct ids: rebuild with a uint16 compact grid

@@ -41,6 +41,7 @@ struct DeviceWorld {
     std::vector<LumRadMaterial> h_mats;
     std::vector<uint8_t> h_cgrid;         // compact ids (uint8 or uint16)
     std::vector<uint32_t> h_cbits;
+    std::vector<int> h_cslot;             // palette slot of each compact id (-1: none)
     bool grid_dirty = true;
     bool compact_dirty = true;
     int n_compact = 0;
@@ -53,6 +54,7 @@ struct DeviceWorld {
     int16_t* d_grid = nullptr;
     void* d_cgrid = nullptr;
     uint32_t* d_cbits = nullptr;
+    int* d_cslot = nullptr;               // cbits_cap entries
     size_t cbits_cap = 0;
     uint8_t* d_pal = nullptr;
     float4* d_mats = nullptr;
@@ -69,8 +71,6 @@ struct DeviceWorld {
     std::map<int, float4*> d_dirs;
     // blockify: the frame's grid with temporary blocks (empty when not blockified)
     std::vector<int16_t> h_cur;
-    int* d_slot_of = nullptr;             // palette slot of each compact id (-1: none)
-    size_t slot_of_cap = 0;
 
     int init(int X, int Y, int Z, int slots, int precision, cudaStream_t stream);
     void release();

@@ -251,8 +251,18 @@ __device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchVi
             it++;
         }
         lookups += 1 + it;
-        int blk;
-        const int cur = solid ? voxel_value(w, vx, vy, vz, blk) : 0;
+        int blk = 0;
+        int cur = 0;
+        if (solid) {
+            if (!RECORD && w.cslot) {
+                // the hit block's palette slot through its compact id (one dependent load less
+                // than reading the int16 grid; same slot: a compact id stands for one block id)
+                const int slot = __ldg(w.cslot + cid);
+                cur = slot >= 0 ? __ldg(w.pal + ((slot << 12) | ((vz & 15) << 8) | ((vy & 15) << 4) | (vx & 15))) : 0;
+            } else {
+                cur = voxel_value(w, vx, vy, vz, blk);
+            }
+        }
         const float nx = -fmul((float)stx, fsx), ny = -fmul((float)sty, fsy), nz = -fmul((float)stz, fsz);
         const float fr = fadd(fadd(fmul(fsub(tmx, tdx), fsx), fmul(fsub(tmy, tdy), fsy)), fmul(fsub(tmz, tdz), fsz));
         // material (GetMat :145-157) and sample_radiance (:161-166); /16 == *0.0625 exactly
