@@ -43,7 +43,6 @@ struct Batch {
     long long n_tasks = 0;
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
-    float4* d_ray_od = nullptr;
     uint2* d_ray_res = nullptr;
     size_t ray_cap = 0;
     Tuning tuning;
@@ -92,12 +91,9 @@ int build(Batch* b) {
     b->n_tasks = begin;
     const size_t need = (size_t)std::min<long long>(std::max<long long>(begin, 1), kChunkTasks) * kTaskRays;
     if (need > b->ray_cap) {
-        cudaFree(b->d_ray_od);
         cudaFree(b->d_ray_res);
-        b->d_ray_od = nullptr;
         b->d_ray_res = nullptr;
         b->ray_cap = 0;
-        LUMRAD_TRY(cudaMalloc(&b->d_ray_od, need * 2 * sizeof(float4)));
         LUMRAD_TRY(cudaMalloc(&b->d_ray_res, need * sizeof(uint2)));
         b->ray_cap = need;
     }
@@ -110,7 +106,6 @@ int build(Batch* b) {
         la.n_tasks = b->n_tasks;
         la.queue = b->d_queue;
         la.error = b->d_error;
-        la.ray_od = b->d_ray_od;
         la.ray_res = b->d_ray_res;
         la.guided_div = b->tuning.guided_div;
         la.max_chunk = b->tuning.max_chunk;
@@ -250,7 +245,6 @@ void lumrad_batch_destroy(LumRadBatch batch) {
     }
     cudaFree(b->d_queue);
     cudaFree(b->d_error);
-    cudaFree(b->d_ray_od);
     cudaFree(b->d_ray_res);
     if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->ev_end) cudaEventDestroy(b->ev_end);

@@ -321,14 +321,11 @@ int Context::ensure_rays(long long n_tasks) {
     const size_t need = (size_t)std::min<long long>(std::max<long long>(n_tasks, 1), kChunkTasks) * kTaskRays;
     if (need <= ray_cap) return LUMRAD_OK;
     LUMRAD_TRY(cudaStreamSynchronize(stream));
-    cudaFree(d_ray_od);
     cudaFree(d_ray_res);
     cudaFree(d_ray_blk);
-    d_ray_od = nullptr;
     d_ray_res = nullptr;
     d_ray_blk = nullptr;
     ray_cap = 0;
-    LUMRAD_TRY(cudaMalloc(&d_ray_od, need * 2 * sizeof(float4)));
     LUMRAD_TRY(cudaMalloc(&d_ray_res, need * sizeof(uint2)));
     LUMRAD_TRY(cudaMalloc(&d_ray_blk, need * sizeof(int)));
     ray_cap = need;
@@ -396,7 +393,6 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     la.queue = d_queue;
     la.error = d_error;
     if ((rc = ensure_rays(la.n_tasks))) return rc;
-    la.ray_od = d_ray_od;
     la.ray_res = d_ray_res;
     la.ray_blk = d_ray_blk;
     const int slot = (int)(n_passes % kRing);
@@ -464,7 +460,6 @@ void Context::release() {
     cudaFree(d_req);
     cudaFree(d_queue);
     cudaFree(d_error);
-    cudaFree(d_ray_od);
     cudaFree(d_ray_res);
     cudaFree(d_ray_blk);
     for (auto& kv : resident) cudaFree(kv.second.ptr);

@@ -138,7 +138,6 @@ struct Slot {
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
     int* h_error = nullptr;       // pinned
-    float4* d_ray_od = nullptr;
     uint2* d_ray_res = nullptr;
     bool busy = false;
     std::vector<SRequest> reqs;
@@ -385,7 +384,6 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     la.n_tasks = begin;
     la.queue = sl.d_queue;
     la.error = sl.d_error;
-    la.ray_od = sl.d_ray_od;
     la.ray_res = sl.d_ray_res;
     la.guided_div = sv->tuning.guided_div;
     la.max_chunk = sv->tuning.max_chunk;
@@ -439,7 +437,6 @@ void destroy_server(Server* sv) {
         if (sl.h_error) cudaFreeHost(sl.h_error);
         cudaFree(sl.d_queue);
         cudaFree(sl.d_error);
-        cudaFree(sl.d_ray_od);
         cudaFree(sl.d_ray_res);
         if (sl.ev_done) cudaEventDestroy(sl.ev_done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
@@ -500,10 +497,9 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
             *sl.h_error = 0;
             LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, 2 * sizeof(unsigned long long), sl.stream));
             LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
-            LUMRAD_TRY(cudaMalloc(&sl.d_ray_od, rays * 2 * sizeof(float4)));
             LUMRAD_TRY(cudaMalloc(&sl.d_ray_res, rays * sizeof(uint2)));
             LUMRAD_TRY(cudaStreamSynchronize(sl.stream));
-            sv->fixed += rays * (2 * sizeof(float4) + sizeof(uint2)) + 2 * sizeof(unsigned long long) + sizeof(int);
+            sv->fixed += rays * sizeof(uint2) + 2 * sizeof(unsigned long long) + sizeof(int);
         }
         if (sv->fixed > sv->budget()) return fail(LUMRAD_ENOMEM, "the launch buffers alone exceed the HBM budget");
         return LUMRAD_OK;

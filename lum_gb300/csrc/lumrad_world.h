@@ -106,7 +106,6 @@ struct Context {
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
     // rays of one march/finalize round (up to kChunkTasks * 32 rays)
-    float4* d_ray_od = nullptr;
     uint2* d_ray_res = nullptr;
     int* d_ray_blk = nullptr;
     size_t ray_cap = 0;

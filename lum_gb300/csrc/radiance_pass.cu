@@ -6,19 +6,20 @@
 //   march_kernel     persistent warps take tasks from a queue in guided chunks (large early,
 //                    single tasks at the end).  A warp sets up a task's 32 rays in lock step
 //                    (hash seeds, direction, origin, 1/direction) into one half of a 64-ray ring in
-//                    shared memory and writes them to the round's ray buffer.  Its lanes march
+//                    shared memory.  Its lanes march
 //                    in a flat loop, one coarse step per iteration; a lane whose ray ends writes
 //                    (fraction, info) and takes the next ray in ring order.  A half is set up again
 //                    as soon as its rays are handed out, so lanes never wait for each other.
-//   finalize_kernel  one warp per task, eight consecutive tasks per CTA, in lock step: refine
-//                    DDA, material, trilinear fetch of the previous radiance, shading,
+//   finalize_kernel  one warp per task, eight consecutive tasks per CTA, in lock step: the ray
+//                    set up again (cheaper than a round trip through L2), refine DDA, material,
+//                    trilinear fetch of the previous radiance, shading,
 //                    xor-butterfly sum.  When R/32 divides 8 a probe's subgroups share a CTA and
 //                    their means are summed in order from shared memory; otherwise through
 //                    global scratch and a per-probe counter.
 //
 // Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
-// world (uint8 ids + occupancy bits, L1-resident); the ray buffers between the kernels
-// (40 B per ray) stay in L2.
+// world (uint8 ids + occupancy bits, L1-resident); between the kernels each ray keeps 8 B
+// (coarse fraction, info word), 67 MB for a full round, L2-resident.
 
 #include "radiance_device.cuh"
 
@@ -156,8 +157,6 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             so[slot] = o4;
             sd[slot] = d4;
             si[slot] = make_float4(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z), 0.0f);
-            __stcg(la.ray_od + 2 * ((long long)base + lane), o4);
-            __stcg(la.ray_od + 2 * ((long long)base + lane) + 1, d4);
             if (loaded & kTaskRays) base1 = base; else base0 = base;
             loaded += kTaskRays;
             loaded_now = true;
@@ -268,12 +267,12 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     float3 v = make_float3(0.0f, 0.0f, 0.0f);
     if (valid) {
         const long long idx = (long long)(t - la.chunk_begin) * kTaskRays + lane;
-        const float4 o4 = __ldcg(la.ray_od + 2 * idx), d4 = __ldcg(la.ray_od + 2 * idx + 1);
         const uint2 res = __ldcg(la.ray_res + idx);
         const int blk = RECORD ? __ldcg(la.ray_blk + idx) : 0;
+        float3 o, d;
+        setup_ray(*wp, g, k * kTaskRays + lane, o, d);   // bit-identical to the march's set-up
         uint32_t lookups;
-        float3 L = finalize_ray<Store, RECORD>(*wp, march_view(*wp), make_float3(o4.x, o4.y, o4.z),
-                                               make_float3(d4.x, d4.y, d4.z), __uint_as_float(res.x), res.y, blk,
+        float3 L = finalize_ray<Store, RECORD>(*wp, march_view(*wp), o, d, __uint_as_float(res.x), res.y, blk,
                                                (long long)t_local * kTaskRays + lane, lookups);
         L = butterfly_sum(L);
         v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
@@ -442,14 +441,13 @@ constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 // byte offsets of the parts of the array
 constexpr size_t kNaCgrid = 0;                                                        // uint16 per block
 constexpr size_t kNaCbits = align256(kNaCgrid + 2 * (size_t)kNoAllocMaxBlocks);      // 512 B per compact id
-constexpr size_t kNaRayOd = align256(kNaCbits + (size_t)(LUMRAD_MAX_BLOCK_SLOTS + 2) * 512);
-constexpr size_t kNaRayRes = align256(kNaRayOd + (size_t)kNoAllocRoundTasks * kTaskRays * 2 * sizeof(float4));
+constexpr size_t kNaRayRes = align256(kNaCbits + (size_t)(LUMRAD_MAX_BLOCK_SLOTS + 2) * 512);
 constexpr size_t kNaDirs = align256(kNaRayRes + (size_t)kNoAllocRoundTasks * kTaskRays * sizeof(uint2));
 constexpr size_t kNaQueue = align256(kNaDirs + 256 * sizeof(float4));
 constexpr size_t kNaError = kNaQueue + 2 * sizeof(unsigned long long);
 constexpr size_t kNaStats = align256(kNaError + sizeof(int));
 constexpr size_t kNaBytes = align256(kNaStats + 2 * sizeof(unsigned long long));
-static_assert(kNaBytes <= (9u << 20), "no-allocation scratch must stay under 9 MiB");
+static_assert(kNaBytes <= (5u << 20), "no-allocation scratch must stay under 5 MiB");
 
 }  // namespace
 }  // namespace lumrad
@@ -609,7 +607,6 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     la.n_tasks = n_tasks;
     la.queue = queue;
     la.error = error;
-    la.ray_od = reinterpret_cast<float4*>(base + kNaRayOd);
     la.ray_res = reinterpret_cast<uint2*>(base + kNaRayRes);
     const int blocks = march_grid(false, nd->num_sms);
     la.total_warps = blocks * kWarps;
