@@ -47,6 +47,7 @@ MAX_DIST = 256.0
 BLEND = 0.1
 SEED = 1234
 S_R = 12            # bytes of FP32 RGB radiance per probe
+CHUNK_TASKS = 1 << 18   # 32-ray tasks per march/finalize round of the library
 # DRAM bytes (read + write) of one pass's two kernels in an ncu capture of this workload
 # (march 0.16 + 7.53 MB, finalize 68.60 + 0.84 MB; ncu replays with cold caches)
 NCU_DRAM_BYTES_PER_PASS = 77.13e6
@@ -224,7 +225,7 @@ def batched_leg(local: int, steps: int, warmup: int, flush):
                 "plain_value": plain, "plain_ms_per_step": float(np.mean(pms)),
                 "speedup_vs_plain": batched / plain, "steps": steps,
                 "ray_steps_per_s": st["steps"] / (ms[-1] / 1000.0),
-                "gpu_launches_per_step": 1 + 2 * -(-tasks // 65536)})
+                "gpu_launches_per_step": 1 + 2 * -(-tasks // CHUNK_TASKS)})
     return out
 
 
