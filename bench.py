@@ -49,8 +49,8 @@ SEED = 1234
 S_R = 12            # bytes of FP32 RGB radiance per probe
 CHUNK_TASKS = 1 << 18   # 32-ray tasks per march/finalize round of the library
 # DRAM bytes (read + write) of one pass's two kernels in an ncu capture of this workload
-# (march 0.16 + 7.53 MB, finalize 68.60 + 0.84 MB; ncu replays with cold caches)
-NCU_DRAM_BYTES_PER_PASS = 77.13e6
+# (march 0.16 + 0.00 MB, finalize 14.78 + 0.00 MB; ncu replays with cold caches)
+NCU_DRAM_BYTES_PER_PASS = 14.94e6
 
 
 def pass_lists(dims):
