@@ -493,7 +493,7 @@ def main():
         e2e_s += time.perf_counter() - t0
     e2e_value = job_value(args.steps * rays_per_step, world_size, max_over_ranks(e2e_s, pg, dev))
     h2d = int(sum(l.shape[0] * 8 for l in lists))
-    d2h = int(world.n_blocks * 16)
+    d2h = int(world.n_blocks * 12)   # the volume as packed RGB floats
 
     batched = None
     if "batched" in legs:

@@ -472,6 +472,8 @@ void Context::release() {
     cudaFree(d_list_count);
     if (h_list_count) cudaFreeHost(h_list_count);
     cudaFree(d_gather);
+    cudaFree(d_rgb);
+    if (h_rgb) cudaFreeHost(h_rgb);
     for (auto& m : models) cudaFree(m.d_vox);
     models.clear();
     cudaFree(d_map_owner);
@@ -658,32 +660,15 @@ int lumrad_get_radiance(LumRadContext ctx, float* rgb) {
     if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
     LUMRAD_TRY(cudaSetDevice(c->device));
     DeviceWorld& w = c->world;
-    if (w.precision == LUMRAD_PRECISION_FP32) {
-        std::vector<float4> h(w.W);
-        LUMRAD_TRY(cudaMemcpyAsync(h.data(), w.d_rad[w.cur], w.W * 16, cudaMemcpyDeviceToHost, c->stream));
-        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
-        for (size_t i = 0; i < w.W; i++) {
-            rgb[3 * i] = h[i].x; rgb[3 * i + 1] = h[i].y; rgb[3 * i + 2] = h[i].z;
-        }
-    } else {
-        std::vector<uint16_t> h(w.W * 4);
-        LUMRAD_TRY(cudaMemcpyAsync(h.data(), w.d_rad[w.cur], w.W * 8, cudaMemcpyDeviceToHost, c->stream));
-        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
-        for (size_t i = 0; i < w.W; i++)
-            for (int k = 0; k < 3; k++) {
-                const uint16_t bits = h[4 * i + k];
-                float v;
-                if (w.precision == LUMRAD_PRECISION_FP16) {
-                    __half_raw r;
-                    r.x = bits;
-                    v = __half2float(__half(r));
-                } else {
-                    const uint32_t u = (uint32_t)bits << 16;
-                    std::memcpy(&v, &u, 4);
-                }
-                rgb[3 * i + k] = v;
-            }
+    // packed to RGB floats on the device (FP16/BF16 widened exactly), one copy through pinned memory
+    if (!c->d_rgb) {
+        LUMRAD_TRY(cudaMalloc(&c->d_rgb, w.W * 3 * sizeof(float)));
+        LUMRAD_TRY(cudaMallocHost(&c->h_rgb, w.W * 3 * sizeof(float)));
     }
+    LUMRAD_TRY(launch_pack_rgb(w.d_rad[w.cur], w.precision, (long long)w.W, c->d_rgb, c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(c->h_rgb, c->d_rgb, w.W * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    std::memcpy(rgb, c->h_rgb, w.W * 3 * sizeof(float));
     return c->check_error();
 }
 

@@ -113,6 +113,9 @@ cudaError_t launch_shift_radiance(const void* src, void* dst, int X, int Y, int 
 cudaError_t launch_gather(const void* rad, int X, int Y, int Z, int precision, const float* pts, int n, float* out,
                           cudaStream_t stream);
 
+// The volume rad (W probes, storage `precision`) as W*3 packed floats.
+cudaError_t launch_pack_rgb(const void* rad, int precision, long long W, float* out, cudaStream_t stream);
+
 // One mesh of map.comp: column-major inverse transform (float), the dispatch origin in world
 // voxels (pco.shift) and the dispatch size in voxels (a multiple of 4 per axis).
 struct MapArgs {

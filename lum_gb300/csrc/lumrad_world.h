@@ -135,6 +135,9 @@ struct Context {
     size_t specials_cap = 0;
     int* d_list_count = nullptr;
     int* h_list_count = nullptr;          // pinned
+    // volume read-back: packed RGB on the device, pinned staging on the host
+    float* d_rgb = nullptr;
+    float* h_rgb = nullptr;
     // gather staging (host-buffer calls)
     float* d_gather = nullptr;
     size_t gather_cap = 0;                // points

@@ -299,7 +299,33 @@ __global__ void __launch_bounds__(128) compact_bits_kernel(const uint8_t* __rest
     cbits[(size_t)c * 128 + w] = bits;
 }
 
+// A radiance volume as packed RGB floats (the storage type decoded exactly).
+template <class Store>
+__global__ void pack_rgb_kernel(const typename Store::T* __restrict__ rad, float* __restrict__ out, long long W) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W; i += (long long)gridDim.x * blockDim.x) {
+        const float3 v = Store::load(rad, (int)i);
+        out[3 * i] = v.x;
+        out[3 * i + 1] = v.y;
+        out[3 * i + 2] = v.z;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_pack_rgb(const void* rad, int precision, long long W, float* out, cudaStream_t stream) {
+    const int blocks = (int)std::min<long long>((W + 255) / 256, 152LL * 8);
+    switch (precision) {
+        case LUMRAD_PRECISION_FP16:
+            pack_rgb_kernel<StoreF16><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(rad), out, W);
+            break;
+        case LUMRAD_PRECISION_BF16:
+            pack_rgb_kernel<StoreBF16><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(rad), out, W);
+            break;
+        default:
+            pack_rgb_kernel<StoreF32><<<blocks, 256, 0, stream>>>(static_cast<const float4*>(rad), out, W);
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_palette_copies(uint8_t* pal, const int2* copies, int n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
