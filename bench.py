@@ -281,7 +281,8 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
                 "probe_rays_per_s": rays / span, "requests_per_s": len(lat) / span, "span_s": span,
                 "submitted_late": bool(late)}
 
-    out = {"config": dict(SERVE_WORKLOAD, world_blocks_total=int(sum(w.n_blocks for w in worlds)),
+    out = {"config": dict(SERVE_WORKLOAD, requests_per_rate=n_requests,
+                          world_blocks_total=int(sum(w.n_blocks for w in worlds)),
                           l2="inputs resident; no flush (a serving loop runs warm)")}
     budget = SERVE_WORKLOAD["hbm_budget_gb"] * 1e9
     srv = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=3)
