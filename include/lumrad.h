@@ -338,6 +338,11 @@ double lumrad_server_now(LumRadServer server);
 /* The world's volume after its last completed request (waits for its launch), W*3 floats. */
 int  lumrad_server_get_radiance(LumRadServer server, int world, float* rgb);
 int  lumrad_server_stats(LumRadServer server, LumRadServerStats* out);
+/* The same list built on the device of a context, for its world (the request list of a relight
+ * request made on the GPU: edit mask, separable dilation, scan-order compaction).  Writes up to
+ * cap entries; *n = full length. */
+int  lumrad_build_dirty_list(LumRadContext ctx, const LumRadEdit* edits, int n_edits, int radius, int16_t* out,
+                             int cap, int* n);
 /* Probes within Chebyshev distance radius of the edits of a world of world_size blocks, as
  * (x, y, z, 0) int16 in x-fastest scan order: the request list a relight request runs.  Host
  * only; cap 0 returns the count in *n. */

@@ -123,6 +123,15 @@ class RadianceWorld:
         check(self.lib.lumrad_build_update_list(self.h, ptr(out), n.value, C.byref(n)))
         return out[: n.value]
 
+    def build_dirty_list(self, edits, radius: int = 2) -> np.ndarray:
+        """Probes within `radius` blocks of the edits, derived on the device; (n, 4) int16."""
+        e = _edits(edits)
+        n = C.c_int()
+        out = np.zeros((self.n_blocks, 4), dtype=np.int16)
+        check(self.lib.lumrad_build_dirty_list(self.h, e.ctypes.data if e.size else None, e.size, radius, ptr(out),
+                                               self.n_blocks, C.byref(n)))
+        return out[: n.value]
+
     def request_update(self, x: int, y: int, z: int) -> None:
         check(self.lib.lumrad_request_update(self.h, x, y, z))
 

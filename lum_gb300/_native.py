@@ -136,6 +136,7 @@ _SIGS = {
     "lumrad_server_get_radiance": (C.c_int, [_P, C.c_int, _P]),
     "lumrad_server_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "lumrad_dirty_probes": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, C.POINTER(C.c_int)]),
+    "lumrad_build_dirty_list": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, C.POINTER(C.c_int)]),
 }
 
 _lib = None

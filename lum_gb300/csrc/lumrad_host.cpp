@@ -409,9 +409,7 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     return LUMRAD_OK;
 }
 
-int Context::build_list_device(bool consume, int* n) {
-    int rc = world.sync_inputs(stream);
-    if (rc) return rc;
+int Context::ensure_list_scratch() {
     const long long W = (long long)world.W;
     if (!list.bits) {
         LUMRAD_TRY(cudaMalloc(&list.bits, list_scratch_words(W) * sizeof(uint32_t)));
@@ -421,6 +419,14 @@ int Context::build_list_device(bool consume, int* n) {
         LUMRAD_TRY(cudaMalloc(&d_list_count, sizeof(int)));
         LUMRAD_TRY(cudaMallocHost(&h_list_count, sizeof(int)));
     }
+    return LUMRAD_OK;
+}
+
+int Context::build_list_device(bool consume, int* n) {
+    int rc = world.sync_inputs(stream);
+    if (rc) return rc;
+    const long long W = (long long)world.W;
+    if ((rc = ensure_list_scratch())) return rc;
     const size_t ns = specials.size() / 4;
     if ((rc = ensure_req_capacity((size_t)W + ns))) return rc;
     if (ns > specials_cap) {
@@ -471,6 +477,8 @@ void Context::release() {
     cudaFree(d_specials);
     cudaFree(d_list_count);
     if (h_list_count) cudaFreeHost(h_list_count);
+    cudaFree(d_dirty_mask);
+    cudaFree(d_edits);
     cudaFree(d_gather);
     cudaFree(d_rgb);
     if (h_rgb) cudaFreeHost(h_rgb);
@@ -715,6 +723,44 @@ int lumrad_build_update_list(LumRadContext ctx, int16_t* out, int cap, int* n) {
     int total = 0;
     int rc = c->build_list_device(false, &total);   // building the list alone keeps the queue
     if (rc) return rc;
+    if (cap > 0 && total > 0) {
+        LUMRAD_TRY(cudaMemcpyAsync(out, c->d_req, (size_t)std::min(total, cap) * sizeof(short4), cudaMemcpyDeviceToHost,
+                                   c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    }
+    *n = total;
+    return LUMRAD_OK;
+}
+
+int lumrad_build_dirty_list(LumRadContext ctx, const LumRadEdit* edits, int n_edits, int radius, int16_t* out, int cap,
+                            int* n) {
+    Context* c = as_ctx(ctx);
+    if (!c || !n || n_edits < 0 || (n_edits > 0 && !edits) || (cap > 0 && !out)) return fail(LUMRAD_EINVAL, "bad argument");
+    if (radius < 0 || radius > 15) return fail(LUMRAD_EINVAL, "radius must be in [0, 15]");
+    const DeviceWorld& w = c->world;
+    for (int k = 0; k < n_edits; k++)
+        if (edits[k].x < 0 || edits[k].y < 0 || edits[k].z < 0 || edits[k].x >= w.X || edits[k].y >= w.Y || edits[k].z >= w.Z)
+            return fail(LUMRAD_EINVAL, "edit outside the world");
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    int rc = c->ensure_list_scratch();
+    if (rc) return rc;
+    if ((rc = c->ensure_req_capacity(w.W))) return rc;
+    if (!c->d_dirty_mask) LUMRAD_TRY(cudaMalloc(&c->d_dirty_mask, 2 * w.W));
+    if ((size_t)n_edits > c->edits_cap) {
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+        cudaFree(c->d_edits);
+        c->d_edits = nullptr;
+        c->edits_cap = 0;
+        LUMRAD_TRY(cudaMalloc(&c->d_edits, std::max<size_t>(n_edits, 256) * sizeof(short4)));
+        c->edits_cap = std::max<size_t>(n_edits, 256);
+    }
+    if (n_edits > 0)
+        LUMRAD_TRY(cudaMemcpyAsync(c->d_edits, edits, (size_t)n_edits * sizeof(short4), cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(launch_dirty_list(c->d_edits, n_edits, w.X, w.Y, w.Z, radius, c->d_dirty_mask, c->d_dirty_mask + w.W,
+                                 c->list, c->d_req, c->d_list_count, c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(c->h_list_count, c->d_list_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    const int total = *c->h_list_count;
     if (cap > 0 && total > 0) {
         LUMRAD_TRY(cudaMemcpyAsync(out, c->d_req, (size_t)std::min(total, cap) * sizeof(short4), cudaMemcpyDeviceToHost,
                                    c->stream));

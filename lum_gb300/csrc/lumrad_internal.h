@@ -103,6 +103,13 @@ size_t list_scratch_ctas(long long W);
 cudaError_t launch_update_list(const int16_t* grid, int X, int Y, int Z, const short4* specials, int n_specials,
                                const ListScratch& scratch, short4* out, int* count, cudaStream_t stream);
 
+// Probes within Chebyshev distance `radius` of the edited blocks (edits as (x, y, z, block), all
+// inside the world), in scan order, into out (W entries); *count (device) receives the length.
+// mask_a and mask_b are W bytes of scratch each.
+cudaError_t launch_dirty_list(const short4* edits, int n_edits, int X, int Y, int Z, int radius, uint8_t* mask_a,
+                              uint8_t* mask_b, const ListScratch& scratch, short4* out, int* count,
+                              cudaStream_t stream);
+
 // shift_radiance (internal_render.cpp:1218-1335) from src into dst: dst(p) = src(p + shift)
 // where p + shift is inside the world, src(p) elsewhere.
 cudaError_t launch_shift_radiance(const void* src, void* dst, int X, int Y, int Z, int sx, int sy, int sz,

@@ -135,6 +135,9 @@ struct Context {
     size_t specials_cap = 0;
     int* d_list_count = nullptr;
     int* h_list_count = nullptr;          // pinned
+    uint8_t* d_dirty_mask = nullptr;      // 2 W bytes: the dirty-probe dilation's ping-pong masks
+    short4* d_edits = nullptr;
+    size_t edits_cap = 0;
     // volume read-back: packed RGB on the device, pinned staging on the host
     float* d_rgb = nullptr;
     float* h_rgb = nullptr;
@@ -150,6 +153,7 @@ struct Context {
     // Builds update_radiance's list on the device into d_req; *n = its length.  The queued
     // specials are consumed when `consume` is set.
     int build_list_device(bool consume, int* n);
+    int ensure_list_scratch();
     int shift_volume(int dx, int dy, int dz);
     void release();
 };

@@ -128,6 +128,58 @@ list_write_kernel(const uint32_t* __restrict__ bits, const int* __restrict__ off
     out[pos] = make_short4((short)x, (short)(q % Y), (short)(q / Y), 0);
 }
 
+// Dirty probes of block edits (Chebyshev distance <= r): a byte mask of the edited blocks, dilated
+// along x, then y, then z; the last pass writes one bit per block and the CTA counts, as
+// list_flags_kernel does, so list_scan_kernel and list_write_kernel emit the list in scan order.
+__global__ void dirty_mark_kernel(const short4* __restrict__ edits, int n, int X, int Y, uint8_t* __restrict__ mask) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const short4 e = edits[k];
+    mask[(size_t)e.x + (size_t)X * ((size_t)e.y + (size_t)Y * e.z)] = 1;
+}
+
+// one axis of the dilation: out[i] = OR of in over [-r, r] steps of `stride` along an axis of n
+__global__ void dirty_dilate_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, int X, int Y, int Z,
+                                    int axis, int r, long long W) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < W; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % X);
+        const long long q = i / X;
+        const int y = (int)(q % Y), z = (int)(q / Y);
+        const int c = axis == 0 ? x : (axis == 1 ? y : z);
+        const int n = axis == 0 ? X : (axis == 1 ? Y : Z);
+        const long long stride = axis == 0 ? 1 : (axis == 1 ? (long long)X : (long long)X * Y);
+        uint8_t v = 0;
+        for (int d = max(c - r, 0); d <= min(c + r, n - 1); d++) v |= __ldg(in + i + (long long)(d - c) * stride);
+        out[i] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kListCta)
+dirty_flags_kernel(const uint8_t* __restrict__ in, int X, int Y, int Z, int r, long long W, uint32_t* __restrict__ bits,
+                   int* __restrict__ cta_counts) {
+    __shared__ int s_cnt[kListCta / 32];
+    const long long i = (long long)blockIdx.x * kListCta + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool flag = false;
+    if (i < W) {   // the z pass of the dilation
+        const long long XY = (long long)X * Y;
+        const int z = (int)(i / XY);
+        for (int d = max(z - r, 0); d <= min(z + r, Z - 1) && !flag; d++) flag = __ldg(in + i + (long long)(d - z) * XY) != 0;
+    }
+    const unsigned b = __ballot_sync(kFull, flag);
+    const long long word = i >> 5;
+    if (lane == 0) {
+        if (word < (W + 31) / 32) bits[word] = b;
+        s_cnt[warp] = __popc(b);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int w = 0; w < kListCta / 32; w++) c += s_cnt[w];
+        cta_counts[blockIdx.x] = c;
+    }
+}
+
 // Specials in request order, each unless its block is already listed (duplicates are kept, as
 // in the reference: `set` only marks rule-listed blocks).
 __global__ void __launch_bounds__(kScanCta)
@@ -366,6 +418,22 @@ cudaError_t launch_update_list(const int16_t* grid, int X, int Y, int Z, const s
     list_scan_kernel<<<1, kScanCta, 0, stream>>>(s.cta_counts, ctas, s.cta_offsets, s.listed);
     list_write_kernel<<<ctas, kListCta, 0, stream>>>(s.bits, s.cta_offsets, X, Y, W, out);
     list_specials_kernel<<<1, kScanCta, 0, stream>>>(specials, n_specials, s.bits, X, Y, s.listed, out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dirty_list(const short4* edits, int n_edits, int X, int Y, int Z, int radius, uint8_t* mask_a,
+                              uint8_t* mask_b, const ListScratch& s, short4* out, int* count, cudaStream_t stream) {
+    const long long W = (long long)X * Y * Z;
+    const int ctas = (int)((W + kListCta - 1) / kListCta);
+    const int blocks = (int)std::min<long long>((W + 255) / 256, 152LL * 16);
+    cudaError_t e = cudaMemsetAsync(mask_a, 0, (size_t)W, stream);
+    if (e != cudaSuccess) return e;
+    if (n_edits > 0) dirty_mark_kernel<<<(n_edits + 255) / 256, 256, 0, stream>>>(edits, n_edits, X, Y, mask_a);
+    dirty_dilate_kernel<<<blocks, 256, 0, stream>>>(mask_a, mask_b, X, Y, Z, 0, radius, W);
+    dirty_dilate_kernel<<<blocks, 256, 0, stream>>>(mask_b, mask_a, X, Y, Z, 1, radius, W);
+    dirty_flags_kernel<<<ctas, kListCta, 0, stream>>>(mask_a, X, Y, Z, radius, W, s.bits, s.cta_counts);
+    list_scan_kernel<<<1, kScanCta, 0, stream>>>(s.cta_counts, ctas, s.cta_offsets, count);
+    list_write_kernel<<<ctas, kListCta, 0, stream>>>(s.bits, s.cta_offsets, X, Y, W, out);
     return cudaGetLastError();
 }
 

@@ -186,3 +186,17 @@ def test_blockify_out_of_slots_leaves_the_world():
             rw.blockify(9, [(m, (0.0, 0.0, 0.0, 1.0), (1.0, 1.0, 1.0))])
         assert ei.value.code == lum_gb300._native.LUMRAD_ENOMEM
         assert np.array_equal(rw.get_world(), w.grid)
+
+
+@pytest.mark.parametrize("dims,frac,radius", [((8, 8, 8), 0.002, 2), ((16, 12, 9), 0.05, 2), ((33, 17, 5), 0.03, 1),
+                                              ((64, 64, 32), 0.01, 2), ((7, 5, 3), 0.5, 3), ((20, 20, 20), 0.001, 0)])
+def test_dirty_list_on_device_matches_host(dims, frac, radius):
+    """The device derivation of a relight request's probes equals the host one and numpy's."""
+    import lum_gb300
+    w = worldgen.terrain_world(dims, seed=41, n_types=8)
+    edits = worldgen.edit_request(dims, frac, seed=42, stream=radius)
+    with _rw(w) as rw:
+        got = rw.build_dirty_list(edits, radius)
+        assert np.array_equal(got, lum_gb300.dirty_probes(dims, edits, radius))
+        assert np.array_equal(got, worldgen.dirty_probes(dims, edits, radius))
+        assert rw.build_dirty_list(np.zeros((0, 4), np.int16), radius).shape == (0, 4)
