@@ -5,17 +5,17 @@
 //
 //   march_kernel     persistent warps take tasks from a queue in guided chunks (large early,
 //                    single tasks at the end).  A warp sets up a task's 32 rays in lock step
-//                    (hash seeds, direction, origin, 1/direction) into one half of a 64-ray ring in
-//                    shared memory.  Its lanes march
-//                    in a flat loop, one coarse step per iteration; a lane whose ray ends writes
-//                    (fraction, info) and takes the next ray in ring order.  A half is set up again
-//                    as soon as its rays are handed out, so lanes never wait for each other.
+//                    (hash seeds, direction, origin, 1/direction) into one half of a 64-ray ring
+//                    in shared memory.  Its lanes march in a flat loop, one coarse step per
+//                    iteration; a lane whose ray ends writes (fraction, info) and takes the next
+//                    ray in ring order.  A half is set up again as soon as its rays are handed
+//                    out, so lanes never wait for each other.
 //   finalize_kernel  one warp per task, eight consecutive tasks per CTA, in lock step: the ray
 //                    set up again (cheaper than a round trip through L2), refine DDA, material,
-//                    trilinear fetch of the previous radiance, shading,
-//                    xor-butterfly sum.  When R/32 divides 8 a probe's subgroups share a CTA and
-//                    their means are summed in order from shared memory; otherwise through
-//                    global scratch and a per-probe counter.
+//                    trilinear fetch of the previous radiance, shading, xor-butterfly sum.  When
+//                    R/32 divides 8 a probe's subgroups share a CTA and their means are summed in
+//                    order from shared memory; otherwise through global scratch and a per-probe
+//                    counter.  Lookup and hit counters are summed per CTA.
 //
 // Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
 // world (uint8 ids + occupancy bits, L1-resident); between the kernels each ray keeps 8 B
