@@ -357,9 +357,12 @@ int Context::stage_requests(const int16_t* req, size_t n) {
 
 int Context::check_error() {
     if (!have_pass) return LUMRAD_OK;
-    int e = 0;
-    LUMRAD_TRY(cudaMemcpyAsync(&e, d_error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    LUMRAD_TRY(cudaMemcpyAsync(h_err, d_error, sizeof(int), cudaMemcpyDeviceToHost, stream));
     LUMRAD_TRY(cudaStreamSynchronize(stream));
+    return handle_error(*h_err);
+}
+
+int Context::handle_error(int e) {
     if (e != 0) {
         cudaMemsetAsync(d_error, 0, sizeof(int), stream);
         cudaMemsetAsync(d_queue, 0, 2 * sizeof(unsigned long long), stream);
@@ -396,11 +399,10 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     la.ray_res = d_ray_res;
     la.ray_blk = d_ray_blk;
     const int slot = (int)(n_passes % kRing);
-    LUMRAD_TRY(cudaEventRecord(ev_start, stream));
     LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
     LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream));
     LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
-    LUMRAD_TRY(cudaEventRecord(ev_end, stream));
+    last_slot = slot;
     n_passes++;
     world.cur = 1 - world.cur;
     have_pass = true;
@@ -485,8 +487,7 @@ void Context::release() {
     for (auto& m : models) cudaFree(m.d_vox);
     models.clear();
     cudaFree(d_map_owner);
-    if (ev_start) cudaEventDestroy(ev_start);
-    if (ev_end) cudaEventDestroy(ev_end);
+    if (h_err) cudaFreeHost(h_err);
     if (ev_req) cudaEventDestroy(ev_req);
     for (int i = 0; i < kRing; i++) {
         if (ring0[i]) cudaEventDestroy(ring0[i]);
@@ -542,8 +543,8 @@ int lumrad_create(const LumRadSettings* s, LumRadContext* out) {
         LUMRAD_TRY(cudaSetDevice(c->device));
         LUMRAD_TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device));
         LUMRAD_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-        LUMRAD_TRY(cudaEventCreate(&c->ev_start));
-        LUMRAD_TRY(cudaEventCreate(&c->ev_end));
+        LUMRAD_TRY(cudaMallocHost(&c->h_err, sizeof(int)));
+        *c->h_err = 0;
         LUMRAD_TRY(cudaEventCreateWithFlags(&c->ev_req, cudaEventDisableTiming));
         for (int i = 0; i < Context::kRing; i++) {
             LUMRAD_TRY(cudaEventCreate(&c->ring0[i]));
@@ -675,9 +676,10 @@ int lumrad_get_radiance(LumRadContext ctx, float* rgb) {
     }
     LUMRAD_TRY(launch_pack_rgb(w.d_rad[w.cur], w.precision, (long long)w.W, c->d_rgb, c->stream));
     LUMRAD_TRY(cudaMemcpyAsync(c->h_rgb, c->d_rgb, w.W * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(c->h_err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));   // one wait for the volume and the error word
     std::memcpy(rgb, c->h_rgb, w.W * 3 * sizeof(float));
-    return c->check_error();
+    return c->have_pass ? c->handle_error(*c->h_err) : LUMRAD_OK;
 }
 
 int lumrad_set_radiance(LumRadContext ctx, const float* rgb) {
@@ -777,8 +779,8 @@ int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
     if (rc) return rc;
     LUMRAD_TRY(cudaSetDevice(c->device));
     if (params->size == 0 && c->have_pass) {
-        LUMRAD_TRY(cudaEventSynchronize(c->ev_end));
-        LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ev_start, c->ev_end));
+        LUMRAD_TRY(cudaEventSynchronize(c->ring1[c->last_slot]));
+        LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
     }
     if ((rc = check_unowned(c))) return rc;
     // a frame of Renderer::submitFrame: shift_radiance, then update_radiance (renderer.cpp:436-438)
@@ -916,7 +918,7 @@ int lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out) {
     LUMRAD_TRY(cudaMemcpyAsync(h, c->world.d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     float ms = 0.0f;
-    LUMRAD_TRY(cudaEventElapsedTime(&ms, c->ev_start, c->ev_end));
+    LUMRAD_TRY(cudaEventElapsedTime(&ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
     *out = c->last;
     out->steps = h[0];
     out->hits = h[1];

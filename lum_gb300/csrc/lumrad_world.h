@@ -111,8 +111,10 @@ struct Context {
     size_t ray_cap = 0;
 
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_req = nullptr;
-    cudaEvent_t ring0[kRing] = {}, ring1[kRing] = {};
+    cudaEvent_t ev_req = nullptr;
+    cudaEvent_t ring0[kRing] = {}, ring1[kRing] = {};   // around each pass's kernels
+    int last_slot = 0;                    // ring entry of the last pass
+    int* h_err = nullptr;                 // pinned copy of the error word
     long long n_passes = 0;
     bool have_pass = false;
     bool req_copy_pending = false;
@@ -150,6 +152,7 @@ struct Context {
     int stage_requests(const int16_t* req, size_t n);
     int run_pass(const short4* d_req, int n, const LumRadPassParams* p);
     int check_error();
+    int handle_error(int e);              // resets the launch counters after a reported error
     // Builds update_radiance's list on the device into d_req; *n = its length.  The queued
     // specials are consumed when `consume` is set.
     int build_list_device(bool consume, int* n);
