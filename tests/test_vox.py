@@ -53,7 +53,9 @@ def test_scene_clamps_and_crops(tmp_path):
     assert np.array_equal(out, np.clip(g[:2, :, :4], 0, 15))
 
 
-REF = "/root/reference/assets"
+from oracle import build_ref  # noqa: E402  (where the reference tree is, when it is present)
+
+REF = os.path.join(build_ref.REFERENCE, "assets")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference assets absent")
