@@ -45,6 +45,7 @@ extern "C" {
 #define LUMRAD_EDEVICE  -3  /* CUDA error; the message is kept by lumrad_last_error() */
 #define LUMRAD_ETIMEOUT -4  /* a bounded wait ran out */
 #define LUMRAD_ESTATE   -5  /* call not valid in the current state (e.g. no hits recorded) */
+#define LUMRAD_ECANCELED -6 /* a server request cancelled before it ran */
 
 /* ---- constants (src/renderer/src/internal_types.hpp:13-25) -------------------------------- */
 #define LUMRAD_BLOCK_SIZE          16     /* BLOCK_SIZE */
@@ -284,7 +285,11 @@ int  lumrad_batch_stats(LumRadBatch batch, LumRadPassStats* out);
  * A world's requests run one after another in submission order, so each result is the same
  * whether the request runs alone or among others.  Nothing runs until lumrad_server_progress
  * or lumrad_server_run is called.  A context registered with a server belongs to it until the
- * server is destroyed: read its volume with lumrad_server_get_radiance. */
+ * server is destroyed: read its volume with lumrad_server_get_radiance.
+ * Under the HBM budget the server evicts idle worlds, least recently used first, when a world
+ * or a request does not fit: an evicted world's device buffers are released and its grid,
+ * palette, materials and volume kept on the host; it is uploaded again when a request for it
+ * comes due.  Results do not depend on evictions. */
 typedef void* LumRadServer;
 
 typedef struct {
@@ -301,7 +306,8 @@ typedef struct { int16_t x, y, z, block; } LumRadEdit;
 typedef struct {
     long long request;            /* id given by lumrad_server_submit */
     int    world;
-    int    status;                /* LUMRAD_OK, LUMRAD_ENOMEM (never fits the budget), LUMRAD_EDEVICE */
+    int    status;                /* LUMRAD_OK, LUMRAD_ENOMEM (never fits the budget), LUMRAD_ECANCELED,
+                                     LUMRAD_EDEVICE */
     int    probes;                /* probes relit */
     int    rays_per_probe;
     double arrival_s;             /* server clock (lumrad_server_now) */
@@ -317,6 +323,8 @@ typedef struct {
     double launch_bytes;          /* fixed per-slot buffers */
     double peak_inflight_bytes;   /* largest admitted request bytes on the GPU at once */
     int    max_requests_in_launch;
+    long long evictions;          /* worlds evicted to make room */
+    long long readmissions;       /* evicted worlds uploaded again */
 } LumRadServerStats;
 
 int  lumrad_server_create(const LumRadServerSettings* settings, LumRadServer* out);
@@ -332,6 +340,9 @@ int  lumrad_server_progress(LumRadServer server);
 /* Calls lumrad_server_progress until every queued request has completed, or timeout_s passes
  * (LUMRAD_ETIMEOUT). */
 int  lumrad_server_run(LumRadServer server, double timeout_s);
+/* Cancels a request that has not been launched yet (*cancelled = 1; it completes with
+ * LUMRAD_ECANCELED); a running, finished or unknown request is left alone (*cancelled = 0). */
+int  lumrad_server_cancel(LumRadServer server, long long request, int* cancelled);
 /* Takes up to cap completions (oldest first). */
 int  lumrad_server_poll(LumRadServer server, LumRadCompletion* out, int cap, int* n);
 double lumrad_server_now(LumRadServer server);

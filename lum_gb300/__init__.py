@@ -341,6 +341,12 @@ class RadianceServer:
     def run(self, timeout_s: float = 600.0) -> None:
         check(self.lib.lumrad_server_run(self.h, float(timeout_s)))
 
+    def cancel(self, request: int) -> bool:
+        """Cancels a request not launched yet; True if it was."""
+        out = C.c_int()
+        check(self.lib.lumrad_server_cancel(self.h, int(request), C.byref(out)))
+        return bool(out.value)
+
     def poll(self, cap: int = 65536) -> np.ndarray:
         from ._native import COMPLETION_DTYPE
         out = np.zeros(cap, dtype=COMPLETION_DTYPE)

@@ -19,6 +19,7 @@ LUMRAD_ENOMEM = -2
 LUMRAD_EDEVICE = -3
 LUMRAD_ETIMEOUT = -4
 LUMRAD_ESTATE = -5
+LUMRAD_ECANCELED = -6
 
 PRECISION = {"fp32": 0, "fp16": 1, "bf16": 2}
 
@@ -59,7 +60,8 @@ class ServerSettings(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("requests", C.c_longlong), ("probes", C.c_uint64),
                 ("rays", C.c_uint64), ("resident_bytes", C.c_double), ("launch_bytes", C.c_double),
-                ("peak_inflight_bytes", C.c_double), ("max_requests_in_launch", C.c_int)]
+                ("peak_inflight_bytes", C.c_double), ("max_requests_in_launch", C.c_int),
+                ("evictions", C.c_longlong), ("readmissions", C.c_longlong)]
 
 
 # LumRadEdit and LumRadCompletion as numpy records (same layout as the C structs)
@@ -132,6 +134,7 @@ _SIGS = {
     "lumrad_server_progress": (C.c_int, [_P]),
     "lumrad_server_run": (C.c_int, [_P, C.c_double]),
     "lumrad_server_poll": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int)]),
+    "lumrad_server_cancel": (C.c_int, [_P, C.c_longlong, C.POINTER(C.c_int)]),
     "lumrad_server_now": (C.c_double, [_P]),
     "lumrad_server_get_radiance": (C.c_int, [_P, C.c_int, _P]),
     "lumrad_server_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),

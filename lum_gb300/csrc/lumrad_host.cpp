@@ -64,6 +64,7 @@ int DeviceWorld::init(int X_, int Y_, int Z_, int slots, int precision_, cudaStr
     h_pal.assign((size_t)n_slots * 4096, 0);
     h_pal_dev.assign((size_t)n_slots * 4096, 0);
     h_mats.assign(LUMRAD_MATERIALS, LumRadMaterial{});
+    h_mats_dev.assign(LUMRAD_MATERIALS, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     LUMRAD_TRY(cudaMalloc(&d_grid, W * sizeof(int16_t)));
     LUMRAD_TRY(cudaMalloc(&d_cgrid, W * sizeof(uint16_t)));
     LUMRAD_TRY(cudaMalloc(&d_pal, h_pal.size()));
@@ -90,6 +91,40 @@ void DeviceWorld::release() {
     d_dirs.clear();
     d_grid = nullptr; d_cgrid = nullptr; d_cbits = nullptr; d_cslot = nullptr; d_pal = nullptr; d_mats = nullptr;
     d_rad[0] = d_rad[1] = nullptr; d_scratch = nullptr; d_probe_count = nullptr; d_stats = nullptr; d_hits = nullptr;
+}
+
+int DeviceWorld::evict(cudaStream_t stream) {
+    if (evicted) return LUMRAD_OK;
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    h_rad_saved.resize(W * rad_stride);
+    LUMRAD_TRY(cudaMemcpy(h_rad_saved.data(), d_rad[cur], W * rad_stride, cudaMemcpyDeviceToHost));
+    release();
+    cbits_cap = scratch_cap = count_cap = hits_cap = hits_n = 0;
+    hits_recorded = false;
+    evicted = true;
+    return LUMRAD_OK;
+}
+
+int DeviceWorld::readmit(cudaStream_t stream) {
+    if (!evicted) return LUMRAD_OK;
+    LUMRAD_TRY(cudaMalloc(&d_grid, W * sizeof(int16_t)));
+    LUMRAD_TRY(cudaMalloc(&d_cgrid, W * sizeof(uint16_t)));
+    LUMRAD_TRY(cudaMalloc(&d_pal, h_pal_dev.size()));
+    LUMRAD_TRY(cudaMalloc(&d_mats, LUMRAD_MATERIALS * sizeof(float4)));
+    LUMRAD_TRY(cudaMalloc(&d_stats, 2 * sizeof(unsigned long long)));
+    for (int i = 0; i < 2; i++) LUMRAD_TRY(cudaMalloc(&d_rad[i], W * rad_stride));
+    LUMRAD_TRY(cudaMemcpyAsync(d_grid, h_grid.data(), W * sizeof(int16_t), cudaMemcpyHostToDevice, stream));
+    LUMRAD_TRY(cudaMemcpyAsync(d_pal, h_pal_dev.data(), h_pal_dev.size(), cudaMemcpyHostToDevice, stream));
+    LUMRAD_TRY(cudaMemcpyAsync(d_mats, h_mats_dev.data(), LUMRAD_MATERIALS * sizeof(float4), cudaMemcpyHostToDevice,
+                               stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
+    LUMRAD_TRY(cudaMemcpyAsync(d_rad[cur], h_rad_saved.data(), W * rad_stride, cudaMemcpyHostToDevice, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    std::vector<uint8_t>().swap(h_rad_saved);
+    evicted = false;
+    grid_dirty = false;
+    compact_dirty = true;   // compact ids and masks built again from the host grid and palette
+    return sync_inputs(stream);
 }
 
 // Renumbers the block ids present in the grid into compact ids (0 stays 0; every id whose palette
@@ -656,7 +691,7 @@ int lumrad_upload_material_palette(LumRadContext ctx) {
     if (!c) return fail(LUMRAD_EINVAL, "null context");
     if (int rc = check_unowned(c)) return rc;
     LUMRAD_TRY(cudaSetDevice(c->device));
-    std::vector<float4> m(LUMRAD_MATERIALS);
+    std::vector<float4>& m = c->world.h_mats_dev;
     const auto& hm = c->world.h_mats;
     for (int i = 0; i < LUMRAD_MATERIALS; i++) m[i] = make_float4(hm[i].color[0], hm[i].color[1], hm[i].color[2], hm[i].emmit);
     LUMRAD_TRY(cudaMemcpyAsync(c->world.d_mats, m.data(), m.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));

@@ -122,6 +122,7 @@ struct SWorld {
     Context* ctx = nullptr;
     size_t bytes = 0;
     bool busy = false;
+    double last_use = 0.0;        // server clock of its last launch (eviction order)
     int last_slot = -1;
     std::deque<SRequest> fifo;
     std::vector<int32_t> stamp;   // dedupe of a request's edits
@@ -248,6 +249,55 @@ void complete_now(Server* sv, const SRequest& r, int status) {
     sv->pending--;
 }
 
+// Per-pass buffers of a world at their size for 256 rays, so the serving loop never reallocates them.
+int prepare_world(DeviceWorld& dw, cudaStream_t stream) {
+    int rc = dw.ensure_scratch(dw.W, 256);
+    if (rc) return rc;
+    for (int R : {32, 64, 128, 256}) {
+        const float4* d = nullptr;
+        if ((rc = dw.ensure_dirs(R, stream, &d))) return rc;
+    }
+    return LUMRAD_OK;
+}
+
+// Evicts idle resident worlds, least recently used first and never one marked in `keep`, until
+// `need` more device bytes fit the budget beside the resident worlds and the launches in flight.
+// An evicted world keeps its grid, palette, materials and volume on the host.
+int make_room(Server* sv, size_t need, const std::vector<char>& keep, bool* fits) {
+    *fits = true;
+    const size_t budget = sv->budget();
+    if (budget == (size_t)-1) return LUMRAD_OK;
+    while (sv->resident + sv->fixed + sv->inflight + need > budget) {
+        int victim = -1;
+        for (size_t w = 0; w < sv->worlds.size(); w++) {
+            const SWorld& sw = sv->worlds[w];
+            if (sw.ctx->world.evicted || sw.busy || keep[w]) continue;
+            if (victim < 0 || sw.last_use < sv->worlds[victim].last_use) victim = (int)w;
+        }
+        if (victim < 0) {
+            *fits = false;
+            return LUMRAD_OK;
+        }
+        SWorld& v = sv->worlds[victim];
+        int rc = v.ctx->world.evict(v.ctx->stream);
+        if (rc) return rc;
+        sv->resident -= v.bytes;
+        sv->st.evictions++;
+    }
+    return LUMRAD_OK;
+}
+
+int readmit_world(Server* sv, SWorld& sw) {
+    DeviceWorld& dw = sw.ctx->world;
+    int rc = dw.readmit(sw.ctx->stream);
+    if (rc) return rc;
+    if ((rc = prepare_world(dw, sw.ctx->stream))) return rc;
+    sw.bytes = dw.footprint();
+    sv->resident += sw.bytes;
+    sv->st.readmissions++;
+    return LUMRAD_OK;
+}
+
 // Forms and enqueues one launch on slot `k`; *started = false if no request was due and fit.
 // With `free_slots` launch slots idle, a launch takes at most 1/free_slots of the due requests,
 // so under load several launches run at once and a finished one frees its worlds while the
@@ -270,16 +320,28 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     size_t bytes = 0;
     int cap = (int)((cand.size() + (size_t)free_slots - 1) / (size_t)free_slots);
     if (sv->s.max_requests_per_launch > 0) cap = std::min(cap, sv->s.max_requests_per_launch);
+    std::vector<char> keep(sv->worlds.size(), 0);
+    int rc;
     for (int w : cand) {
         SWorld& sw = sv->worlds[w];
-        const size_t need = sv->request_bytes(sw.fifo.front());
-        if (budget != (size_t)-1 && sv->resident + sv->fixed + need > budget) {   // can never fit
+        const bool resident = !sw.ctx->world.evicted;
+        const size_t req = sv->request_bytes(sw.fifo.front());
+        // can never fit: not even with every other world evicted and nothing in flight
+        if (budget != (size_t)-1 && sv->fixed + sw.bytes + req > budget) {
             complete_now(sv, sw.fifo.front(), LUMRAD_ENOMEM);
             sw.fifo.pop_front();
             continue;
         }
-        if (budget != (size_t)-1 && sv->resident + sv->fixed + sv->inflight + bytes + need > budget) continue;
-        bytes += need;
+        keep[w] = 1;
+        bool fits = true;
+        if ((rc = make_room(sv, bytes + req + (resident ? 0 : sw.bytes), keep, &fits))) return rc;
+        if (!fits) {   // waits for launches in flight to retire
+            keep[w] = 0;
+            continue;
+        }
+        if (!resident && (rc = readmit_world(sv, sw))) return rc;
+        bytes += req;
+        sw.last_use = now;
         sl.reqs.push_back(std::move(sw.fifo.front()));
         sw.fifo.pop_front();
         if ((int)sl.reqs.size() >= cap) break;
@@ -292,7 +354,6 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     sv->lists.clear();
     std::vector<size_t> list_off(nl);
     sl.probes.assign(nl, 0);
-    int rc;
     for (int j = 0; j < nl; j++) {
         SRequest& r = sl.reqs[j];
         SWorld& sw = sv->worlds[r.world];
@@ -441,7 +502,10 @@ void destroy_server(Server* sv) {
         if (sl.ev_done) cudaEventDestroy(sl.ev_done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
-    for (auto& w : sv->worlds) w.ctx->owner = nullptr;
+    for (auto& w : sv->worlds) {   // contexts go back to their callers resident and usable
+        if (w.ctx->world.evicted) w.ctx->world.readmit(w.ctx->stream);
+        w.ctx->owner = nullptr;
+    }
     delete sv;
 }
 
@@ -530,17 +594,15 @@ int lumrad_server_add_world(LumRadServer server, LumRadContext world, int* id) {
     LUMRAD_TRY(cudaSetDevice(sv->s.device));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     DeviceWorld& dw = c->world;
+    if (!dw.h_cur.empty()) dw.grid_dirty = true;   // a blockified frame is dropped: edits apply to the loaded world
     int rc = dw.sync_inputs(c->stream);
     if (rc) return rc;
-    // per-pass buffers at their size for 256 rays, so the serving loop never reallocates them
-    if ((rc = dw.ensure_scratch(dw.W, 256))) return rc;
-    for (int R : {32, 64, 128, 256}) {
-        const float4* d = nullptr;
-        if ((rc = dw.ensure_dirs(R, c->stream, &d))) return rc;
-    }
+    if ((rc = prepare_world(dw, c->stream))) return rc;
     const size_t bytes = dw.footprint();
-    if (sv->resident + sv->fixed + bytes > sv->budget())
-        return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget");
+    if (sv->fixed + bytes > sv->budget()) return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget");
+    bool fits = true;
+    if ((rc = make_room(sv, bytes, std::vector<char>(sv->worlds.size(), 0), &fits))) return rc;
+    if (!fits) return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget beside the busy worlds");
     SWorld w;
     w.ctx = c;
     w.bytes = bytes;
@@ -598,6 +660,21 @@ int lumrad_server_run(LumRadServer server, double timeout_s) {
     return LUMRAD_OK;
 }
 
+int lumrad_server_cancel(LumRadServer server, long long request, int* cancelled) {
+    Server* sv = as_server(server);
+    if (!sv || !cancelled) return fail(LUMRAD_EINVAL, "null argument");
+    *cancelled = 0;
+    for (auto& sw : sv->worlds)
+        for (auto it = sw.fifo.begin(); it != sw.fifo.end(); ++it)
+            if (it->id == request) {
+                complete_now(sv, *it, LUMRAD_ECANCELED);
+                sw.fifo.erase(it);
+                *cancelled = 1;
+                return LUMRAD_OK;
+            }
+    return LUMRAD_OK;
+}
+
 int lumrad_server_poll(LumRadServer server, LumRadCompletion* out, int cap, int* n) {
     Server* sv = as_server(server);
     if (!sv || !n || (cap > 0 && !out)) return fail(LUMRAD_EINVAL, "bad argument");
@@ -626,12 +703,36 @@ int lumrad_server_get_radiance(LumRadServer server, int world, float* rgb) {
         int rc = retire(sv);
         if (rc) return rc;
     }
+    const DeviceWorld& dw = w.ctx->world;
+    if (dw.evicted) {   // the volume kept on the host
+        for (size_t i = 0; i < dw.W; i++)
+            for (int k = 0; k < 3; k++) {
+                float v;
+                if (dw.precision == LUMRAD_PRECISION_FP32) {
+                    std::memcpy(&v, dw.h_rad_saved.data() + 16 * i + 4 * k, 4);
+                } else {
+                    uint16_t bits;
+                    std::memcpy(&bits, dw.h_rad_saved.data() + 8 * i + 2 * k, 2);
+                    if (dw.precision == LUMRAD_PRECISION_FP16) {
+                        __half_raw r;
+                        r.x = bits;
+                        v = __half2float(__half(r));
+                    } else {
+                        const uint32_t u = (uint32_t)bits << 16;
+                        std::memcpy(&v, &u, 4);
+                    }
+                }
+                rgb[3 * i + k] = v;
+            }
+        return LUMRAD_OK;
+    }
     return lumrad_get_radiance(w.ctx, rgb);
 }
 
 int lumrad_server_stats(LumRadServer server, LumRadServerStats* out) {
     Server* sv = as_server(server);
     if (!sv || !out) return fail(LUMRAD_EINVAL, "null argument");
+    sv->st.resident_bytes = (double)sv->resident;
     *out = sv->st;
     return LUMRAD_OK;
 }

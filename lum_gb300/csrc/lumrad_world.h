@@ -39,6 +39,7 @@ struct DeviceWorld {
     std::vector<uint8_t> h_pal;           // staged palette (lumrad_load_block)
     std::vector<uint8_t> h_pal_dev;       // palette as uploaded
     std::vector<LumRadMaterial> h_mats;
+    std::vector<float4> h_mats_dev;       // materials as uploaded
     std::vector<uint8_t> h_cgrid;         // compact ids (uint8 or uint16)
     std::vector<uint32_t> h_cbits;
     std::vector<int> h_cslot;             // palette slot of each compact id (-1: none)
@@ -71,9 +72,16 @@ struct DeviceWorld {
     std::map<int, float4*> d_dirs;
     // blockify: the frame's grid with temporary blocks (empty when not blockified)
     std::vector<int16_t> h_cur;
+    // eviction: the device buffers released, the volume kept here (raw storage, W * rad_stride)
+    bool evicted = false;
+    std::vector<uint8_t> h_rad_saved;
 
     int init(int X, int Y, int Z, int slots, int precision, cudaStream_t stream);
     void release();
+    // Releases every device buffer of the world, keeping its grid, palette, materials and volume
+    // on the host; readmit allocates and uploads them again (then the world is as it was).
+    int evict(cudaStream_t stream);
+    int readmit(cudaStream_t stream);
     void build_compact() { build_compact(h_grid.data()); }
     void build_compact(const int16_t* g);   // compact ids of grid g (W ids)
     // Compact id of block id b, assigning the next free one (and its occupancy mask in h_cbits)

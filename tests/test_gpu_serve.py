@@ -179,3 +179,62 @@ def test_owned_context_rejects_direct_calls():
     rws[0].radiance_pass(worldgen.all_probes(DIMS[0]), lum_gb300.pass_params())
     rws[0].synchronize()
     rws[0].close()
+
+
+def test_eviction_under_a_tight_budget_changes_nothing():
+    """A budget that holds the launch buffers and about two worlds: the server evicts and
+    re-admits worlds, and every world ends bit-identical to the unconstrained server's."""
+    import lum_gb300
+    worlds = _worlds()
+    reqs = _requests(3, seed=4)
+    free, free_rws = _server(worlds, [0, 1, 2, 3])
+    _submit(free, reqs, [0, 1, 2, 3])
+    free.run(timeout_s=300)
+    st0 = free.stats()
+    budget = st0["launch_bytes"] + st0["resident_bytes"] / 2 + 40_000   # about two of the four worlds
+    tight, tight_rws = _server(worlds, [0, 1, 2, 3], hbm_budget_bytes=budget)
+    _submit(tight, reqs, [0, 1, 2, 3])
+    tight.run(timeout_s=300)
+    st1 = tight.stats()
+    assert st1["requests"] == len(reqs) and st1["evictions"] > 0 and st1["readmissions"] > 0
+    assert st1["resident_bytes"] + st1["launch_bytes"] <= budget
+    for i in range(4):   # evicted worlds read from their host copy, resident ones from the device
+        assert tight.get_radiance(i).tobytes() == free.get_radiance(i).tobytes()
+    tight.close()
+    # the contexts come back resident and usable
+    for rw in tight_rws:
+        rw.radiance_pass(worldgen.all_probes(rw.dims)[:5], lum_gb300.pass_params(rays=32))
+        rw.synchronize()
+    free.close()
+    for rw in free_rws + tight_rws:
+        rw.close()
+
+
+def test_cancel_before_launch():
+    import lum_gb300
+    worlds = _worlds()
+    reqs = _requests(2, seed=5)
+    a, a_rws = _server(worlds, [0, 1])
+    b, b_rws = _server(worlds, [0, 1])
+    mine = [(i, e, lum_gb300.pass_params(rays=r, max_dist=64.0, blend=0.1, time_seed=seed))
+            for i, e, r, seed in reqs if i in (0, 1)]
+    skip = [k for k, (i, _, _) in enumerate(mine) if i == 1][1]   # world 1's second request
+    dropped = None
+    for k, (i, e, p) in enumerate(mine):
+        rid = a.submit(i, e, p)
+        if k == skip:
+            dropped = rid
+        else:
+            b.submit(i, e, p)
+    assert a.cancel(dropped) is True
+    assert a.cancel(dropped) is False
+    a.run(timeout_s=120)
+    b.run(timeout_s=120)
+    d = a.poll()
+    assert (d[d["request"] == dropped]["status"] == lum_gb300._native.LUMRAD_ECANCELED).all()
+    for i in (0, 1):
+        assert a.get_radiance(i).tobytes() == b.get_radiance(i).tobytes()
+    for s in (a, b):
+        s.close()
+    for rw in a_rws + b_rws:
+        rw.close()
