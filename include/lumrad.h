@@ -325,6 +325,7 @@ typedef struct {
     int    max_requests_in_launch;
     long long evictions;          /* worlds evicted to make room */
     long long readmissions;       /* evicted worlds uploaded again */
+    double peak_device_bytes;     /* largest resident + launch buffers + in flight, ever */
 } LumRadServerStats;
 
 int  lumrad_server_create(const LumRadServerSettings* settings, LumRadServer* out);

@@ -61,7 +61,7 @@ class ServerStats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("requests", C.c_longlong), ("probes", C.c_uint64),
                 ("rays", C.c_uint64), ("resident_bytes", C.c_double), ("launch_bytes", C.c_double),
                 ("peak_inflight_bytes", C.c_double), ("max_requests_in_launch", C.c_int),
-                ("evictions", C.c_longlong), ("readmissions", C.c_longlong)]
+                ("evictions", C.c_longlong), ("readmissions", C.c_longlong), ("peak_device_bytes", C.c_double)]
 
 
 # LumRadEdit and LumRadCompletion as numpy records (same layout as the C structs)

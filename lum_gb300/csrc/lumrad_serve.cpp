@@ -468,6 +468,8 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     sv->st.launches++;
     sv->st.max_requests_in_launch = std::max(sv->st.max_requests_in_launch, nl);
     sv->st.peak_inflight_bytes = std::max(sv->st.peak_inflight_bytes, (double)sv->inflight);
+    sv->st.peak_device_bytes =
+        std::max(sv->st.peak_device_bytes, (double)(sv->resident + sv->fixed + sv->inflight));
     *started = true;
     return LUMRAD_OK;
 }
@@ -609,6 +611,7 @@ int lumrad_server_add_world(LumRadServer server, LumRadContext world, int* id) {
     w.stamp.assign(dw.W, 0);
     sv->worlds.push_back(std::move(w));
     sv->resident += bytes;
+    sv->st.peak_device_bytes = std::max(sv->st.peak_device_bytes, (double)(sv->resident + sv->fixed + sv->inflight));
     sv->st.resident_bytes = (double)sv->resident;
     c->owner = sv;
     *id = (int)sv->worlds.size() - 1;
