@@ -73,6 +73,7 @@ int wait_runs(Batch* b) {
 // World table, task offsets (each world starts at a multiple of 8 tasks so a probe's subgroups
 // share a finalize CTA), buffers, and the two graphs.
 int build(Batch* b) {
+    NvtxRange range("lumrad batch build");
     int rc = wait_runs(b);
     if (rc) return rc;
     const int nw = (int)b->worlds.size();
@@ -144,6 +145,7 @@ int check_batch_error(Batch* b) {
 }
 
 int run_graph(Batch* b, int time_seed) {
+    NvtxRange range("lumrad batch run");
     int rc;
     if (b->dirty && (rc = build(b))) return rc;
     const int k = (int)(b->runs & 1);

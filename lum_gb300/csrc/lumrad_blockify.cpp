@@ -104,6 +104,7 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
     Context* c = as_ctx(ctx);
     if (!c || n_meshes < 0 || (n_meshes > 0 && (!models || !transforms))) return fail(LUMRAD_EINVAL, "bad argument");
     if (int rc = check_unowned(c)) return rc;
+    NvtxRange range("lumrad blockify");
     DeviceWorld& w = c->world;
     if (static_blocks < 1 || static_blocks > w.n_slots) return fail(LUMRAD_EINVAL, "static_blocks must be in [1, max_block_types]");
     if (n_meshes >= (1 << 23)) return fail(LUMRAD_EINVAL, "too many meshes");

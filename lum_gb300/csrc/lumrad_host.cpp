@@ -409,6 +409,7 @@ int Context::handle_error(int e) {
 }
 
 int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in) {
+    NvtxRange range("lumrad radiance pass");
     if (int rc = check_unowned(this)) return rc;
     LumRadPassParams p = *p_in;
     if (p.size == 0) {
@@ -460,6 +461,7 @@ int Context::ensure_list_scratch() {
 }
 
 int Context::build_list_device(bool consume, int* n) {
+    NvtxRange range("lumrad update list");
     int rc = world.sync_inputs(stream);
     if (rc) return rc;
     const long long W = (long long)world.W;
@@ -489,6 +491,7 @@ int Context::build_list_device(bool consume, int* n) {
 // copy extent); here any axis with |shift| >= its size leaves the volume unchanged.
 int Context::shift_volume(int dx, int dy, int dz) {
     if (dx == 0 && dy == 0 && dz == 0) return LUMRAD_OK;
+    NvtxRange range("lumrad shift radiance");
     if (std::abs(dx) >= world.X || std::abs(dy) >= world.Y || std::abs(dz) >= world.Z) return LUMRAD_OK;
     LUMRAD_TRY(launch_shift_radiance(world.d_rad[world.cur], world.d_rad[1 - world.cur], world.X, world.Y, world.Z, dx,
                                      dy, dz, world.precision, stream));

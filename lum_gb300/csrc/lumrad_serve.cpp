@@ -303,6 +303,7 @@ int readmit_world(Server* sv, SWorld& sw) {
 // so under load several launches run at once and a finished one frees its worlds while the
 // others still keep the GPU busy.
 int launch(Server* sv, int k, int free_slots, bool* started) {
+    NvtxRange range("lumrad server launch");
     *started = false;
     Slot& sl = *sv->slots[k];
     const double now = sv->now();

@@ -10,9 +10,19 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "lumrad_internal.h"
 
 namespace lumrad {
+
+// An NVTX range around a host call, shown on profiler timelines (no cost without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 extern thread_local std::string g_error;
 int fail(int code, const std::string& msg);
