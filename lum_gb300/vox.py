@@ -111,6 +111,15 @@ def material_palette(path: str) -> np.ndarray:
     return m
 
 
+def save_scene(path: str, grid: np.ndarray) -> None:
+    """A scene file as save_scene writes it (load_stuff.cpp:218-231): the ivec3 world size (x, y, z)
+    and the int16 grid, x-fastest.  grid is (Z, Y, X)."""
+    g = np.ascontiguousarray(grid, dtype="<i2")
+    Z, Y, X = g.shape
+    with open(path, "wb") as f:
+        f.write(struct.pack("<iii", X, Y, Z) + g.tobytes())
+
+
 def load_scene(path: str, world_size, palette_slots: int) -> np.ndarray:
     """The int16 grid (Z, Y, X) of a scene file (load_stuff.cpp:187-210): an ivec3 header and an
     x-fastest int16 grid; the part inside world_size is read, ids clamped to [0, palette_slots]."""

@@ -66,3 +66,13 @@ def test_reference_demo_assets():
     assert b.shape == (16, 16, 16) and (b > 0).mean() > 0.5
     m = vox.material_palette(os.path.join(REF, "tank_body.vox"))
     assert (m[:, 4] > 0).sum() > 0
+
+
+def test_scene_round_trip(tmp_path):
+    from lum_gb300 import worldgen
+    w = worldgen.terrain_world((9, 7, 5), seed=3, n_types=12)
+    p = str(tmp_path / "scene")
+    vox.save_scene(p, w.grid)
+    assert np.array_equal(vox.load_scene(p, w.dims, 12), w.grid)
+    # a smaller world reads the corner that fits
+    assert np.array_equal(vox.load_scene(p, (4, 3, 2), 12), w.grid[:2, :3, :4])
