@@ -358,6 +358,9 @@ class RadianceServer:
         return float(self.lib.lumrad_server_now(self.h))
 
     def get_radiance(self, world: int) -> np.ndarray:
+        if not 0 <= world < len(self.worlds):
+            from ._native import LUMRAD_EINVAL
+            raise LumRadError(LUMRAD_EINVAL, "unknown world")
         X, Y, Z = self.worlds[world].dims
         out = np.empty((Z, Y, X, 3), dtype=np.float32)
         check(self.lib.lumrad_server_get_radiance(self.h, world, ptr(out)))
