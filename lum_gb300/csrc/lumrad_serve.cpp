@@ -134,6 +134,8 @@ struct Slot {
     cudaEvent_t ev_done = nullptr;
     uint8_t* h_pack = nullptr;
     size_t h_cap = 0;
+    std::vector<uint8_t*> h_old;  // outgrown pinned packs, freed with the server (freeing pinned
+                                  // memory synchronises the device, which would stall every launch)
     uint8_t* d_pack = nullptr;
     size_t d_cap = 0;
     unsigned long long* d_queue = nullptr;
@@ -182,13 +184,13 @@ struct Server {
 
 Server* as_server(LumRadServer h) { return reinterpret_cast<Server*>(h); }
 
-int grow_pinned(uint8_t** p, size_t* cap, size_t need) {
+int grow_pinned(uint8_t** p, size_t* cap, size_t need, std::vector<uint8_t*>& old) {
     if (need <= *cap) return LUMRAD_OK;
     const size_t c = std::max(need, *cap * 2);
-    if (*p) cudaFreeHost(*p);
-    *p = nullptr;
-    *cap = 0;
-    LUMRAD_TRY(cudaMallocHost(p, c));
+    uint8_t* q = nullptr;
+    LUMRAD_TRY(cudaMallocHost(&q, c));
+    if (*p) old.push_back(*p);
+    *p = q;
     *cap = c;
     return LUMRAD_OK;
 }
@@ -406,7 +408,7 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     const size_t off_e = align_up((size_t)nl * sizeof(WorldPass), 256);
     const size_t off_l = align_up(off_e + sv->erec.size() * sizeof(EditRecord), 256);
     const size_t total = off_l + sv->lists.size() * sizeof(short4);
-    if ((rc = grow_pinned(&sl.h_pack, &sl.h_cap, total))) return rc;
+    if ((rc = grow_pinned(&sl.h_pack, &sl.h_cap, total, sl.h_old))) return rc;
     if (total > sl.d_cap) {
         const size_t c = std::max(total, sl.d_cap * 2);
         if (sl.d_pack) LUMRAD_TRY(cudaFreeAsync(sl.d_pack, sl.stream));
@@ -498,6 +500,7 @@ void destroy_server(Server* sv) {
         if (sl.d_pack) cudaFreeAsync(sl.d_pack, sl.stream);
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.h_pack) cudaFreeHost(sl.h_pack);
+        for (uint8_t* p : sl.h_old) cudaFreeHost(p);
         if (sl.h_error) cudaFreeHost(sl.h_error);
         cudaFree(sl.d_queue);
         cudaFree(sl.d_error);
@@ -565,8 +568,14 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
             LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, 2 * sizeof(unsigned long long), sl.stream));
             LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
             LUMRAD_TRY(cudaMalloc(&sl.d_ray_res, rays * sizeof(uint2)));
+            // request packs sized up front so the serving loop rarely grows them
+            const size_t pack = (size_t)16 << 20;
+            LUMRAD_TRY(cudaMallocHost(&sl.h_pack, pack));
+            sl.h_cap = pack;
+            LUMRAD_TRY(cudaMallocAsync(reinterpret_cast<void**>(&sl.d_pack), pack, sl.stream));
+            sl.d_cap = pack;
             LUMRAD_TRY(cudaStreamSynchronize(sl.stream));
-            sv->fixed += rays * sizeof(uint2) + 2 * sizeof(unsigned long long) + sizeof(int);
+            sv->fixed += rays * sizeof(uint2) + pack + 2 * sizeof(unsigned long long) + sizeof(int);
         }
         if (sv->fixed > sv->budget()) return fail(LUMRAD_ENOMEM, "the launch buffers alone exceed the HBM budget");
         return LUMRAD_OK;
