@@ -4,14 +4,17 @@ Workload (one "step"): the 64x64x16-block terrain world plus 2000 random blocks 
 8 successive passes (multi-bounce, each reading the previous pass's volume), each over a seeded
 10% subset of the probes, 256 rays per probe, max_dist 256, blend 0.1, FP32 radiance.
 
-  value      probe-rays/s with every input resident in HBM (request lists uploaded once);
+  value      probe-rays/s with every input resident in HBM (request lists uploaded once), the
+             step's 8 passes in one lumrad_radiance_passes_resident call (one march launch for
+             all 8, then each pass's finalize in order; bit-identical to 8 single passes);
              CUDA events on the pass stream around each step; L2 flushed (256 MiB write)
              between steps, outside the timed region.
-  e2e        the same metric through the C ABI with host buffers: each pass copies its request
-             list host->device, each step reads the radiance volume back.
-  roofline   algorithmic bytes of one pass (3 B per grid+palette lookup, 16+8*12 B per hit,
-             8+2*12 B per probe; counts exact from the kernels' counters) over the pass kernels'
-             own event-timed duration (march + finalize), against the measured HBM copy peak.
+  single_pass  the same step as 8 lumrad_radiance_pass_resident calls (one frame's update each).
+  e2e        the same metric through the C ABI with host buffers: each step copies its 8 request
+             lists host->device (lumrad_radiance_passes) and reads the radiance volume back.
+  roofline   algorithmic bytes of one step (3 B per grid+palette lookup, 16+8*12 B per hit,
+             8+2*12 B per probe; counts exact from the kernels' counters) over the step's kernels'
+             own event-timed duration (march + 8 finalize), against the measured HBM copy peak.
   cpu_baseline  the CPU oracle (port, OpenMP over all host cores) on whole steps, ~12 s.
 
 --impl reference times the reference's implementation of the same workload on the host cores:
@@ -48,9 +51,10 @@ BLEND = 0.1
 SEED = 1234
 S_R = 12            # bytes of FP32 RGB radiance per probe
 CHUNK_TASKS = 1 << 18   # 32-ray tasks per march/finalize round of the library
-# DRAM bytes (read + write) of one pass's two kernels in an ncu capture of this workload
-# (march 0.16 + 0.00 MB, finalize 14.78 + 0.00 MB; ncu replays with cold caches)
-NCU_DRAM_BYTES_PER_PASS = 14.94e6
+# DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
+# finalize launches) in an ncu capture of this workload; ncu replays with cold caches
+# (march 1.23 + 46.12 MB, finalizes 118.31 + 0 MB)
+NCU_DRAM_BYTES_PER_STEP = 165.67e6
 
 
 def pass_lists(dims):
@@ -435,61 +439,75 @@ def main():
         st = rw.pass_stats()
         pass_steps.append(st["steps"])
         pass_bytes.append(algorithmic_bytes(st["steps"], st["hits"], st["probes"]))
+    slots = list(range(PASSES))
+    plist = [params(p) for p in range(PASSES)]
+
+    def step_resident():
+        # the step's 8 passes in one call: one march launch for all of them, then each pass's
+        # finalize in order (bit-identical to 8 single passes); one kernel-time entry
+        rw.radiance_passes_resident(slots, plist)
+        return 1
+
     for _ in range(args.warmup):
-        for p in range(PASSES):
-            rw.radiance_pass_resident(p, params(p))
+        step_resident()
     rw.synchronize()
 
-    step_ms = []
-    kernel_ms = []
-    with ClockSampler(local) as clocks:
-        # ~1.5 s of the same passes first, so the clock samples see the GPU under this load
-        soak_end = time.perf_counter() + 1.5
-        while time.perf_counter() < soak_end:
-            for p in range(PASSES):
-                rw.radiance_pass_resident(p, params(p))
-            rw.synchronize()
-        if pg:
-            pg.barrier()
-        torch.cuda.synchronize()
-        for _ in range(args.steps):
+    def timed_steps(run, n):
+        st, kt_all = [], []
+        for _ in range(n):
             with torch.cuda.stream(stream):
                 flush.zero_()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            for p in range(PASSES):
-                rw.radiance_pass_resident(p, params(p))
+            k = run()
             e1.record(stream)
-            kt = rw.kernel_times(PASSES)   # synchronises after the step's passes
-            kernel_ms.extend(kt.tolist())
-            step_ms.append(e0.elapsed_time(e1))
+            kt_all.append(float(rw.kernel_times(k).sum()))   # synchronises after the step
+            st.append(e0.elapsed_time(e1))
+        return st, kt_all
+
+    def single_step():
+        for p in range(PASSES):
+            rw.radiance_pass_resident(p, params(p))
+        return PASSES
+
+    with ClockSampler(local) as clocks:
+        # ~1.5 s of the same passes first, so the clock samples see the GPU under this load
+        soak_end = time.perf_counter() + 1.5
+        while time.perf_counter() < soak_end:
+            step_resident()
+            rw.synchronize()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        step_ms, kernel_ms = timed_steps(step_resident, args.steps)
         torch.cuda.synchronize()
         if pg:
             pg.barrier()
+        # the drop-in's one-pass-per-call path (a frame's update_radiance) on the same passes
+        single_ms, single_kernel_ms = timed_steps(single_step, args.steps)
     dev = f"cuda:{local}"
     total_ms = max_over_ranks(float(sum(step_ms)), pg, dev)
     value = job_value(args.steps * rays_per_step, world_size, total_ms / 1000.0)
+    single_total_ms = max_over_ranks(float(sum(single_ms)), pg, dev)
 
     hbm_peak, peak_kind = load_peaks()
-    bytes_per_launch = float(np.mean(pass_bytes))
-    kern_avg_s = float(np.mean(kernel_ms)) / 1000.0
+    bytes_per_launch = float(np.sum(pass_bytes))       # the step's 8 passes: one march launch
+    kern_avg_s = float(np.mean(kernel_ms)) / 1000.0    # march + 8 finalize launches of a step
     achieved = bytes_per_launch / kern_avg_s / 1e9
 
     # ---------------------------------------------------------------- end to end (e2e)
     rw2 = lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], device=local)
     rw2.load(world)
     for _ in range(max(1, args.warmup)):
-        for p in range(PASSES):
-            rw2.radiance_pass(lists[p], params(p))
+        rw2.radiance_passes(lists, plist)
         rw2.get_radiance()
     e2e_s = 0.0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for p in range(PASSES):
-            rw2.radiance_pass(lists[p], params(p))
+        rw2.radiance_passes(lists, plist)
         rw2.get_radiance()
         e2e_s += time.perf_counter() - t0
     e2e_value = job_value(args.steps * rays_per_step, world_size, max_over_ranks(e2e_s, pg, dev))
@@ -518,12 +536,17 @@ def main():
             "e2e": {"value": e2e_value, "unit": "probe-rays/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": NCU_DRAM_BYTES_PER_PASS, "peak_kind": peak_kind,
+                         "frac": achieved / hbm_peak, "traffic": NCU_DRAM_BYTES_PER_STEP, "peak_kind": peak_kind,
                          "bytes_per_launch": bytes_per_launch, "kernel_ms_avg": kern_avg_s * 1e3,
-                         "ray_steps_per_s": float(np.mean(pass_steps)) / kern_avg_s},
+                         "launch": "one step: a march launch over its 8 passes + 8 finalize launches",
+                         "ray_steps_per_s": float(np.sum(pass_steps)) / kern_avg_s},
+            "single_pass": {"value": job_value(args.steps * rays_per_step, world_size, single_total_ms / 1000.0),
+                            "unit": "probe-rays/s", "ms_per_step": single_total_ms / args.steps,
+                            "kernel_ms_per_pass": float(np.mean(single_kernel_ms)) / PASSES,
+                            "path": "lumrad_radiance_pass_resident once per pass (one frame's update)"},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "gpu_launches": 2 * PASSES * args.steps,   # march + finalize per pass
+            "gpu_launches": (1 + PASSES) * args.steps,   # one march + a finalize per pass, per step
             "batched": batched,
             "serving": serving,
         }

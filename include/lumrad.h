@@ -190,6 +190,19 @@ int  lumrad_radiance_pass_i8(LumRadContext ctx, const int8_t* requests, int n,
 int  lumrad_upload_requests(LumRadContext ctx, int slot, const int16_t* requests, int n);
 int  lumrad_radiance_pass_resident(LumRadContext ctx, int slot, const LumRadPassParams* params);
 
+/* n passes in order, with results equal bit for bit to n lumrad_radiance_pass calls over the same
+ * lists (requests[i] holds counts[i] entries) — successive frames' update_radiance passes
+ * (internal_render.cpp:1129-1214) in one call.  The traversal does not read the radiance volume,
+ * so the marches of consecutive passes share one launch (their rays wait in device memory) and
+ * each pass's shading/blend then runs in order on its predecessor's volume.  Every params[i]
+ * needs size >= 1 and record_hits 0.  Afterwards lumrad_get_pass_stats sums probes, rays, steps
+ * and hits over the n passes and lumrad_get_kernel_times has one entry for the whole call. */
+int  lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, const int* counts,
+                            const LumRadPassParams* params, int n);
+/* The same over resident lists (slots[i] for pass i). */
+int  lumrad_radiance_passes_resident(LumRadContext ctx, const int* slots, const LumRadPassParams* params,
+                                     int n);
+
 /* Hit records of the last pass run with record_hits = 1: n_groups*R entries in dispatch
  * order (entry g*R + r = ray r of workgroup g).  *n = number available. */
 int  lumrad_get_hits(LumRadContext ctx, LumRadHit* out, size_t cap, size_t* n);

@@ -196,6 +196,22 @@ class RadianceWorld:
         check(self.lib.lumrad_gather_radiance(self.h, ptr(p), p.shape[0], ptr(out)))
         return out
 
+    def radiance_passes(self, lists, params) -> None:
+        """Passes over int16 (n, 4) lists in order, as radiance_pass over each would run them;
+        their marches share launches."""
+        reqs = [np.ascontiguousarray(r, dtype=np.int16).reshape(-1, 4) for r in lists]
+        n = len(reqs)
+        ptrs = (C.c_void_p * max(n, 1))(*[r.ctypes.data for r in reqs])
+        counts = (C.c_int * max(n, 1))(*[r.shape[0] for r in reqs])
+        ps = (PassParams * max(n, 1))(*params)
+        check(self.lib.lumrad_radiance_passes(self.h, ptrs, counts, ps, n))
+
+    def radiance_passes_resident(self, slots, params) -> None:
+        n = len(slots)
+        sl = (C.c_int * max(n, 1))(*[int(s) for s in slots])
+        ps = (PassParams * max(n, 1))(*params)
+        check(self.lib.lumrad_radiance_passes_resident(self.h, sl, ps, n))
+
     def upload_requests(self, slot: int, requests: np.ndarray) -> None:
         req = np.ascontiguousarray(requests, dtype=np.int16)
         check(self.lib.lumrad_upload_requests(self.h, slot, ptr(req), req.shape[0]))

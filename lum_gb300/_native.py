@@ -100,6 +100,8 @@ _SIGS = {
     "lumrad_radiance_pass_i8": (C.c_int, [_P, _P, C.c_int, C.POINTER(PassParams)]),
     "lumrad_upload_requests": (C.c_int, [_P, C.c_int, _P, C.c_int]),
     "lumrad_radiance_pass_resident": (C.c_int, [_P, C.c_int, C.POINTER(PassParams)]),
+    "lumrad_radiance_passes": (C.c_int, [_P, _P, _P, C.POINTER(PassParams), C.c_int]),
+    "lumrad_radiance_passes_resident": (C.c_int, [_P, _P, C.POINTER(PassParams), C.c_int]),
     "lumrad_get_hits": (C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "lumrad_get_pass_stats": (C.c_int, [_P, C.POINTER(PassStats)]),
     "lumrad_get_stream": (C.c_int, [_P, C.POINTER(_P)]),

@@ -352,8 +352,8 @@ int Context::ensure_req_capacity(size_t n) {
     return LUMRAD_OK;
 }
 
-int Context::ensure_rays(long long n_tasks) {
-    const size_t need = (size_t)std::min<long long>(std::max<long long>(n_tasks, 1), kChunkTasks) * kTaskRays;
+int Context::ensure_rays(long long n_tasks, long long cap_tasks) {
+    const size_t need = (size_t)std::min<long long>(std::max<long long>(n_tasks, 1), cap_tasks) * kTaskRays;
     if (need <= ray_cap) return LUMRAD_OK;
     LUMRAD_TRY(cudaStreamSynchronize(stream));
     cudaFree(d_ray_res);
@@ -447,6 +447,116 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     return LUMRAD_OK;
 }
 
+int Context::ensure_pass_table(int n) {
+    if (n <= ptab_cap) return LUMRAD_OK;
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    for (int h = 0; h < 2; h++) {
+        if (h_ptab[h]) cudaFreeHost(h_ptab[h]);
+        h_ptab[h] = nullptr;
+    }
+    cudaFree(d_ptab);
+    d_ptab = nullptr;
+    ptab_cap = 0;
+    const int cap = std::max(n, 16);
+    for (int h = 0; h < 2; h++) LUMRAD_TRY(cudaMallocHost(&h_ptab[h], cap * sizeof(WorldPass)));
+    LUMRAD_TRY(cudaMalloc(&d_ptab, cap * sizeof(WorldPass)));
+    ptab_cap = cap;
+    return LUMRAD_OK;
+}
+
+// The passes' marches do not read the radiance volume, so consecutive passes whose tasks fit
+// kMultiTasks share one march launch (one queue drain instead of one per pass); each pass's
+// finalize then runs in order, reading the volume its predecessor wrote.  A pass larger than
+// kMultiTasks runs alone in rounds, as lumrad_radiance_pass runs it.  Results are those of n
+// single passes, bit for bit; counters and the kernel-time entry cover all n.
+int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPassParams* ps, int n) {
+    NvtxRange range("lumrad radiance passes");
+    if (int rc = check_unowned(this)) return rc;
+    if (n <= 0) return LUMRAD_OK;
+    int rc = world.sync_inputs(stream);
+    if (rc) return rc;
+    const int slot = (int)(n_passes % kRing);
+    LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
+    LUMRAD_TRY(cudaMemsetAsync(world.d_stats, 0, 2 * sizeof(unsigned long long), stream));
+    const size_t vol_bytes = (size_t)world.W * world.rad_stride;
+    uint64_t probes = 0, rays = 0;
+    auto aligned_tasks = [&](int i) -> long long {
+        const long long t = (long long)(ns[i] / ps[i].size) * (ps[i].rays_per_probe / 32);
+        return (t + kWarps - 1) / kWarps * kWarps;
+    };
+    int i = 0;
+    while (i < n) {
+        if (aligned_tasks(i) > kMultiTasks) {
+            // one pass in rounds of kChunkTasks
+            LaunchArgs la;
+            std::memset(&la, 0, sizeof la);
+            if ((rc = world.fill_pass(reqs[i], ns[i], ps[i], stream, &la.single))) return rc;
+            LUMRAD_TRY(cudaMemcpyAsync(la.single.next, la.single.prev, vol_bytes, cudaMemcpyDeviceToDevice, stream));
+            la.n_worlds = 1;
+            la.n_tasks = la.single.n_tasks;
+            la.queue = d_queue;
+            la.error = d_error;
+            if ((rc = ensure_rays(la.n_tasks))) return rc;
+            la.ray_res = d_ray_res;
+            la.ray_blk = d_ray_blk;
+            LUMRAD_TRY(launch_radiance(la, world.precision, false, num_sms, stream));
+            probes += (uint64_t)la.single.n_groups;
+            rays += (uint64_t)la.single.n_groups * la.single.R;
+            world.cur = 1 - world.cur;
+            i++;
+            continue;
+        }
+        // the longest run of passes from i whose tasks fit one march launch
+        int j = i;
+        long long total = 0;
+        while (j < n && aligned_tasks(j) <= kMultiTasks - total) total += aligned_tasks(j++);
+        const int k = j - i;
+        if ((rc = ensure_pass_table(k))) return rc;
+        WorldPass* tab = h_ptab[ptab_half];
+        if (ev_ptab[ptab_half]) LUMRAD_TRY(cudaEventSynchronize(ev_ptab[ptab_half]));   // its last copy is done
+        long long begin = 0;
+        for (int q = 0; q < k; q++) {
+            if ((rc = world.fill_pass(reqs[i + q], ns[i + q], ps[i + q], stream, &tab[q]))) return rc;
+            tab[q].task_begin = begin;
+            begin += aligned_tasks(i + q);
+            probes += (uint64_t)tab[q].n_groups;
+            rays += (uint64_t)tab[q].n_groups * tab[q].R;
+            world.cur = 1 - world.cur;   // the next pass reads what this one writes
+        }
+        for (int q = 0; q < k; q++) {    // buffers fill_pass may have grown on a later pass
+            tab[q].scratch = world.d_scratch;
+            tab[q].probe_count = world.d_probe_count;
+            tab[q].stats = world.d_stats;
+        }
+        if ((rc = ensure_rays(total, kMultiTasks))) return rc;
+        LUMRAD_TRY(cudaMemcpyAsync(d_ptab, tab, k * sizeof(WorldPass), cudaMemcpyHostToDevice, stream));
+        if (!ev_ptab[ptab_half]) LUMRAD_TRY(cudaEventCreateWithFlags(&ev_ptab[ptab_half], cudaEventDisableTiming));
+        LUMRAD_TRY(cudaEventRecord(ev_ptab[ptab_half], stream));
+        ptab_half ^= 1;
+        LaunchArgs la;
+        std::memset(&la, 0, sizeof la);
+        la.worlds = d_ptab;
+        la.n_worlds = k;
+        la.n_tasks = total;
+        la.queue = d_queue;
+        la.error = d_error;
+        la.ray_res = d_ray_res;
+        la.ray_blk = d_ray_blk;
+        LUMRAD_TRY(launch_passes(la, tab, k, vol_bytes, world.precision, num_sms, stream));
+        i = j;
+    }
+    LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
+    last_slot = slot;
+    n_passes++;
+    frame += n;
+    have_pass = true;
+    world.hits_recorded = false;
+    world.hits_n = 0;
+    last.probes = probes;
+    last.rays = rays;
+    return LUMRAD_OK;
+}
+
 int Context::ensure_list_scratch() {
     const long long W = (long long)world.W;
     if (!list.bits) {
@@ -508,6 +618,11 @@ void Context::release() {
     cudaFree(d_error);
     cudaFree(d_ray_res);
     cudaFree(d_ray_blk);
+    for (int h = 0; h < 2; h++) {
+        if (h_ptab[h]) cudaFreeHost(h_ptab[h]);
+        if (ev_ptab[h]) cudaEventDestroy(ev_ptab[h]);
+    }
+    cudaFree(d_ptab);
     for (auto& kv : resident) cudaFree(kv.second.ptr);
     if (h_req_pinned) cudaFreeHost(h_req_pinned);
     cudaFree(list.bits);
@@ -930,6 +1045,80 @@ int lumrad_radiance_pass_resident(LumRadContext ctx, int slot, const LumRadPassP
     if (params->size == 0) return fail(LUMRAD_EINVAL, "size 0 (adaptive) is only valid for lumrad_update_radiance");
     LUMRAD_TRY(cudaSetDevice(c->device));
     return c->run_pass(it->second.ptr, it->second.n, params);
+}
+
+static int check_pass_list(const LumRadPassParams* params, int n) {
+    if (n < 0 || (n > 0 && !params)) return fail(LUMRAD_EINVAL, "bad pass list");
+    for (int i = 0; i < n; i++) {
+        int rc = check_params(&params[i]);
+        if (rc) return rc;
+        if (params[i].size == 0) return fail(LUMRAD_EINVAL, "size 0 (adaptive) is only valid for lumrad_update_radiance");
+        if (params[i].record_hits) return fail(LUMRAD_EINVAL, "hit records need lumrad_radiance_pass");
+    }
+    return LUMRAD_OK;
+}
+
+int lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, const int* counts,
+                           const LumRadPassParams* params, int n) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    int rc = check_pass_list(params, n);
+    if (rc) return rc;
+    if (n > 0 && (!requests || !counts)) return fail(LUMRAD_EINVAL, "bad request lists");
+    size_t total = 0;
+    for (int i = 0; i < n; i++) {
+        if (counts[i] < 0 || (counts[i] > 0 && !requests[i])) return fail(LUMRAD_EINVAL, "bad request list");
+        total += (size_t)counts[i];
+    }
+    if (n == 0) return LUMRAD_OK;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    if ((rc = check_unowned(c))) return rc;
+    // every list in one pinned buffer and one copy
+    if ((rc = c->ensure_req_capacity(total))) return rc;
+    if (c->req_copy_pending) {
+        LUMRAD_TRY(cudaEventSynchronize(c->ev_req));
+        c->req_copy_pending = false;
+    }
+    if (total > c->h_req_cap) {
+        if (c->h_req_pinned) cudaFreeHost(c->h_req_pinned);
+        c->h_req_pinned = nullptr;
+        c->h_req_cap = 0;
+        const size_t cap = std::max<size_t>(total, 1024);
+        LUMRAD_TRY(cudaMallocHost(&c->h_req_pinned, cap * 4 * sizeof(int16_t)));
+        c->h_req_cap = cap;
+    }
+    std::vector<const short4*> reqs((size_t)n);
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        if (counts[i] > 0) std::memcpy(c->h_req_pinned + off * 4, requests[i], (size_t)counts[i] * 4 * sizeof(int16_t));
+        reqs[i] = c->d_req + off;
+        off += (size_t)counts[i];
+    }
+    if (total > 0) {
+        LUMRAD_TRY(cudaMemcpyAsync(c->d_req, c->h_req_pinned, total * sizeof(short4), cudaMemcpyHostToDevice, c->stream));
+        LUMRAD_TRY(cudaEventRecord(c->ev_req, c->stream));
+        c->req_copy_pending = true;
+    }
+    return c->run_passes(reqs.data(), counts, params, n);
+}
+
+int lumrad_radiance_passes_resident(LumRadContext ctx, const int* slots, const LumRadPassParams* params, int n) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    int rc = check_pass_list(params, n);
+    if (rc) return rc;
+    if (n > 0 && !slots) return fail(LUMRAD_EINVAL, "bad slot list");
+    std::vector<const short4*> reqs((size_t)n);
+    std::vector<int> counts((size_t)n);
+    for (int i = 0; i < n; i++) {
+        auto it = c->resident.find(slots[i]);
+        if (it == c->resident.end()) return fail(LUMRAD_EINVAL, "no request list uploaded in this slot");
+        reqs[i] = it->second.ptr;
+        counts[i] = it->second.n;
+    }
+    if (n == 0) return LUMRAD_OK;
+    LUMRAD_TRY(cudaSetDevice(c->device));
+    return c->run_passes(reqs.data(), counts.data(), params, n);
 }
 
 int lumrad_get_hits(LumRadContext ctx, LumRadHit* out, size_t cap, size_t* n) {

@@ -14,6 +14,9 @@ constexpr int kTaskRays = 32;
 // tasks' rays (8 B per ray: 67 MB, L2-resident on GB300).  Fewer, larger rounds shorten the
 // march kernel's tails (measured: 2^18 tasks 13% faster than 2^16 on many small worlds).
 constexpr int kChunkTasks = 1 << 18;
+// Tasks of one march launch over several passes of a context (their rays, 8 B each, are kept
+// until the passes' finalize launches: 2^19 tasks = 134 MB, about the L2)
+constexpr int kMultiTasks = 1 << 19;
 
 // One world's pass as the kernels see it (all pointers are device pointers).
 //
@@ -64,6 +67,7 @@ struct LaunchArgs {
     int* error;                  // set non-zero if a warp's scheduler stops making progress
     uint2* ray_res;              // per ray of the round: coarse fraction bits, info word
     int* ray_blk;                // per ray of the round: block id at the last coarse step (records)
+    int ray_origin;              // task whose rays start ray_res (the march launch's chunk_begin)
     // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
     // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
     int guided_div, max_chunk, march_ctas;
@@ -81,6 +85,13 @@ struct Tuning {
 // kernel.  Returns a CUDA error code.
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms,
                             cudaStream_t stream);
+
+// Several passes of one context (table `args.worlds`, pass i's tasks from worlds[i].task_begin,
+// n_tasks <= kMultiTasks in all): one march launch over every pass's tasks; then, pass by pass,
+// its next volume becomes a copy of its prev volume (`vol_bytes`) and the finalize kernel runs
+// over its tasks.  `h_tab` is the host copy of the table.  No hit records.
+cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_passes, size_t vol_bytes,
+                          int precision, int num_sms, cudaStream_t stream);
 
 // Start of a multi-world pass: copies every world's prev volume into its next volume and clears
 // its counters (descriptors already on the device).

@@ -123,7 +123,8 @@ struct Context {
     std::map<int, Resident> resident;
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
-    // rays of one march/finalize round (up to kChunkTasks * 32 rays)
+    // rays of one march/finalize round (up to kChunkTasks * 32 rays), or of one march launch over
+    // several passes (up to kMultiTasks * 32)
     uint2* d_ray_res = nullptr;
     int* d_ray_blk = nullptr;
     size_t ray_cap = 0;
@@ -164,11 +165,22 @@ struct Context {
     // gather staging (host-buffer calls)
     float* d_gather = nullptr;
     size_t gather_cap = 0;                // points
+    // pass tables of lumrad_radiance_passes*: two pinned halves (one may still be copying) and
+    // the device table (stream order keeps a copy behind the launches that read the last one)
+    WorldPass* h_ptab[2] = {nullptr, nullptr};
+    WorldPass* d_ptab = nullptr;
+    int ptab_cap = 0;
+    int ptab_half = 0;
+    cudaEvent_t ev_ptab[2] = {nullptr, nullptr};
 
     int ensure_req_capacity(size_t n);
-    int ensure_rays(long long n_tasks);
+    int ensure_rays(long long n_tasks, long long cap_tasks = kChunkTasks);
     int stage_requests(const int16_t* req, size_t n);
     int run_pass(const short4* d_req, int n, const LumRadPassParams* p);
+    // n passes in order (requests reqs[i], ns[i] of them, params ps[i], all validated, size >= 1,
+    // no hit records): marches of consecutive passes share launches
+    int run_passes(const short4* const* reqs, const int* ns, const LumRadPassParams* ps, int n);
+    int ensure_pass_table(int n);
     int check_error();
     int handle_error(int e);              // resets the launch counters after a reported error
     // Builds update_radiance's list on the device into d_req; *n = its length.  The queued

@@ -131,8 +131,12 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                     if (pending == t) pending = -1; else tb++;
                     continue;
                 }
-                if (__any_sync(kFull, my >= 0) || loaded > issued) {
-                    if (pending != t) tb++;   // another world: drain this one first
+                // another world: drain this one first, unless it is another pass over the same
+                // compact world with the same bound (passes of one context), whose rays march alike
+                const bool alike = reinterpret_cast<const uint8_t*>(wq->cgrid) == mv.cgrid &&
+                                   wq->max_dist == max_dist;
+                if (!alike && (__any_sync(kFull, my >= 0) || loaded > issued)) {
+                    if (pending != t) tb++;
                     pending = t;
                     break;
                 }
@@ -266,7 +270,7 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     const bool local = nsub > 1 && (kWarps % nsub) == 0 && (wp->task_begin % kWarps) == 0;
     float3 v = make_float3(0.0f, 0.0f, 0.0f);
     if (valid) {
-        const long long idx = (long long)(t - la.chunk_begin) * kTaskRays + lane;
+        const long long idx = (long long)(t - la.ray_origin) * kTaskRays + lane;
         const uint2 res = __ldcg(la.ray_res + idx);
         const int blk = RECORD ? __ldcg(la.ray_blk + idx) : 0;
         float3 o, d;
@@ -343,6 +347,7 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
     for (long long c0 = 0; c0 < a.n_tasks; c0 += kChunkTasks) {
         args.chunk_begin = (int)c0;
         args.chunk_end = (int)min(c0 + (long long)kChunkTasks, a.n_tasks);
+        args.ray_origin = args.chunk_begin;
         const int n = args.chunk_end - args.chunk_begin;
         march_kernel<RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
         finalize_kernel<Store, RECORD><<<(n + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(args);
@@ -350,7 +355,40 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+template <class Store>
+cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, size_t vol_bytes, int num_sms,
+                     cudaStream_t stream) {
+    const int blocks = march_grid(false, num_sms, a.march_ctas);
+    LaunchArgs args = a;
+    args.total_warps = blocks * kWarps;
+    args.chunk_begin = 0;
+    args.chunk_end = (int)a.n_tasks;
+    args.ray_origin = 0;
+    if (a.n_tasks > 0) march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(args);
+    for (int i = 0; i < n_passes; i++) {
+        const WorldPass& w = h_tab[i];
+        cudaError_t e = cudaMemcpyAsync(w.next, w.prev, vol_bytes, cudaMemcpyDeviceToDevice, stream);
+        if (e != cudaSuccess) return e;
+        if (w.n_tasks <= 0) continue;
+        args.chunk_begin = (int)w.task_begin;
+        args.chunk_end = (int)(w.task_begin + w.n_tasks);
+        const int n = args.chunk_end - args.chunk_begin;
+        finalize_kernel<Store, false><<<(n + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(args);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_passes, size_t vol_bytes,
+                          int precision, int num_sms, cudaStream_t stream) {
+    if (args.n_tasks > kMultiTasks) return cudaErrorInvalidValue;
+    switch (precision) {
+        case LUMRAD_PRECISION_FP16: return passes_t<StoreF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
+        case LUMRAD_PRECISION_BF16: return passes_t<StoreBF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
+        default: return passes_t<StoreF32>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
+    }
+}
 
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream) {
     if (args.n_tasks <= 0) return cudaSuccess;
@@ -613,6 +651,7 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     for (long long c0 = 0; c0 < n_tasks; c0 += kNoAllocRoundTasks) {
         la.chunk_begin = (int)c0;
         la.chunk_end = (int)std::min(c0 + (long long)kNoAllocRoundTasks, n_tasks);
+        la.ray_origin = la.chunk_begin;
         const int tasks = la.chunk_end - la.chunk_begin;
         march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(la);
         finalize_kernel<StoreF32, false><<<(tasks + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(la);

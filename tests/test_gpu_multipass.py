@@ -1,0 +1,113 @@
+"""Several passes in one call (lumrad_radiance_passes[_resident]): the marches of consecutive
+passes share one launch and the finalize steps run in order.  Each case equals the same passes
+run one call at a time, bit for bit, and the oracle's chained passes within 1e-5."""
+import numpy as np
+import pytest
+
+from lum_gb300 import worldgen
+from tests.helpers import RTOL, random_prev, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _passes(w):
+    """Eight passes with different lists, ray counts (one subgroup, subgroups combined in one CTA,
+    3 subgroups combined through global scratch, 16 subgroups), bounds, blends and slicing, and
+    an empty list."""
+    lists = [worldgen.probe_subset(w.dims, f, seed=40, stream=i) for i, f in
+             enumerate((0.3, 1.0, 0.5, 0.2, 0.7, 0.4, 0.6, 0.9))]
+    lists[5] = lists[5][:0]
+    spec = [dict(rays=64, max_dist=96.0, blend=0.1), dict(rays=256, max_dist=96.0, blend=0.2),
+            dict(rays=96, max_dist=96.0, blend=0.1), dict(rays=512, max_dist=64.0, blend=0.3),
+            dict(rays=32, max_dist=64.0, blend=0.1), dict(rays=64, max_dist=64.0, blend=0.1),
+            dict(rays=128, max_dist=128.0, blend=0.05, size=2, shift=1), dict(rays=64, max_dist=128.0, blend=0.1)]
+    for i, s in enumerate(spec):
+        s["time_seed"] = 11 + 3 * i
+    return lists, spec
+
+
+def _run(w, lists, spec, prev, mode, precision="fp32"):
+    import lum_gb300
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], precision=precision) as rw:
+        rw.load(w)
+        rw.set_radiance(prev)
+        params = [lum_gb300.pass_params(**s) for s in spec]
+        steps = hits = probes = 0
+        if mode == "single":
+            for l, p in zip(lists, params):
+                rw.radiance_pass(l, p)
+                st = rw.pass_stats()
+                steps += st["steps"]; hits += st["hits"]; probes += st["probes"]
+        elif mode == "multi":
+            rw.radiance_passes(lists, params)
+            st = rw.pass_stats()
+            steps, hits, probes = st["steps"], st["hits"], st["probes"]
+            assert rw.kernel_times(64).shape[0] == 1   # one entry for the call
+        else:
+            for i, l in enumerate(lists):
+                rw.upload_requests(10 + i, l)
+            rw.radiance_passes_resident([10 + i for i in range(len(lists))], params)
+            st = rw.pass_stats()
+            steps, hits, probes = st["steps"], st["hits"], st["probes"]
+        return rw.get_radiance(), (steps, hits, probes)
+
+
+@pytest.mark.parametrize("mode", ["multi", "resident"])
+def test_passes_equal_single_passes_and_oracle(mode):
+    import oracle
+    w = worldgen.terrain_world((11, 9, 6), seed=41, n_types=12)
+    lists, spec = _passes(w)
+    prev = random_prev(w, seed=42)
+    single, st_single = _run(w, lists, spec, prev, "single")
+    got, st = _run(w, lists, spec, prev, mode)
+    assert got.tobytes() == single.tobytes()
+    assert st == st_single
+    cur = prev
+    for l, s in zip(lists, spec):
+        cur, _, _ = oracle.radiance_pass(w, l, prev=cur, **s)
+    assert rel_err(got, cur).max() <= RTOL
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_passes_low_precision(precision):
+    w = worldgen.terrain_world((9, 8, 5), seed=43, n_types=10)
+    lists, spec = _passes(w)
+    prev = random_prev(w, seed=44)
+    single, st_single = _run(w, lists, spec, prev, "single", precision)
+    got, st = _run(w, lists, spec, prev, "multi", precision)
+    assert got.tobytes() == single.tobytes()
+    assert st == st_single
+
+
+def test_passes_split_into_launches_and_rounds():
+    """Passes larger than one shared march launch: 2^19 tasks each (one launch apiece) and 2^20
+    tasks (rounds, as a single pass runs), between smaller ones."""
+    w = worldgen.terrain_world((64, 64, 32), seed=45, n_types=24)
+    allp = worldgen.all_probes(w.dims)
+    small = worldgen.probe_subset(w.dims, 0.05, seed=46)
+    lists = [small, allp, allp, small, allp, small]
+    spec = [dict(rays=64), dict(rays=128), dict(rays=128), dict(rays=32), dict(rays=256), dict(rays=64)]
+    for i, s in enumerate(spec):
+        s.update(max_dist=48.0, blend=0.1, time_seed=i)
+    prev = random_prev(w, seed=47)
+    single, st_single = _run(w, lists, spec, prev, "single")
+    got, st = _run(w, lists, spec, prev, "multi")
+    assert got.tobytes() == single.tobytes()
+    assert st == st_single
+
+
+def test_passes_bad_arguments():
+    import lum_gb300
+    w = worldgen.terrain_world((4, 4, 4), seed=48)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        req = worldgen.all_probes(w.dims)
+        with pytest.raises(lum_gb300.LumRadError):
+            rw.radiance_passes([req], [lum_gb300.pass_params(rays=64, size=0)])
+        with pytest.raises(lum_gb300.LumRadError):
+            rw.radiance_passes([req], [lum_gb300.pass_params(rays=64, record_hits=True)])
+        with pytest.raises(lum_gb300.LumRadError):
+            rw.radiance_passes_resident([3], [lum_gb300.pass_params(rays=64)])
+        rw.radiance_passes([], [])   # nothing to do
+        rw.radiance_passes([req], [lum_gb300.pass_params(rays=64)])   # the context is still usable
+        assert rw.get_radiance().max() > 0.0
