@@ -55,6 +55,9 @@ CHUNK_TASKS = 1 << 18   # 32-ray tasks per march/finalize round of the library
 # finalize launches) in an ncu capture of this workload; ncu replays with cold caches
 # (march 1.23 + 46.12 MB, finalizes 118.31 + 0 MB)
 NCU_DRAM_BYTES_PER_STEP = 165.67e6
+# L2 bytes (lts__t_bytes.sum) of the same 9 launches in an ncu capture (march 644.4 MB,
+# finalizes 491.4 MB)
+NCU_L2_BYTES_PER_STEP = 1135.7e6
 
 
 def pass_lists(dims):
@@ -72,6 +75,30 @@ def load_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def l2_read_gbs(device: int) -> float:
+    """L2-resident read rate of this GPU, the reference for the path's L2 roofline: one kernel
+    summing 64 rows that are all the same 24 MiB float array (a stride-0 view: 1.5 GiB read from
+    a buffer well inside the 129 MB L2), best of 5 launches, CUDA events."""
+    import torch
+    n = 24 * 1024 * 1024 // 4
+    rows = 64
+    a = torch.rand(n, device=f"cuda:{device}")
+    v = a.expand(rows, n)
+    out = torch.empty(rows, device=a.device)
+    for _ in range(3):
+        torch.sum(v, dim=1, out=out)
+    best = 0.0
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.sum(v, dim=1, out=out)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 4.0 * n * rows / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return best
 
 
 class ClockSampler:
@@ -492,6 +519,7 @@ def main():
     single_total_ms = max_over_ranks(float(sum(single_ms)), pg, dev)
 
     hbm_peak, peak_kind = load_peaks()
+    l2_peak = l2_read_gbs(local)
     bytes_per_launch = float(np.sum(pass_bytes))       # the step's 8 passes: one march launch
     kern_avg_s = float(np.mean(kernel_ms)) / 1000.0    # march + 8 finalize launches of a step
     achieved = bytes_per_launch / kern_avg_s / 1e9
@@ -499,16 +527,21 @@ def main():
     # ---------------------------------------------------------------- end to end (e2e)
     rw2 = lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], device=local)
     rw2.load(world)
+    # the caller's request lists and result buffer in page-locked host memory
+    pinned = [torch.from_numpy(np.ascontiguousarray(l)).pin_memory() for l in lists]
+    host_lists = [t.numpy() for t in pinned]
+    out_t = torch.empty(world.grid.shape + (3,), dtype=torch.float32).pin_memory()
+    host_out = out_t.numpy()
     for _ in range(max(1, args.warmup)):
-        rw2.radiance_passes(lists, plist)
-        rw2.get_radiance()
+        rw2.radiance_passes(host_lists, plist)
+        rw2.get_radiance(out=host_out)
     e2e_s = 0.0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rw2.radiance_passes(lists, plist)
-        rw2.get_radiance()
+        rw2.radiance_passes(host_lists, plist)
+        rw2.get_radiance(out=host_out)
         e2e_s += time.perf_counter() - t0
     e2e_value = job_value(args.steps * rays_per_step, world_size, max_over_ranks(e2e_s, pg, dev))
     h2d = int(sum(l.shape[0] * 8 for l in lists))
@@ -540,6 +573,10 @@ def main():
                          "bytes_per_launch": bytes_per_launch, "kernel_ms_avg": kern_avg_s * 1e3,
                          "launch": "one step: a march launch over its 8 passes + 8 finalize launches",
                          "ray_steps_per_s": float(np.sum(pass_steps)) / kern_avg_s},
+            "l2_roofline": {"achieved": achieved, "peak": l2_peak, "unit": "GB/s", "frac": achieved / l2_peak,
+                            "peak_kind": "measured in this run: L2-resident read (64 row sums over one 24 MiB "
+                                         "array, one launch, best of 5)",
+                            "traffic": NCU_L2_BYTES_PER_STEP},
             "single_pass": {"value": job_value(args.steps * rays_per_step, world_size, single_total_ms / 1000.0),
                             "unit": "probe-rays/s", "ms_per_step": single_total_ms / args.steps,
                             "kernel_ms_per_pass": float(np.mean(single_kernel_ms)) / PASSES,

@@ -104,9 +104,14 @@ class RadianceWorld:
         self.upload_material_palette()
 
     # ---- radiance volume
-    def get_radiance(self) -> np.ndarray:
+    def get_radiance(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The volume as (Z, Y, X, 3) float32; into `out` if given (a page-locked `out`, e.g. a
+        pinned torch tensor's numpy view, receives the device copy directly)."""
         X, Y, Z = self.dims
-        out = np.empty((Z, Y, X, 3), dtype=np.float32)
+        if out is None:
+            out = np.empty((Z, Y, X, 3), dtype=np.float32)
+        elif out.dtype != np.float32 or out.size != 3 * self.n_blocks or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float32 array of (Z, Y, X, 3) values")
         check(self.lib.lumrad_get_radiance(self.h, ptr(out)))
         return out
 

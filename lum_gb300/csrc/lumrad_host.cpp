@@ -817,21 +817,35 @@ int lumrad_upload_material_palette(LumRadContext ctx) {
     return LUMRAD_OK;
 }
 
+// Whether [p, p + bytes) lies in page-locked host memory (cudaMallocHost / cudaHostRegister).
+static bool host_pinned(const void* p, size_t bytes) {
+    for (const void* q : {p, static_cast<const void*>(static_cast<const char*>(p) + bytes - 1)}) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
 int lumrad_get_radiance(LumRadContext ctx, float* rgb) {
     Context* c = as_ctx(ctx);
     if (!c || !rgb) return fail(LUMRAD_EINVAL, "null argument");
     LUMRAD_TRY(cudaSetDevice(c->device));
     DeviceWorld& w = c->world;
-    // packed to RGB floats on the device (FP16/BF16 widened exactly), one copy through pinned memory
-    if (!c->d_rgb) {
-        LUMRAD_TRY(cudaMalloc(&c->d_rgb, w.W * 3 * sizeof(float)));
-        LUMRAD_TRY(cudaMallocHost(&c->h_rgb, w.W * 3 * sizeof(float)));
-    }
+    const size_t bytes = w.W * 3 * sizeof(float);
+    // packed to RGB floats on the device (FP16/BF16 widened exactly); one copy, straight into the
+    // caller's array when it is page-locked, else through the context's pinned buffer
+    const bool direct = host_pinned(rgb, bytes);
+    if (!c->d_rgb) LUMRAD_TRY(cudaMalloc(&c->d_rgb, bytes));
+    if (!direct && !c->h_rgb) LUMRAD_TRY(cudaMallocHost(&c->h_rgb, bytes));
     LUMRAD_TRY(launch_pack_rgb(w.d_rad[w.cur], w.precision, (long long)w.W, c->d_rgb, c->stream));
-    LUMRAD_TRY(cudaMemcpyAsync(c->h_rgb, c->d_rgb, w.W * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(direct ? rgb : c->h_rgb, c->d_rgb, bytes, cudaMemcpyDeviceToHost, c->stream));
     LUMRAD_TRY(cudaMemcpyAsync(c->h_err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));   // one wait for the volume and the error word
-    std::memcpy(rgb, c->h_rgb, w.W * 3 * sizeof(float));
+    if (!direct) std::memcpy(rgb, c->h_rgb, bytes);
     return c->have_pass ? c->handle_error(*c->h_err) : LUMRAD_OK;
 }
 

@@ -111,3 +111,21 @@ def test_passes_bad_arguments():
         rw.radiance_passes([], [])   # nothing to do
         rw.radiance_passes([req], [lum_gb300.pass_params(rays=64)])   # the context is still usable
         assert rw.get_radiance().max() > 0.0
+
+
+def test_read_back_into_pinned_buffer():
+    """get_radiance into a page-locked array (copied to directly) equals the staged read-back."""
+    import torch
+    import lum_gb300
+    w = worldgen.terrain_world((7, 6, 5), seed=49)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        rw.radiance_passes([worldgen.all_probes(w.dims)] * 2,
+                           [lum_gb300.pass_params(rays=64, blend=0.2, time_seed=s) for s in (1, 2)])
+        staged = rw.get_radiance()
+        t = torch.zeros(w.grid.shape + (3,), dtype=torch.float32).pin_memory()
+        got = rw.get_radiance(out=t.numpy())
+        assert got.tobytes() == staged.tobytes()
+        assert t.numpy().tobytes() == staged.tobytes()
+        with pytest.raises(ValueError):
+            rw.get_radiance(out=np.zeros(3, np.float32))
