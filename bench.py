@@ -527,9 +527,11 @@ def main():
     # ---------------------------------------------------------------- end to end (e2e)
     rw2 = lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], device=local)
     rw2.load(world)
-    # the caller's request lists and result buffer in page-locked host memory
-    pinned = [torch.from_numpy(np.ascontiguousarray(l)).pin_memory() for l in lists]
-    host_lists = [t.numpy() for t in pinned]
+    # the caller's request lists (back to back in one array) and result buffer in page-locked
+    # host memory
+    pinned = torch.from_numpy(np.concatenate(lists)).pin_memory()
+    cuts = np.cumsum([0] + [l.shape[0] for l in lists])
+    host_lists = [pinned.numpy()[cuts[i]:cuts[i + 1]] for i in range(PASSES)]
     out_t = torch.empty(world.grid.shape + (3,), dtype=torch.float32).pin_memory()
     host_out = out_t.numpy()
     for _ in range(max(1, args.warmup)):

@@ -819,6 +819,7 @@ int lumrad_upload_material_palette(LumRadContext ctx) {
 
 // Whether [p, p + bytes) lies in page-locked host memory (cudaMallocHost / cudaHostRegister).
 static bool host_pinned(const void* p, size_t bytes) {
+    if (bytes == 0) return false;
     for (const void* q : {p, static_cast<const void*>(static_cast<const char*>(p) + bytes - 1)}) {
         cudaPointerAttributes a;
         if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
@@ -1087,12 +1088,41 @@ int lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, co
     if (n == 0) return LUMRAD_OK;
     LUMRAD_TRY(cudaSetDevice(c->device));
     if ((rc = check_unowned(c))) return rc;
-    // every list in one pinned buffer and one copy
     if ((rc = c->ensure_req_capacity(total))) return rc;
     if (c->req_copy_pending) {
         LUMRAD_TRY(cudaEventSynchronize(c->ev_req));
         c->req_copy_pending = false;
     }
+    std::vector<const short4*> reqs((size_t)n);
+    // Page-locked lists and an idle stream: DMA straight from the caller's arrays (one copy per
+    // run of adjacent lists), launch, and return once the copies (not the passes) are done.
+    const cudaError_t idle = cudaStreamQuery(c->stream);
+    if (idle == cudaErrorNotReady) cudaGetLastError();   // a busy stream is no error for later checks
+    bool direct = total > 0 && idle == cudaSuccess;
+    for (int i = 0; direct && i < n; i++)
+        direct = counts[i] == 0 || host_pinned(requests[i], (size_t)counts[i] * 4 * sizeof(int16_t));
+    if (direct) {
+        size_t off = 0;
+        int i = 0;
+        while (i < n) {
+            if (counts[i] == 0) { reqs[i++] = c->d_req + off; continue; }
+            const int16_t* src = requests[i];
+            const size_t first = off;
+            int j = i;
+            while (j < n && (counts[j] == 0 || requests[j] == src + (off - first) * 4)) {
+                reqs[j] = c->d_req + off;
+                off += (size_t)counts[j++];
+            }
+            LUMRAD_TRY(cudaMemcpyAsync(c->d_req + first, src, (off - first) * sizeof(short4), cudaMemcpyHostToDevice,
+                                       c->stream));
+            i = j;
+        }
+        LUMRAD_TRY(cudaEventRecord(c->ev_req, c->stream));
+        rc = c->run_passes(reqs.data(), counts, params, n);
+        LUMRAD_TRY(cudaEventSynchronize(c->ev_req));
+        return rc;
+    }
+    // else every list through one pinned buffer and one copy
     if (total > c->h_req_cap) {
         if (c->h_req_pinned) cudaFreeHost(c->h_req_pinned);
         c->h_req_pinned = nullptr;
@@ -1101,7 +1131,6 @@ int lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, co
         LUMRAD_TRY(cudaMallocHost(&c->h_req_pinned, cap * 4 * sizeof(int16_t)));
         c->h_req_cap = cap;
     }
-    std::vector<const short4*> reqs((size_t)n);
     size_t off = 0;
     for (int i = 0; i < n; i++) {
         if (counts[i] > 0) std::memcpy(c->h_req_pinned + off * 4, requests[i], (size_t)counts[i] * 4 * sizeof(int16_t));

@@ -288,18 +288,22 @@ __device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchVi
             rec.fraction = canon_nan(fr);
         }
     } else {
-        // sky and sun (radiance.comp:334-343); globalLightDir = normalize(0.5, 0.5, -0.9)
-        const float3 gl = normalize3(make_float3(0.5f, 0.5f, -0.9f));
-        const float g = -fadd(fadd(fmul(d.x, gl.x), fmul(d.y, gl.y)), fmul(d.z, gl.z));
+        // sky and sun (radiance.comp:334-343).  Constants, each the FP32 round-to-nearest result
+        // of the shader's expression (normalize3 above on (0.5, 0.5, -0.9), then the products):
+        //   globalLightDir = (kGl, kGl, kGlz);  0.9*3 = kSun, 0.6*3 = kSunB;  0.1*(0.53, 0.81, 0.92)
+        constexpr unsigned kGl = 0x3edfab13u, kGlz = 0xbf494d2au, kSun = 0x402cccccu, kSunB = 0x3fe66667u;
+        constexpr unsigned kSkyR = 0x3d591687u, kSkyG = 0x3da5e354u, kSkyB = 0x3dbc6a7fu;
+        const float gl = __uint_as_float(kGl);
+        const float g = -fadd(fadd(fmul(d.x, gl), fmul(d.y, gl)), fmul(d.z, __uint_as_float(kGlz)));
         light = make_float3(0.0f, 0.0f, 0.0f);
         if (g > 0.95f) {
-            light.x = fadd(light.x, fmul(g, fmul(0.9f, 3.0f)));
-            light.y = fadd(light.y, fmul(g, fmul(0.9f, 3.0f)));
-            light.z = fadd(light.z, fmul(g, fmul(0.6f, 3.0f)));
+            light.x = fadd(light.x, fmul(g, __uint_as_float(kSun)));
+            light.y = fadd(light.y, fmul(g, __uint_as_float(kSun)));
+            light.z = fadd(light.z, fmul(g, __uint_as_float(kSunB)));
         }
-        light.x = fadd(light.x, fmul(0.53f, 0.1f));
-        light.y = fadd(light.y, fmul(0.81f, 0.1f));
-        light.z = fadd(light.z, fmul(0.92f, 0.1f));
+        light.x = fadd(light.x, __uint_as_float(kSkyR));
+        light.y = fadd(light.y, __uint_as_float(kSkyG));
+        light.z = fadd(light.z, __uint_as_float(kSkyB));
     }
     if (RECORD) w.hits[gr] = rec;
     return light;

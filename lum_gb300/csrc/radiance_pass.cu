@@ -6,7 +6,7 @@
 //   march_kernel     persistent warps take tasks from a queue in guided chunks (large early,
 //                    single tasks at the end).  A warp sets up a task's 32 rays in lock step
 //                    (hash seeds, direction, origin, 1/direction) into one half of a 64-ray ring
-//                    in shared memory.  Its lanes march in a flat loop, one coarse step per
+//                    in shared memory.  Its lanes march in a flat loop, two coarse steps per
 //                    iteration; a lane whose ray ends writes (fraction, info) and takes the next
 //                    ray in ring order.  A half is set up again as soon as its rays are handed
 //                    out, so lanes never wait for each other.
@@ -183,46 +183,52 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         }
         // 3. march; leave to set up more when a ring half is free and tasks may remain
         while (true) {
+            // two coarse steps per iteration (a lane whose ray ends in the first takes no second):
+            // the warp's vote and hand-out below run once per two steps
             bool fin = false;
-            if (my >= 0) {
-                frac = fadd(frac, 0.5f);
-                steps++;
-                const float px = fadd(ox, fmul(dx, frac));
-                const float py = fadd(oy, fmul(dy, frac));
-                const float pz = fadd(oz, fmul(dz, frac));
-                const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
-                int cid;
-                const bool solid = solid_at(mv, ix, iy, iz, cid);
-                if (cid == 0) {
-                    // empty block: skip to its far corner (radiance.comp:215-226)
-                    const float bx = fadd((float)((ix / 16) * 16), cx);
-                    const float by = fadd((float)((iy / 16) * 16), cy);
-                    const float bz = fadd((float)((iz / 16) * 16), cz);
-                    const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
-                    const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
-                    const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
-                    frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
-                }
-                uint32_t info = 0;
-                if (solid) {
-                    fin = true;
-                    info = (uint32_t)steps | (1u << 24);
-                } else if (px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz || frac >= max_dist) {
-                    fin = true;
-                    info = (uint32_t)steps;
-                } else if (steps >= max_steps) {
-                    fin = true;
-                    info = (uint32_t)steps | (1u << 25);
-                }
-                if (fin) {
-                    if (RECORD) {
-                        int blk;
-                        const int v = voxel_value(*wp, ix, iy, iz, blk);
-                        if (solid) info |= (uint32_t)v << 16;
-                        la.ray_blk[my] = blk;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                if (my >= 0) {
+                    frac = fadd(frac, 0.5f);
+                    steps++;
+                    const float px = fadd(ox, fmul(dx, frac));
+                    const float py = fadd(oy, fmul(dy, frac));
+                    const float pz = fadd(oz, fmul(dz, frac));
+                    const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
+                    int cid;
+                    const bool solid = solid_at(mv, ix, iy, iz, cid);
+                    if (cid == 0) {
+                        // empty block: skip to its far corner (radiance.comp:215-226)
+                        const float bx = fadd((float)((ix / 16) * 16), cx);
+                        const float by = fadd((float)((iy / 16) * 16), cy);
+                        const float bz = fadd((float)((iz / 16) * 16), cz);
+                        const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
+                        const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
+                        const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
+                        frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
                     }
-                    __stcg(la.ray_res + my, make_uint2(__float_as_uint(frac), info));
-                    my = -1;
+                    uint32_t info = 0;
+                    if (solid) {
+                        fin = true;
+                        info = (uint32_t)steps | (1u << 24);
+                    } else if (px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz ||
+                               frac >= max_dist) {
+                        fin = true;
+                        info = (uint32_t)steps;
+                    } else if (steps >= max_steps) {
+                        fin = true;
+                        info = (uint32_t)steps | (1u << 25);
+                    }
+                    if (fin) {
+                        if (RECORD) {
+                            int blk;
+                            const int v = voxel_value(*wp, ix, iy, iz, blk);
+                            if (solid) info |= (uint32_t)v << 16;
+                            la.ray_blk[my] = blk;
+                        }
+                        __stcg(la.ray_res + my, make_uint2(__float_as_uint(frac), info));
+                        my = -1;
+                    }
                 }
             }
             const unsigned fm = __ballot_sync(kFull, fin);
@@ -281,12 +287,8 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
         L = butterfly_sum(L);
         v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
         // counters: lookups and hits of this task, summed per CTA below
-        unsigned a = lookups, h = (res.y >> 24) & 1u;
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) {
-            a += __shfl_xor_sync(kFull, a, m);
-            h += __shfl_xor_sync(kFull, h, m);
-        }
+        const unsigned a = __reduce_add_sync(kFull, lookups);
+        const unsigned h = __popc(__ballot_sync(kFull, (res.y >> 24) & 1u));
         if (lane == 0) {
             s_stat[w][0] = a;
             s_stat[w][1] = h;

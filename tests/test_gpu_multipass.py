@@ -129,3 +129,28 @@ def test_read_back_into_pinned_buffer():
         assert t.numpy().tobytes() == staged.tobytes()
         with pytest.raises(ValueError):
             rw.get_radiance(out=np.zeros(3, np.float32))
+
+
+def test_page_locked_lists():
+    """Lists in page-locked memory (adjacent in one array, apart, or mixed with pageable ones) are
+    copied straight from the caller's arrays; the volume equals the staged copies' one."""
+    import torch
+    import lum_gb300
+    w = worldgen.terrain_world((9, 7, 5), seed=50)
+    lists = [worldgen.probe_subset(w.dims, f, seed=51, stream=i) for i, f in enumerate((0.4, 0.0, 0.8, 0.5))]
+    params = [lum_gb300.pass_params(rays=64, blend=0.1, time_seed=20 + i) for i in range(4)]
+    flat = torch.from_numpy(np.concatenate(lists)).pin_memory()
+    cuts = np.cumsum([0] + [l.shape[0] for l in lists])
+    adjacent = [flat.numpy()[cuts[i]:cuts[i + 1]] for i in range(4)]
+    apart_t = [torch.from_numpy(l.copy()).pin_memory() for l in lists]
+    apart = [t.numpy() for t in apart_t]
+    mixed = [apart[0], lists[1], apart[2], lists[3]]
+    out = []
+    for ls in (lists, adjacent, apart, mixed):
+        with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+            rw.load(w)
+            rw.radiance_passes(ls, params)
+            rw.radiance_passes(ls, params)   # the stream busy or idle: either copy path
+            out.append(rw.get_radiance())
+    for o in out[1:]:
+        assert o.tobytes() == out[0].tobytes()

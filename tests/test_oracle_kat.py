@@ -192,3 +192,21 @@ def test_f64_oracle_keeps_fp32_traversal():
     b, hb, _ = oracle.radiance_pass(w, req, rays=64, blend=0.1, record_hits=True, precision="f64")
     assert ha.tobytes() == hb.tobytes()
     assert np.max(np.abs(a - b)) < 1e-5
+
+
+def test_sky_constants_of_the_kernels():
+    """The kernels' sky/sun constants (hex literals in radiance_device.cuh) are the FP32
+    round-to-nearest values of the shader's expressions (radiance.comp:334-343):
+    normalize(0.5, 0.5, -0.9) as v * (1 / sqrt(dot(v, v))), 0.9*3, 0.6*3 and 0.1*(0.53, 0.81, 0.92)."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(__file__), "..", "lum_gb300", "csrc", "radiance_device.cuh")).read()
+    consts = {k: int(v, 16) for k, v in re.findall(r"(k[A-Za-z]+) = 0x([0-9a-f]+)u", src)}
+    f = np.float32
+    v = (f(0.5), f(0.5), f(-0.9))
+    dd = f(f(f(v[0] * v[0]) + f(v[1] * v[1])) + f(v[2] * v[2]))
+    s = f(f(1.0) / f(np.sqrt(dd)))
+    want = {"kGl": f(v[0] * s), "kGlz": f(v[2] * s), "kSun": f(f(0.9) * f(3.0)), "kSunB": f(f(0.6) * f(3.0)),
+            "kSkyR": f(f(0.53) * f(0.1)), "kSkyG": f(f(0.81) * f(0.1)), "kSkyB": f(f(0.92) * f(0.1))}
+    for k, x in want.items():
+        assert consts[k] == int(np.array(x, dtype=np.float32).view(np.uint32)), k
