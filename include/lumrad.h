@@ -196,7 +196,10 @@ int  lumrad_radiance_pass_resident(LumRadContext ctx, int slot, const LumRadPass
  * so the marches of consecutive passes share one launch (their rays wait in device memory) and
  * each pass's shading/blend then runs in order on its predecessor's volume.  Every params[i]
  * needs size >= 1 and record_hits 0.  Afterwards lumrad_get_pass_stats sums probes, rays, steps
- * and hits over the n passes and lumrad_get_kernel_times has one entry for the whole call. */
+ * and hits over the n passes (gpu_ms: the whole call), lumrad_get_kernel_times has one entry for
+ * the whole call, and adaptive slicing (size 0 in lumrad_update_radiance) takes the call's time
+ * per pass as the last frame's.  Page-locked lists are copied straight from the caller's arrays
+ * when the context's stream is idle (the call returns once they are copied). */
 int  lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, const int* counts,
                             const LumRadPassParams* params, int n);
 /* The same over resident lists (slots[i] for pass i). */

@@ -439,6 +439,7 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream));
     LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
     last_slot = slot;
+    last_slot_passes = 1;
     n_passes++;
     world.cur = 1 - world.cur;
     have_pass = true;
@@ -547,6 +548,7 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     }
     LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
     last_slot = slot;
+    last_slot_passes = n;
     n_passes++;
     frame += n;
     have_pass = true;
@@ -949,6 +951,7 @@ int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
     if (params->size == 0 && c->have_pass) {
         LUMRAD_TRY(cudaEventSynchronize(c->ring1[c->last_slot]));
         LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
+        c->last_ms /= (float)c->last_slot_passes;   // a frame's pass time after a several-pass call
     }
     if ((rc = check_unowned(c))) return rc;
     // a frame of Renderer::submitFrame: shift_radiance, then update_radiance (renderer.cpp:436-438)

@@ -132,7 +132,8 @@ struct Context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_req = nullptr;
     cudaEvent_t ring0[kRing] = {}, ring1[kRing] = {};   // around each pass's kernels
-    int last_slot = 0;                    // ring entry of the last pass
+    int last_slot = 0;                    // ring entry of the last pass (or several-pass call)
+    int last_slot_passes = 1;             // passes that entry covers
     int* h_err = nullptr;                 // pinned copy of the error word
     long long n_passes = 0;
     bool have_pass = false;
