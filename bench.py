@@ -50,7 +50,7 @@ MAX_DIST = 256.0
 BLEND = 0.1
 SEED = 1234
 S_R = 12            # bytes of FP32 RGB radiance per probe
-CHUNK_TASKS = 1 << 18   # 32-ray tasks per march/finalize round of the library
+BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches) in an ncu capture of this workload; ncu replays with cold caches
 # (march 1.23 + 46.12 MB, finalizes 118.31 + 0 MB)
@@ -256,7 +256,7 @@ def batched_leg(local: int, steps: int, warmup: int, flush):
                 "plain_value": plain, "plain_ms_per_step": float(np.mean(pms)),
                 "speedup_vs_plain": batched / plain, "steps": steps,
                 "ray_steps_per_s": st["steps"] / (ms[-1] / 1000.0),
-                "gpu_launches_per_step": 1 + 2 * -(-tasks // CHUNK_TASKS)})
+                "gpu_launches_per_step": 1 + 2 * -(-tasks // BATCH_ROUND_TASKS)})
     return out
 
 

@@ -90,7 +90,7 @@ int build(Batch* b) {
     }
     if (begin >= (1LL << 31)) return fail(LUMRAD_EINVAL, "batch has too many subgroups (>= 2^31)");
     b->n_tasks = begin;
-    const size_t need = (size_t)std::min<long long>(std::max<long long>(begin, 1), kChunkTasks) * kTaskRays;
+    const size_t need = (size_t)std::min<long long>(std::max<long long>(begin, 1), kBatchRoundTasks) * kTaskRays;
     if (need > b->ray_cap) {
         cudaFree(b->d_ray_res);
         b->d_ray_res = nullptr;
@@ -108,6 +108,7 @@ int build(Batch* b) {
         la.queue = b->d_queue;
         la.error = b->d_error;
         la.ray_res = b->d_ray_res;
+        la.round_tasks = kBatchRoundTasks;
         la.guided_div = b->tuning.guided_div;
         la.max_chunk = b->tuning.max_chunk;
         la.march_ctas = b->tuning.march_ctas;

@@ -8,12 +8,19 @@ namespace lumrad {
 
 // Warps per CTA of the pass kernels.
 constexpr int kWarps = 8;
+// Warps (one task each) per finalize CTA; a divisor of kWarps, since worlds of a batch start at
+// multiples of kWarps tasks
+constexpr int kFinWarps = 8;
+static_assert(kWarps % kFinWarps == 0, "finalize CTAs must not straddle worlds");
 // A task is one 32-ray subgroup of one probe (the unit radiance.comp sums with subgroupAdd).
 constexpr int kTaskRays = 32;
 // Tasks per march/finalize round: the per-ray buffer between the two kernels holds this many
 // tasks' rays (8 B per ray: 67 MB, L2-resident on GB300).  Fewer, larger rounds shorten the
 // march kernel's tails (measured: 2^18 tasks 13% faster than 2^16 on many small worlds).
 constexpr int kChunkTasks = 1 << 18;
+// Round size of batches: their task spaces are large, and two rounds of 2^20 tasks (402 MB of ray
+// results, past the L2) beat seven of 2^18 by 2% on 256 mixed worlds (fewer queue drains)
+constexpr int kBatchRoundTasks = 1 << 20;
 // Tasks of one march launch over several passes of a context (their rays, 8 B each, are kept
 // until the passes' finalize launches: 2^19 tasks = 134 MB, about the L2)
 constexpr int kMultiTasks = 1 << 19;
@@ -68,6 +75,7 @@ struct LaunchArgs {
     uint2* ray_res;              // per ray of the round: coarse fraction bits, info word
     int* ray_blk;                // per ray of the round: block id at the last coarse step (records)
     int ray_origin;              // task whose rays start ray_res (the march launch's chunk_begin)
+    int round_tasks;             // tasks per march/finalize round (0: kChunkTasks); ray_res holds one round
     // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
     // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
     int guided_div, max_chunk, march_ctas;

@@ -251,20 +251,20 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
 
 // ---------------------------------------------------------------- finalize kernel
 template <class Store, bool RECORD>
-__global__ void __launch_bounds__(kWarps * 32, 4)
+__global__ void __launch_bounds__(kFinWarps * 32, 32 / kFinWarps)
 finalize_kernel(const __grid_constant__ LaunchArgs la) {
-    __shared__ float4 s_mean[kWarps];
-    __shared__ int s_count[kWarps];
-    __shared__ unsigned s_stat[kWarps][2];
+    __shared__ float4 s_mean[kFinWarps];
+    __shared__ int s_count[kFinWarps];
+    __shared__ unsigned s_stat[kFinWarps][2];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
-    if (threadIdx.x < kWarps) {
+    if (threadIdx.x < kFinWarps) {
         s_count[threadIdx.x] = 0;
         s_stat[threadIdx.x][0] = 0;
         s_stat[threadIdx.x][1] = 0;
     }
     __syncthreads();
-    const int t0 = la.chunk_begin + (int)blockIdx.x * kWarps;   // worlds start at multiples of 8
+    const int t0 = la.chunk_begin + (int)blockIdx.x * kFinWarps;   // worlds start at multiples of 8
     const int t = t0 + w;
     const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
     const int t_local = t - (int)wp->task_begin;
@@ -273,7 +273,7 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     const int g = t_local / nsub;
     const int k = t_local - g * nsub;
     // a probe's subgroups share this CTA when R/32 divides 8 (task_begin is a multiple of 8)
-    const bool local = nsub > 1 && (kWarps % nsub) == 0 && (wp->task_begin % kWarps) == 0;
+    const bool local = nsub > 1 && (kFinWarps % nsub) == 0 && (wp->task_begin % kFinWarps) == 0;
     float3 v = make_float3(0.0f, 0.0f, 0.0f);
     if (valid) {
         const long long idx = (long long)(t - la.ray_origin) * kTaskRays + lane;
@@ -322,7 +322,7 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long a = 0, h = 0;
-        for (int j = 0; j < kWarps; j++) {
+        for (int j = 0; j < kFinWarps; j++) {
             a += s_stat[j][0];
             h += s_stat[j][1];
         }
@@ -346,13 +346,14 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
     const int blocks = march_grid(RECORD, num_sms, a.march_ctas);
     LaunchArgs args = a;
     args.total_warps = blocks * kWarps;
-    for (long long c0 = 0; c0 < a.n_tasks; c0 += kChunkTasks) {
+    const long long round = a.round_tasks > 0 ? a.round_tasks : kChunkTasks;
+    for (long long c0 = 0; c0 < a.n_tasks; c0 += round) {
         args.chunk_begin = (int)c0;
-        args.chunk_end = (int)min(c0 + (long long)kChunkTasks, a.n_tasks);
+        args.chunk_end = (int)min(c0 + round, a.n_tasks);
         args.ray_origin = args.chunk_begin;
         const int n = args.chunk_end - args.chunk_begin;
         march_kernel<RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
-        finalize_kernel<Store, RECORD><<<(n + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(args);
+        finalize_kernel<Store, RECORD><<<(n + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, stream>>>(args);
     }
     return cudaGetLastError();
 }
@@ -375,7 +376,7 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
         args.chunk_begin = (int)w.task_begin;
         args.chunk_end = (int)(w.task_begin + w.n_tasks);
         const int n = args.chunk_end - args.chunk_begin;
-        finalize_kernel<Store, false><<<(n + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(args);
+        finalize_kernel<Store, false><<<(n + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, stream>>>(args);
     }
     return cudaGetLastError();
 }
@@ -656,7 +657,7 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
         la.ray_origin = la.chunk_begin;
         const int tasks = la.chunk_end - la.chunk_begin;
         march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(la);
-        finalize_kernel<StoreF32, false><<<(tasks + kWarps - 1) / kWarps, kWarps * 32, 0, stream>>>(la);
+        finalize_kernel<StoreF32, false><<<(tasks + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, stream>>>(la);
     }
     LUMRAD_TRY(cudaGetLastError());
     return LUMRAD_OK;

@@ -53,7 +53,7 @@ def test_demo_step_is_deterministic():
 
 
 def test_full_batch_equals_worlds_one_by_one():
-    """The 256-world mixed batch (58.6M rays, 7 rounds) equals each world's own pass."""
+    """The 256-world mixed batch (58.6M rays, 2 rounds) equals each world's own pass."""
     import lum_gb300
     mix = worldgen.mixed_worlds(n=256, seed=SEED)
 
