@@ -205,7 +205,7 @@ BATCH_WORKLOAD = {
 }
 
 
-def batched_leg(local: int, steps: int, warmup: int, flush):
+def batched_leg(local: int, steps: int, warmup: int, flush, tuning=None):
     """Mixed-size workload: one autotuned batch (one graph replay per step, all 256 worlds in the
     same persistent launches) against the plain path (one pass per world, each world alone)."""
     import torch
@@ -225,7 +225,11 @@ def batched_leg(local: int, steps: int, warmup: int, flush):
         for i, (w, req, r) in enumerate(mix):
             b.set_requests(i, req, lum_gb300.pass_params(rays=r, max_dist=128.0, blend=0.1))
         t0 = time.perf_counter()
-        tuning = b.autotune(repeats=3)
+        if tuning is None:
+            tuning = b.autotune(repeats=3)
+        else:   # fixed settings (profiling captures): guided divisor, chunk cap, march CTAs per SM
+            b.set_tuning(*tuning)
+            tuning = {"guided_div": tuning[0], "max_chunk": tuning[1], "march_ctas": tuning[2], "fixed": True}
         out["tuning"] = dict(tuning, seconds=round(time.perf_counter() - t0, 2))
         for k in range(warmup):
             b.run(k)
@@ -421,6 +425,9 @@ def main():
                     help="comma list of legs: demo (the headline line), batched (the mixed-size batch), "
                          "serving (relight requests)")
     ap.add_argument("--serve-requests", type=int, default=10000, help="requests per arrival rate (serving leg)")
+    ap.add_argument("--batch-tuning", default=None, type=lambda s: tuple(int(x) for x in s.split(",")),
+                    help="fixed batch settings G,C,M (guided divisor, chunk cap, march CTAs per SM) instead of "
+                         "the autotuner (for profiling captures)")
     args = ap.parse_args()
     legs = set(args.legs.split(","))
     rank, local, world_size, pg = dist_setup(args)
@@ -436,7 +443,7 @@ def main():
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
         out = {"diagnostics": True}
         if "batched" in legs:
-            out["batched"] = batched_leg(local, max(3, args.steps // 2), args.warmup, flush)
+            out["batched"] = batched_leg(local, max(3, args.steps // 2), args.warmup, flush, args.batch_tuning)
         if "serving" in legs:
             out["serving"] = serving_leg(local, n_requests=args.serve_requests)
         if rank == 0:
@@ -551,7 +558,7 @@ def main():
 
     batched = None
     if "batched" in legs:
-        batched = batched_leg(local, max(3, args.steps // 2), args.warmup, flush)
+        batched = batched_leg(local, max(3, args.steps // 2), args.warmup, flush, args.batch_tuning)
     serving = None
     if "serving" in legs:
         serving = serving_leg(local, n_requests=args.serve_requests)
