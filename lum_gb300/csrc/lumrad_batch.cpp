@@ -109,6 +109,7 @@ int build(Batch* b) {
         la.error = b->d_error;
         la.ray_res = b->d_ray_res;
         la.round_tasks = kBatchRoundTasks;
+        la.in_cta = combines_in_cta(b->h_table[k], nw) ? 1 : 0;
         la.guided_div = b->tuning.guided_div;
         la.max_chunk = b->tuning.max_chunk;
         la.march_ctas = b->tuning.march_ctas;
@@ -140,7 +141,7 @@ int check_batch_error(Batch* b) {
         cudaMemsetAsync(b->d_error, 0, sizeof(int), b->stream);
         cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(unsigned long long), b->stream);
         cudaStreamSynchronize(b->stream);
-        return fail(LUMRAD_EDEVICE, "radiance kernel scheduler stopped making progress");
+        return fail(LUMRAD_EDEVICE, "radiance kernel reported an error (code " + std::to_string(e) + ")");
     }
     return LUMRAD_OK;
 }

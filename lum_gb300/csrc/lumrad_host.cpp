@@ -403,7 +403,9 @@ int Context::handle_error(int e) {
         cudaMemsetAsync(d_queue, 0, 2 * sizeof(unsigned long long), stream);
         cudaMemsetAsync(world.d_probe_count, 0, world.count_cap * sizeof(int), stream);
         cudaStreamSynchronize(stream);
-        return fail(LUMRAD_EDEVICE, "radiance kernel scheduler stopped making progress (code " + std::to_string(e) + ")");
+        return fail(LUMRAD_EDEVICE, std::string(e & 1 ? "radiance kernel scheduler stopped making progress" :
+                                                "finalize kernel without the cross-CTA combine got a probe spanning CTAs") +
+                                        " (code " + std::to_string(e) + ")");
     }
     return LUMRAD_OK;
 }

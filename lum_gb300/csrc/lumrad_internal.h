@@ -76,10 +76,22 @@ struct LaunchArgs {
     int* ray_blk;                // per ray of the round: block id at the last coarse step (records)
     int ray_origin;              // task whose rays start ray_res (the march launch's chunk_begin)
     int round_tasks;             // tasks per march/finalize round (0: kChunkTasks); ray_res holds one round
+    int in_cta;                  // table launches: 1 if combines_in_cta holds for every world (the lean
+                                 // finalize kernel), 0 for the general one
     // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
     // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
     int guided_div, max_chunk, march_ctas;
 };
+
+// Whether every probe of these worlds combines its subgroup means inside one finalize CTA: R/32
+// divides kFinWarps and the world's tasks start at a multiple of kFinWarps.
+inline bool combines_in_cta(const WorldPass* w, int n) {
+    for (int i = 0; i < n; i++) {
+        const int nsub = w[i].R / 32;
+        if (nsub > 1 && (kFinWarps % nsub != 0 || w[i].task_begin % kFinWarps != 0)) return false;
+    }
+    return true;
+}
 
 // Tunable scheduling of a launch (see LaunchArgs); the defaults are 2, 16 and the occupancy limit.
 struct Tuning {

@@ -449,6 +449,7 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     la.queue = sl.d_queue;
     la.error = sl.d_error;
     la.ray_res = sl.d_ray_res;
+    la.in_cta = combines_in_cta(table, nl) ? 1 : 0;
     la.guided_div = sv->tuning.guided_div;
     la.max_chunk = sv->tuning.max_chunk;
     la.march_ctas = sv->tuning.march_ctas;
