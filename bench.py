@@ -53,11 +53,11 @@ S_R = 12            # bytes of FP32 RGB radiance per probe
 BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches) in an ncu capture of this workload; ncu replays with cold caches
-# (march 1.23 + 46.12 MB, finalizes 118.31 + 0 MB)
-NCU_DRAM_BYTES_PER_STEP = 165.67e6
-# L2 bytes (lts__t_bytes.sum) of the same 9 launches in an ncu capture (march 644.4 MB,
-# finalizes 491.4 MB)
-NCU_L2_BYTES_PER_STEP = 1135.7e6
+# (march 1.08 + 46.01 MB, finalizes 118.24 + 0 MB)
+NCU_DRAM_BYTES_PER_STEP = 165.32e6
+# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 636.2 MB,
+# finalizes 987.9 MB)
+NCU_L2_BYTES_PER_STEP = 1624.0e6
 
 
 def pass_lists(dims):
