@@ -139,7 +139,7 @@ int check_batch_error(Batch* b) {
     LUMRAD_TRY(cudaStreamSynchronize(b->stream));
     if (e != 0) {
         cudaMemsetAsync(b->d_error, 0, sizeof(int), b->stream);
-        cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(unsigned long long), b->stream);
+        cudaMemsetAsync(b->d_queue, 0, kQueueWords * sizeof(unsigned long long), b->stream);
         cudaStreamSynchronize(b->stream);
         return fail(LUMRAD_EDEVICE, "radiance kernel reported an error (code " + std::to_string(e) + ")");
     }
@@ -216,9 +216,9 @@ int lumrad_batch_create(LumRadContext const* worlds, int n_worlds, LumRadBatch* 
             LUMRAD_TRY(cudaMallocHost(&b->h_table[k], n_worlds * sizeof(WorldPass)));
             LUMRAD_TRY(cudaMalloc(&b->d_table[k], n_worlds * sizeof(WorldPass)));
         }
-        LUMRAD_TRY(cudaMalloc(&b->d_queue, 2 * sizeof(unsigned long long)));
+        LUMRAD_TRY(cudaMalloc(&b->d_queue, kQueueWords * sizeof(unsigned long long)));
         LUMRAD_TRY(cudaMalloc(&b->d_error, sizeof(int)));
-        LUMRAD_TRY(cudaMemsetAsync(b->d_queue, 0, 2 * sizeof(unsigned long long), b->stream));
+        LUMRAD_TRY(cudaMemsetAsync(b->d_queue, 0, kQueueWords * sizeof(unsigned long long), b->stream));
         LUMRAD_TRY(cudaMemsetAsync(b->d_error, 0, sizeof(int), b->stream));
         LUMRAD_TRY(cudaStreamSynchronize(b->stream));
         return LUMRAD_OK;

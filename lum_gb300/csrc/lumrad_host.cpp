@@ -400,7 +400,7 @@ int Context::check_error() {
 int Context::handle_error(int e) {
     if (e != 0) {
         cudaMemsetAsync(d_error, 0, sizeof(int), stream);
-        cudaMemsetAsync(d_queue, 0, 2 * sizeof(unsigned long long), stream);
+        cudaMemsetAsync(d_queue, 0, kQueueWords * sizeof(unsigned long long), stream);
         cudaMemsetAsync(world.d_probe_count, 0, world.count_cap * sizeof(int), stream);
         cudaStreamSynchronize(stream);
         return fail(LUMRAD_EDEVICE, std::string(e & 1 ? "radiance kernel scheduler stopped making progress" :
@@ -707,9 +707,9 @@ int lumrad_create(const LumRadSettings* s, LumRadContext* out) {
             LUMRAD_TRY(cudaEventCreate(&c->ring0[i]));
             LUMRAD_TRY(cudaEventCreate(&c->ring1[i]));
         }
-        LUMRAD_TRY(cudaMalloc(&c->d_queue, 2 * sizeof(unsigned long long)));
+        LUMRAD_TRY(cudaMalloc(&c->d_queue, kQueueWords * sizeof(unsigned long long)));
         LUMRAD_TRY(cudaMalloc(&c->d_error, sizeof(int)));
-        LUMRAD_TRY(cudaMemsetAsync(c->d_queue, 0, 2 * sizeof(unsigned long long), c->stream));
+        LUMRAD_TRY(cudaMemsetAsync(c->d_queue, 0, kQueueWords * sizeof(unsigned long long), c->stream));
         LUMRAD_TRY(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream));
         int rc = c->world.init(s->world_size[0], s->world_size[1], s->world_size[2], s->max_block_types,
                                s->precision, c->stream);

@@ -18,6 +18,9 @@ constexpr int kTaskRays = 32;
 // tasks' rays (8 B per ray: 67 MB, L2-resident on GB300).  Fewer, larger rounds shorten the
 // march kernel's tails (measured: 2^18 tasks 13% faster than 2^16 on many small worlds).
 constexpr int kChunkTasks = 1 << 18;
+// Words of a launch's task queue: [0] next march task, [1] march warps finished; zero between
+// launches (the march's last warp resets them)
+constexpr int kQueueWords = 2;
 // Round size of batches: their task spaces are large, and two rounds of 2^20 tasks (402 MB of ray
 // results, past the L2) beat seven of 2^18 by 2% on 256 mixed worlds (fewer queue drains)
 constexpr int kBatchRoundTasks = 1 << 20;
@@ -70,7 +73,7 @@ struct LaunchArgs {
     int total_warps;             // warps of the march grid (set by the launcher)
     int chunk_begin, chunk_end;  // tasks of this march/finalize round (set by the launcher)
     long long n_tasks;           // tasks of all worlds
-    unsigned long long* queue;   // [0] next task, [1] warps finished; zero between launches
+    unsigned long long* queue;   // kQueueWords words (see kQueueWords); zero between launches
     int* error;                  // set non-zero if a warp's scheduler stops making progress
     uint2* ray_res;              // per ray of the round: coarse fraction bits, info word
     int* ray_blk;                // per ray of the round: block id at the last coarse step (records)

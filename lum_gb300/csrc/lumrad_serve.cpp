@@ -204,7 +204,7 @@ int retire(Server* sv) {
         LUMRAD_TRY(q);
         const int err = *sl.h_error;
         if (err) {   // a warp's scheduler gave up: reset the slot's counters
-            LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, 2 * sizeof(unsigned long long), sl.stream));
+            LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, kQueueWords * sizeof(unsigned long long), sl.stream));
             LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
             for (auto& r : sl.reqs) {
                 DeviceWorld& dw = sv->worlds[r.world].ctx->world;
@@ -562,11 +562,11 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
             Slot& sl = *sv->slots.back();
             LUMRAD_TRY(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
             LUMRAD_TRY(cudaEventCreateWithFlags(&sl.ev_done, cudaEventDisableTiming));
-            LUMRAD_TRY(cudaMalloc(&sl.d_queue, 2 * sizeof(unsigned long long)));
+            LUMRAD_TRY(cudaMalloc(&sl.d_queue, kQueueWords * sizeof(unsigned long long)));
             LUMRAD_TRY(cudaMalloc(&sl.d_error, sizeof(int)));
             LUMRAD_TRY(cudaMallocHost(&sl.h_error, sizeof(int)));
             *sl.h_error = 0;
-            LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, 2 * sizeof(unsigned long long), sl.stream));
+            LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, kQueueWords * sizeof(unsigned long long), sl.stream));
             LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
             LUMRAD_TRY(cudaMalloc(&sl.d_ray_res, rays * sizeof(uint2)));
             // request packs sized up front so the serving loop rarely grows them

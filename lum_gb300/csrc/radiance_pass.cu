@@ -500,7 +500,7 @@ constexpr size_t kNaCbits = align256(kNaCgrid + 2 * (size_t)kNoAllocMaxBlocks); 
 constexpr size_t kNaRayRes = align256(kNaCbits + (size_t)(LUMRAD_MAX_BLOCK_SLOTS + 2) * 512);
 constexpr size_t kNaDirs = align256(kNaRayRes + (size_t)kNoAllocRoundTasks * kTaskRays * sizeof(uint2));
 constexpr size_t kNaQueue = align256(kNaDirs + 256 * sizeof(float4));
-constexpr size_t kNaError = kNaQueue + 2 * sizeof(unsigned long long);
+constexpr size_t kNaError = kNaQueue + kQueueWords * sizeof(unsigned long long);
 constexpr size_t kNaStats = align256(kNaError + sizeof(int));
 constexpr size_t kNaBytes = align256(kNaStats + 2 * sizeof(unsigned long long));
 static_assert(kNaBytes <= (5u << 20), "no-allocation scratch must stay under 5 MiB");
@@ -616,7 +616,7 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     const int r_index = R == 32 ? 0 : R == 64 ? 1 : R == 128 ? 2 : 3;
 
     // everything that must start at zero, and this call's inputs derived into the array
-    LUMRAD_TRY(cudaMemsetAsync(queue, 0, 2 * sizeof(unsigned long long), stream));
+    LUMRAD_TRY(cudaMemsetAsync(queue, 0, kQueueWords * sizeof(unsigned long long), stream));
     LUMRAD_TRY(cudaMemsetAsync(error, 0, sizeof(int), stream));
     LUMRAD_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), stream));
     LUMRAD_TRY(cudaMemcpyAsync(dirs, g_noalloc_dirs[r_index], R * sizeof(float4), cudaMemcpyHostToDevice, stream));
