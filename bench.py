@@ -290,6 +290,151 @@ def _serve_trace(srv, reqs, arrivals, params_of):
     return lat, rays, span, late
 
 
+def aux_leg(local: int, reps: int, with_cpu: bool):
+    """The steps either side of the pass, each through the library's API on the GPU and, beside
+    it, on the host cores through the oracle's restatement of the reference's own algorithm (the
+    dirty-probe derivation, which the reference lacks, against this library's host path):
+      update_list  the 27-neighbour update list of the demo world (65,536 blocks), list returned
+                   to the host (the reference builds it on the CPU every frame)
+      dirty_list   the probes within 2 blocks of a 1% edit of a 64x64x32 world, list returned
+      shift        radiance scroll by (1, 1, 0): the demo world and a 512x512x64 one (16.8M blocks)
+      gather       diffuse.frag's 8-probe gather at 1M points of the demo world, device buffers
+      blockify     one frame of blockify + map of 8 rotated 32^3 models into the demo world
+    Device times are CUDA events on the context's stream around enqueued calls (shift, gather);
+    calls that return a host result (lists, blockify) are timed wall-clock, synchronising."""
+    import torch
+    import lum_gb300
+    hbm_peak, _ = load_peaks()
+    dev = torch.device("cuda", local)
+    world = worldgen.demo_world(SEED)
+    rw = lum_gb300.RadianceWorld(world.dims, max_block_types=2048, device=local)   # room for the models' blocks
+    rw.load(world)
+    stream = torch.cuda.ExternalStream(rw.stream(), device=dev)
+    lists = pass_lists(world.dims)
+    rw.radiance_passes(lists, [lum_gb300.pass_params(rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=p)
+                               for p in range(PASSES)])
+    vol = rw.get_radiance()
+    W = world.n_blocks
+
+    def wall(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / n
+
+    def device(fn, n):
+        fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1000.0 / n
+
+    def cpu_time(fn, n=3):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            fn()
+        return (time.perf_counter() - t0) / n
+
+    oracle = None
+    if with_cpu:
+        import oracle as _oracle   # the CPU side only
+        oracle = _oracle
+    out = {"config": {"world": list(world.dims), "seed": SEED}}
+
+    # f1: update list
+    t = wall(rw.build_update_list, reps)
+    n_list = int(rw.build_update_list().shape[0])
+    e = {"us_per_call": t * 1e6, "blocks_per_s": W / t, "listed": n_list}
+    if oracle:
+        tc = cpu_time(lambda: oracle.update_list(world))
+        e["cpu"] = {"us_per_call": tc * 1e6, "kind": "port", "cores": 1}
+    out["update_list"] = e
+
+    # f1: dirty probes of an edit request
+    wd = worldgen.terrain_world((64, 64, 32), seed=SEED)
+    edits = worldgen.edit_request(wd.dims, 0.01, seed=SEED, stream=0)
+    with lum_gb300.RadianceWorld(wd.dims, max_block_types=wd.palette.shape[0], device=local) as rd:
+        rd.load(wd)
+        t = wall(lambda: rd.build_dirty_list(edits, 2), reps)
+        n_dirty = int(rd.build_dirty_list(edits, 2).shape[0])
+    e = {"us_per_call": t * 1e6, "edits": int(edits.shape[0]), "dirty_probes": n_dirty}
+    tc = cpu_time(lambda: lum_gb300.dirty_probes(wd.dims, edits, 2), 5)
+    e["cpu"] = {"us_per_call": tc * 1e6, "kind": "host path of this library (no reference counterpart)", "cores": 1}
+    out["dirty_list"] = e
+
+    # f2: radiance scroll, HBM-bound: 16 B read + 16 B written per block
+    t = device(lambda: rw.shift_radiance(1, 1, 0), reps)
+    e = {"us_per_call": t * 1e6, "gbs": 32.0 * W / t / 1e9}
+    with lum_gb300.RadianceWorld((512, 512, 64), max_block_types=1, device=local) as rb:
+        sb = torch.cuda.ExternalStream(rb.stream(), device=dev)
+
+        def dev_big(n):
+            rb.shift_radiance(1, 1, 0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(sb)
+            for _ in range(n):
+                rb.shift_radiance(1, 1, 0)
+            e1.record(sb)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / 1000.0 / n
+        tb = dev_big(reps)
+    wb = 512 * 512 * 64
+    e["large"] = {"blocks": wb, "us_per_call": tb * 1e6, "gbs": 32.0 * wb / tb / 1e9,
+                  "hbm_frac": 32.0 * wb / tb / 1e9 / hbm_peak}
+    if oracle:
+        tc = cpu_time(lambda: oracle.shift_radiance(vol, (1, 1, 0)))
+        e["cpu"] = {"us_per_call": tc * 1e6, "kind": "port", "cores": 1}
+    out["shift"] = e
+
+    # f4: gather at 1M points inside the world
+    n_pts = 1 << 20
+    rng = np.random.default_rng(SEED)
+    pos = rng.random((n_pts, 3)) * np.array(world.dims) * 16
+    nrm = rng.normal(size=(n_pts, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    pts = np.concatenate([pos, nrm], axis=1).astype(np.float32)
+    d_pts = torch.from_numpy(pts).to(dev)
+    d_rgb = torch.empty((n_pts, 3), dtype=torch.float32, device=dev)
+    t = device(lambda: rw.gather_device(d_pts.data_ptr(), n_pts, d_rgb.data_ptr()), reps)
+    alg = (24 + 12 + 8 * 16) * n_pts
+    e = {"points": n_pts, "us_per_call": t * 1e6, "points_per_s": n_pts / t, "gbs": alg / t / 1e9,
+         "hbm_frac": alg / t / 1e9 / hbm_peak}
+    if oracle:
+        tc = cpu_time(lambda: oracle.gather(vol, pts), 1)
+        e["cpu"] = {"us_per_call": tc * 1e6, "kind": "port", "cores": 1}
+    out["gather"] = e
+
+    # f3: blockify + map of 8 rotated 32^3 models
+    mrng = np.random.default_rng(SEED + 1)
+    model = ((mrng.random((32, 32, 32)) < 0.5) * mrng.integers(1, 256, (32, 32, 32))).astype(np.uint8)
+    mid = rw.load_model(model)
+    meshes = []
+    for i in range(8):
+        q = mrng.normal(size=4)
+        q = tuple(float(x) for x in (q / np.linalg.norm(q)))
+        meshes.append((mid, q, tuple(float(x) for x in mrng.random(3) * np.array(world.dims) * 16 * 0.8 + 40)))
+    static = world.palette.shape[0]
+    t = wall(lambda: rw.blockify(static, meshes), reps)
+    e = {"meshes": len(meshes), "model_voxels": int(model.size), "us_per_call": t * 1e6}
+    if oracle:
+        pal = np.zeros((2048, 16, 16, 16), np.uint8)
+        pal[:static] = world.palette
+        tc = cpu_time(lambda: oracle.blockify(world.grid, pal, static, [model], meshes), 1)
+        e["cpu"] = {"us_per_call": tc * 1e6, "kind": "port", "cores": 1}
+    out["blockify"] = e
+    rw.close()
+    return out
+
+
 def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 10000.0, 20000.0)):
     """Continuous batching of relight requests over 64 resident worlds, at each arrival rate and
     saturated (every request due at once); the plain form (one request per launch, one launch
@@ -421,9 +566,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--legs", default="demo,batched,serving",
+    ap.add_argument("--legs", default="demo,batched,serving,aux",
                     help="comma list of legs: demo (the headline line), batched (the mixed-size batch), "
-                         "serving (relight requests)")
+                         "serving (relight requests), aux (the steps either side of the pass)")
     ap.add_argument("--serve-requests", type=int, default=10000, help="requests per arrival rate (serving leg)")
     ap.add_argument("--batch-tuning", default=None, type=lambda s: tuple(int(x) for x in s.split(",")),
                     help="fixed batch settings G,C,M (guided divisor, chunk cap, march CTAs per SM) instead of "
@@ -446,6 +591,8 @@ def main():
             out["batched"] = batched_leg(local, max(3, args.steps // 2), args.warmup, flush, args.batch_tuning)
         if "serving" in legs:
             out["serving"] = serving_leg(local, n_requests=args.serve_requests)
+        if "aux" in legs:
+            out["aux"] = aux_leg(local, 20, not args.no_cpu and rank == 0)
         if rank == 0:
             print(json.dumps(out))
         return
@@ -562,6 +709,9 @@ def main():
     serving = None
     if "serving" in legs:
         serving = serving_leg(local, n_requests=args.serve_requests)
+    aux = None
+    if "aux" in legs:
+        aux = aux_leg(local, 20, not args.no_cpu and rank == 0)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -595,6 +745,7 @@ def main():
             "gpu_launches": (1 + PASSES) * args.steps,   # one march + a finalize per pass, per step
             "batched": batched,
             "serving": serving,
+            "aux": aux,
         }
         print(json.dumps(line))
     rw.close()

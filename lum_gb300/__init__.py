@@ -201,6 +201,11 @@ class RadianceWorld:
         check(self.lib.lumrad_gather_radiance(self.h, ptr(p), p.shape[0], ptr(out)))
         return out
 
+    def gather_device(self, d_points: int, n: int, d_rgb: int) -> None:
+        """The gather on device pointers ((n, 6) and (n, 3) float32), enqueued on this context's
+        stream (e.g. torch tensors' data_ptr())."""
+        check(self.lib.lumrad_gather_radiance_device(self.h, C.c_void_p(d_points), int(n), C.c_void_p(d_rgb)))
+
     def radiance_passes(self, lists, params) -> None:
         """Passes over int16 (n, 4) lists in order, as radiance_pass over each would run them;
         their marches share launches."""

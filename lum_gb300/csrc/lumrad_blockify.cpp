@@ -174,9 +174,18 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
         a.inv[15] = 1.0f;
     }
 
-    // exec_copies (device): temporary part of the palette cleared, block copies, world upload
-    const size_t tmp_bytes = (size_t)(w.n_slots - static_blocks) * 4096;
-    if (tmp_bytes) LUMRAD_TRY(cudaMemsetAsync(w.d_pal + (size_t)static_blocks * 4096, 0, tmp_bytes, c->stream));
+    // the slots this frame writes: every id from static_blocks up present in the grid (made here
+    // or set by the caller), below n_slots
+    int used_end = static_blocks;
+    for (size_t i = 0; i < w.W; i++) used_end = std::max(used_end, (int)cur[i] + 1);
+    used_end = std::min(used_end, w.n_slots);
+    // exec_copies (device): temporary part of the palette cleared (the slots that may hold voxels:
+    // the rest are zero already), block copies, world upload
+    const int clear_end = std::min(std::max(used_end, w.pal_dirty_end), w.n_slots);
+    if (clear_end > static_blocks)
+        LUMRAD_TRY(cudaMemsetAsync(w.d_pal + (size_t)static_blocks * 4096, 0, (size_t)(clear_end - static_blocks) * 4096,
+                                   c->stream));
+    w.pal_dirty_end = used_end;
     int2* d_copies = nullptr;
     if (!copies.empty()) {
         LUMRAD_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_copies), copies.size() * sizeof(int2), c->stream));
@@ -186,8 +195,9 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
     }
     LUMRAD_TRY(cudaMemcpyAsync(w.d_grid, cur.data(), w.W * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream));
 
-    // map (device), mesh by mesh; writes claimed in the owner words, then resolved
-    const size_t n_tmp = (size_t)(w.n_slots - static_blocks) * 4096;
+    // map (device), mesh by mesh; writes claimed in the owner words (one per voxel of the slots
+    // in use: the map writes only into blocks of the grid), then resolved
+    const size_t n_tmp = (size_t)(used_end - static_blocks) * 4096;
     if (n_meshes > 0 && n_tmp > 0) {
         if (n_tmp > c->map_owner_cap) {
             LUMRAD_TRY(cudaStreamSynchronize(c->stream));
@@ -208,7 +218,7 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
         LUMRAD_TRY(launch_map_resolve(w.d_pal + (size_t)static_blocks * 4096, c->d_map_owner, n_tmp, c->stream));
 
     // compact world of the blockified grid; occupancy masks from the device palette
-    w.build_compact(cur.data());
+    w.build_compact(cur.data(), false);   // the occupancy masks come from the device palette below
     const size_t cap = std::max<size_t>((size_t)w.n_compact, (size_t)w.n_slots + 64);
     if (cap > w.cbits_cap) {
         LUMRAD_TRY(cudaStreamSynchronize(c->stream));

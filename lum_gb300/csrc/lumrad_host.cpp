@@ -115,6 +115,7 @@ int DeviceWorld::readmit(cudaStream_t stream) {
     for (int i = 0; i < 2; i++) LUMRAD_TRY(cudaMalloc(&d_rad[i], W * rad_stride));
     LUMRAD_TRY(cudaMemcpyAsync(d_grid, h_grid.data(), W * sizeof(int16_t), cudaMemcpyHostToDevice, stream));
     LUMRAD_TRY(cudaMemcpyAsync(d_pal, h_pal_dev.data(), h_pal_dev.size(), cudaMemcpyHostToDevice, stream));
+    pal_dirty_end = n_slots;
     LUMRAD_TRY(cudaMemcpyAsync(d_mats, h_mats_dev.data(), LUMRAD_MATERIALS * sizeof(float4), cudaMemcpyHostToDevice,
                                stream));
     LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
@@ -131,7 +132,7 @@ int DeviceWorld::readmit(cudaStream_t stream) {
 // slot is absent shares one all-empty compact id) and builds each compact id's occupancy mask
 // from the palette as uploaded.  Ids that appear later (edits) get the next free compact id
 // through compact_of.
-void DeviceWorld::build_compact(const int16_t* g) {
+void DeviceWorld::build_compact(const int16_t* g, bool host_bits) {
     id_to_c.assign(65536, -1);
     reps.clear();
     empty_c = -1;
@@ -139,7 +140,8 @@ void DeviceWorld::build_compact(const int16_t* g) {
     reps.push_back(0);
     n_compact = 1;
     h_cbits.assign(128, 0u);
-    for (int k = 0; k < 4096 && n_slots > 0; k++)   // block 0 reads palette slot 0 like any other id
+    skip_host_bits = !host_bits;
+    for (int k = 0; k < 4096 && n_slots > 0 && host_bits; k++)   // block 0 reads palette slot 0 like any other id
         if (h_pal_dev[k]) h_cbits[k >> 5] |= 1u << (k & 31);
     h_cslot.assign(1, n_slots > 0 ? 0 : -1);
     cgrid_wide = false;
@@ -154,6 +156,7 @@ void DeviceWorld::build_compact(const int16_t* g) {
         if (cgrid_wide) reinterpret_cast<uint16_t*>(h_cgrid.data())[i] = (uint16_t)c;
         else h_cgrid[i] = (uint8_t)c;
     }
+    skip_host_bits = false;
 }
 
 int DeviceWorld::compact_of(int16_t b, bool* assigned) {
@@ -171,7 +174,7 @@ int DeviceWorld::compact_of(int16_t b, bool* assigned) {
     reps.push_back(has_slot ? b : kEmptyRep);
     h_cslot.push_back(has_slot ? slot : -1);
     h_cbits.resize((size_t)n_compact * 128, 0u);
-    if (has_slot) {
+    if (has_slot && !skip_host_bits) {
         const uint8_t* v = h_pal_dev.data() + (size_t)slot * 4096;
         uint32_t* bits = h_cbits.data() + (size_t)c * 128;
         for (int k = 0; k < 4096; k++)
@@ -796,6 +799,7 @@ int lumrad_upload_block_palette(LumRadContext ctx) {
     LUMRAD_TRY(cudaSetDevice(c->device));
     w.h_pal_dev = w.h_pal;
     LUMRAD_TRY(cudaMemcpyAsync(w.d_pal, w.h_pal_dev.data(), w.h_pal_dev.size(), cudaMemcpyHostToDevice, c->stream));
+    w.pal_dirty_end = w.n_slots;
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     w.compact_dirty = true;
     return LUMRAD_OK;

@@ -82,6 +82,10 @@ struct DeviceWorld {
     std::map<int, float4*> d_dirs;
     // blockify: the frame's grid with temporary blocks (empty when not blockified)
     std::vector<int16_t> h_cur;
+    // one past the highest palette slot that may hold non-zero voxels on the device (blockify
+    // clears the temporary slots up to here); every slot after a palette upload
+    int pal_dirty_end = 1 << 30;
+    bool skip_host_bits = false;          // inside build_compact(g, false)
     // eviction: the device buffers released, the volume kept here (raw storage, W * rad_stride)
     bool evicted = false;
     std::vector<uint8_t> h_rad_saved;
@@ -93,7 +97,9 @@ struct DeviceWorld {
     int evict(cudaStream_t stream);
     int readmit(cudaStream_t stream);
     void build_compact() { build_compact(h_grid.data()); }
-    void build_compact(const int16_t* g);   // compact ids of grid g (W ids)
+    // compact ids of grid g (W ids); host_bits: also the occupancy masks from the host palette
+    // (blockify computes them on the device from the palette it maps into)
+    void build_compact(const int16_t* g, bool host_bits = true);
     // Compact id of block id b, assigning the next free one (and its occupancy mask in h_cbits)
     // if b has none yet; -1 if that needs a wider compact grid (a full rebuild).
     int compact_of(int16_t b, bool* assigned);

@@ -200,3 +200,31 @@ def test_dirty_list_on_device_matches_host(dims, frac, radius):
         assert np.array_equal(got, lum_gb300.dirty_probes(dims, edits, radius))
         assert np.array_equal(got, worldgen.dirty_probes(dims, edits, radius))
         assert rw.build_dirty_list(np.zeros((0, 4), np.int16), radius).shape == (0, 4)
+
+
+def test_blockify_frames_of_different_sizes():
+    """Consecutive frames with more, then fewer, meshes (the smaller frame clears the slots the
+    larger one used), and an origin world holding a dynamic id above the static blocks (its slot
+    is mapped into like a temporary one): each frame's grid and palette equal the oracle's."""
+    import lum_gb300
+    import oracle
+    w = worldgen.terrain_world((9, 8, 6), seed=14, n_types=20)
+    static = w.palette.shape[0]
+    w.grid[2, 3, 4] = static + 30          # a dynamic id set by the caller
+    models = _models()
+    frames = [[(0, _quat(5), (30.0, 20.0, 25.0)), (1, _quat(6), (70.0, 50.0, 40.0)), (0, _quat(7), (60.5, 66.0, 49.0)),
+               (0, (0.0, 0.0, 0.0, 1.0), (64.0, 48.0, 32.0))],
+              [(1, _quat(8), (20.0, 30.0, 20.0))],
+              [],
+              [(0, _quat(9), (50.0, 40.0, 30.0)), (1, _quat(10), (30.0, 60.0, 50.0))]]
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=240) as rw:
+        rw.load(w)
+        for m in models:
+            rw.load_model(m)
+        pal = np.zeros((240, 16, 16, 16), np.uint8)
+        pal[:static] = w.palette
+        for meshes in frames:
+            rw.blockify(static, meshes)
+            ref_g, ref_p = oracle.blockify(w.grid, pal, static, models, meshes)
+            assert np.array_equal(rw.get_world(), ref_g)
+            assert np.array_equal(rw.get_block_palette(), ref_p)
