@@ -14,12 +14,17 @@
 //                    set up again (cheaper than a round trip through L2), refine DDA, material,
 //                    trilinear fetch of the previous radiance, shading, xor-butterfly sum.  When
 //                    R/32 divides 8 a probe's subgroups share a CTA and their means are summed in
-//                    order from shared memory; otherwise through global scratch and a per-probe
+//                    order from shared memory (a lean instantiation, 6 CTAs per SM, when every
+//                    probe of the launch does); otherwise through global scratch and a per-probe
 //                    counter.  Lookup and hit counters are summed per CTA.
+//
+// Several passes of one context (launch_passes): one march launch over all their tasks (the
+// traversal does not read the radiance volume), then each pass's finalize in order.
 //
 // Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
 // world (uint8 ids + occupancy bits, L1-resident); between the kernels each ray keeps 8 B
-// (coarse fraction, info word), 67 MB for a full round, L2-resident.
+// (coarse fraction, info word): 67 MB for a single pass's round of 2^18 tasks (L2-resident),
+// up to 134 MB for several passes, 268 MB for a batch's round of 2^20.
 
 #include "radiance_device.cuh"
 
