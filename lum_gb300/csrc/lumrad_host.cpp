@@ -1108,24 +1108,29 @@ int lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, co
     const cudaError_t idle = cudaStreamQuery(c->stream);
     if (idle == cudaErrorNotReady) cudaGetLastError();   // a busy stream is no error for later checks
     bool direct = total > 0 && idle == cudaSuccess;
-    for (int i = 0; direct && i < n; i++)
-        direct = counts[i] == 0 || host_pinned(requests[i], (size_t)counts[i] * 4 * sizeof(int16_t));
+    // runs of adjacent lists (each run one copy, its page-locking checked once)
+    struct Run { const int16_t* src; size_t first, count; };
+    std::vector<Run> runs;
     if (direct) {
         size_t off = 0;
         int i = 0;
-        while (i < n) {
+        while (i < n && direct) {
             if (counts[i] == 0) { reqs[i++] = c->d_req + off; continue; }
-            const int16_t* src = requests[i];
-            const size_t first = off;
+            const Run r0{requests[i], off, 0};
             int j = i;
-            while (j < n && (counts[j] == 0 || requests[j] == src + (off - first) * 4)) {
+            while (j < n && (counts[j] == 0 || requests[j] == r0.src + (off - r0.first) * 4)) {
                 reqs[j] = c->d_req + off;
                 off += (size_t)counts[j++];
             }
-            LUMRAD_TRY(cudaMemcpyAsync(c->d_req + first, src, (off - first) * sizeof(short4), cudaMemcpyHostToDevice,
-                                       c->stream));
+            runs.push_back(Run{r0.src, r0.first, off - r0.first});
+            direct = host_pinned(r0.src, (off - r0.first) * 4 * sizeof(int16_t));
             i = j;
         }
+    }
+    if (direct) {
+        for (const Run& r : runs)
+            LUMRAD_TRY(cudaMemcpyAsync(c->d_req + r.first, r.src, r.count * sizeof(short4), cudaMemcpyHostToDevice,
+                                       c->stream));
         LUMRAD_TRY(cudaEventRecord(c->ev_req, c->stream));
         rc = c->run_passes(reqs.data(), counts, params, n);
         LUMRAD_TRY(cudaEventSynchronize(c->ev_req));
