@@ -337,16 +337,12 @@ __device__ __forceinline__ void store_probe(const WorldPass& w, int g, float3 ac
     Store::store(reinterpret_cast<typename Store::T*>(w.next), idx, nv);
 }
 
-// Subgroup mean V = sum/32 of subgroup k of workgroup g is done.  R = 32: the probe's mean is V.
-// Otherwise V goes to scratch and the last of the probe's R/32 subgroups sums them in order
-// (radiance.comp:401-407), divides by R/32 and stores.  Lane 0 only.
+// Subgroup mean V = sum/32 of subgroup k of workgroup g (R > 32) is done, and the probe's
+// subgroups span CTAs: V goes to scratch and the last of the probe's R/32 subgroups sums them in
+// order (radiance.comp:401-407), divides by R/32 and stores.  Lane 0 only.
 template <class Store>
 __device__ __forceinline__ void subgroup_done(const WorldPass& w, int g, int k, float3 v) {
     const int nsub = w.R >> 5;
-    if (nsub == 1) {
-        store_probe<Store>(w, g, make_float3(fadd(0.0f, v.x), fadd(0.0f, v.y), fadd(0.0f, v.z)));
-        return;
-    }
     float4* slots = w.scratch + (long long)g * nsub;
     __stcg(slots + k, make_float4(v.x, v.y, v.z, 0.0f));
     // acq_rel at device scope: our mean is visible before the count, and the last subgroup
