@@ -300,6 +300,8 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
       shift        radiance scroll by (1, 1, 0): the demo world and a 512x512x64 one (16.8M blocks)
       gather       diffuse.frag's 8-probe gather at 1M points of the demo world, device buffers
       blockify     one frame of blockify + map of 8 rotated 32^3 models into the demo world
+      frame        lumrad_update_radiance: one frame of the drop-in (device update list of the demo
+                   world, then the pass over it) at the reference's 64 rays, max_dist 128
     Device times are CUDA events on the context's stream around enqueued calls (shift, gather);
     calls that return a host result (lists, blockify) are timed wall-clock, synchronising."""
     import torch
@@ -431,6 +433,13 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
         tc = cpu_time(lambda: oracle.blockify(world.grid, pal, static, [model], meshes), 1)
         e["cpu"] = {"us_per_call": tc * 1e6, "kind": "port", "cores": 1}
     out["blockify"] = e
+
+    # the drop-in frame: update list on the device, then the pass over all 51,992 listed probes
+    rw.blockify(static, [])   # the origin world again
+    fp = lum_gb300.pass_params(rays=64, max_dist=128.0, blend=0.1, time_seed=0)
+    t = wall(lambda: rw.update_radiance(fp), reps)
+    out["frame"] = {"us_per_call": t * 1e6, "probes": n_list, "rays_per_probe": 64,
+                    "probe_rays_per_s": n_list * 64 / t}
     rw.close()
     return out
 
