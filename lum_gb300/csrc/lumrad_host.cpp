@@ -1128,10 +1128,18 @@ int lumrad_radiance_passes(LumRadContext ctx, const int16_t* const* requests, co
         }
     }
     if (direct) {
-        for (const Run& r : runs)
-            LUMRAD_TRY(cudaMemcpyAsync(c->d_req + r.first, r.src, r.count * sizeof(short4), cudaMemcpyHostToDevice,
-                                       c->stream));
-        LUMRAD_TRY(cudaEventRecord(c->ev_req, c->stream));
+        for (const Run& r : runs) {
+            const cudaError_t e = cudaMemcpyAsync(c->d_req + r.first, r.src, r.count * sizeof(short4),
+                                                  cudaMemcpyHostToDevice, c->stream);
+            if (e != cudaSuccess) {
+                cudaStreamSynchronize(c->stream);   // no copy may still read the caller's arrays
+                return fail(LUMRAD_EDEVICE, std::string("request copy: ") + cudaGetErrorString(e));
+            }
+        }
+        if (cudaEventRecord(c->ev_req, c->stream) != cudaSuccess) {
+            cudaStreamSynchronize(c->stream);
+            return fail(LUMRAD_EDEVICE, "request copy: event record failed");
+        }
         rc = c->run_passes(reqs.data(), counts, params, n);
         LUMRAD_TRY(cudaEventSynchronize(c->ev_req));
         return rc;
