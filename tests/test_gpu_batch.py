@@ -87,3 +87,26 @@ def test_batch_in_the_mix_equals_alone():
         assert rws[2].get_radiance().tobytes() == solo[0].get_radiance().tobytes()
     for rw in rws + solo:
         rw.close()
+
+
+@pytest.mark.parametrize("rays", [(96, 64), (512, 32, 128)])
+def test_batch_with_probes_spanning_ctas(rays):
+    """Batches holding ray counts whose subgroups do not fit one finalize CTA (96, 512) run the
+    general finalize kernel (cross-CTA combine) for the whole launch; each world equals the oracle."""
+    import lum_gb300
+    import oracle
+    mix = worldgen.mixed_worlds(n=5, seed=13, max_dims=(9, 8, 6), rays=rays)
+    assert any((r // 32) > 1 and 8 % (r // 32) for _, _, r in mix)
+    rws = _make(mix, first=20)
+    with lum_gb300.RadianceBatch(rws) as b:
+        for i, (w, req, r) in enumerate(mix):
+            b.set_requests(i, req, lum_gb300.pass_params(rays=r, max_dist=96.0, blend=0.1))
+        b.run(7)
+        b.synchronize()
+        got = [rw.get_radiance() for rw in rws]
+    for i, (w, req, r) in enumerate(mix):
+        ref, _, _ = oracle.radiance_pass(w, req, rays=r, max_dist=96.0, blend=0.1, time_seed=7,
+                                         prev=random_prev(w, seed=120 + i))
+        assert rel_err(got[i], ref).max() <= RTOL, (i, r)
+    for rw in rws:
+        rw.close()

@@ -239,3 +239,37 @@ def test_cancel_before_launch():
         s.close()
     for rw in a_rws + b_rws:
         rw.close()
+
+
+def test_server_with_probes_spanning_ctas():
+    """Requests of 96 and 512 rays (subgroups combined across finalize CTAs) in the same launches
+    as 64-ray ones: the general finalize kernel; each world equals the oracle's chain of passes."""
+    import oracle
+    worlds = _worlds()
+    which = [0, 1, 3]
+    rays = {0: 96, 1: 512, 3: 64}
+    reqs = []
+    for k in range(2):
+        for i in which:
+            e = worldgen.edit_request(DIMS[i], 0.02, seed=7, stream=10 * i + k)
+            reqs.append((i, e, rays[i], 500 + 10 * i + k))
+    srv, rws = _server(worlds, which, max_inflight=2)
+    _submit(srv, reqs, which)
+    srv.run(timeout_s=300)
+    done = srv.poll()
+    assert len(done) == len(reqs) and (done["status"] == 0).all()
+    for k, i in enumerate(which):
+        w = worlds[i]
+        cur = random_prev(w, seed=200 + i)
+        grid = w.grid
+        for j, e, r, seed in reqs:
+            if j != i:
+                continue
+            grid = worldgen.apply_edits(grid, e)
+            we = dataclasses.replace(w, grid=grid)
+            cur, _, _ = oracle.radiance_pass(we, worldgen.dirty_probes(w.dims, e, 2), rays=r, max_dist=64.0,
+                                             blend=0.1, time_seed=seed, prev=cur)
+        assert rel_err(srv.get_radiance(k), cur).max() <= RTOL, i
+    srv.close()
+    for rw in rws:
+        rw.close()
