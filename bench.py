@@ -302,6 +302,8 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
       blockify     one frame of blockify + map of 8 rotated 32^3 models into the demo world
       frame        lumrad_update_radiance: one frame of the drop-in (device update list of the demo
                    world, then the pass over it) at the reference's 64 rays, max_dist 128
+      precision    the demo step (8 passes in one call) with FP32, FP16 and BF16 radiance storage,
+                   steps back to back (L2 not flushed)
     Device times are CUDA events on the context's stream around enqueued calls (shift, gather);
     calls that return a host result (lists, blockify) are timed wall-clock, synchronising."""
     import torch
@@ -441,6 +443,29 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
     out["frame"] = {"us_per_call": t * 1e6, "probes": n_list, "rays_per_probe": 64,
                     "probe_rays_per_s": n_list * 64 / t}
     rw.close()
+
+    # the demo step at each radiance storage precision (C4: FP16/BF16 storage, FP32 arithmetic)
+    plist = [lum_gb300.pass_params(rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=p) for p in range(PASSES)]
+    rays_step = sum(l.shape[0] for l in lists) * RAYS
+    prec = {}
+    for name in ("fp32", "fp16", "bf16"):
+        with lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], precision=name,
+                                     device=local) as rp:
+            rp.load(world)
+            for p, l in enumerate(lists):
+                rp.upload_requests(p, l)
+            sp = torch.cuda.ExternalStream(rp.stream(), device=dev)
+            rp.radiance_passes_resident(list(range(PASSES)), plist)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(sp)
+            for _ in range(reps):
+                rp.radiance_passes_resident(list(range(PASSES)), plist)
+            e1.record(sp)
+            e1.synchronize()
+            t = e0.elapsed_time(e1) / 1000.0 / reps
+            prec[name] = {"ms_per_step": t * 1e3, "probe_rays_per_s": rays_step / t}
+    out["precision"] = prec
     return out
 
 
