@@ -520,9 +520,15 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
         if ((rc = ensure_pass_table(k))) return rc;
         WorldPass* tab = h_ptab[ptab_half];
         if (ev_ptab[ptab_half]) LUMRAD_TRY(cudaEventSynchronize(ev_ptab[ptab_half]));   // its last copy is done
+        // a failure before the group's launch leaves the volume as the previous group left it
+        const int cur0 = world.cur;
+        auto undo = [&](int code) {
+            world.cur = cur0;
+            return code;
+        };
         long long begin = 0;
         for (int q = 0; q < k; q++) {
-            if ((rc = world.fill_pass(reqs[i + q], ns[i + q], ps[i + q], stream, &tab[q]))) return rc;
+            if ((rc = world.fill_pass(reqs[i + q], ns[i + q], ps[i + q], stream, &tab[q]))) return undo(rc);
             tab[q].task_begin = begin;
             begin += aligned_tasks(i + q);
             probes += (uint64_t)tab[q].n_groups;
@@ -534,10 +540,11 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
             tab[q].probe_count = world.d_probe_count;
             tab[q].stats = world.d_stats;
         }
-        if ((rc = ensure_rays(total, kMultiTasks))) return rc;
-        LUMRAD_TRY(cudaMemcpyAsync(d_ptab, tab, k * sizeof(WorldPass), cudaMemcpyHostToDevice, stream));
-        if (!ev_ptab[ptab_half]) LUMRAD_TRY(cudaEventCreateWithFlags(&ev_ptab[ptab_half], cudaEventDisableTiming));
-        LUMRAD_TRY(cudaEventRecord(ev_ptab[ptab_half], stream));
+        if ((rc = ensure_rays(total, kMultiTasks))) return undo(rc);
+        cudaError_t e = cudaMemcpyAsync(d_ptab, tab, k * sizeof(WorldPass), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess && !ev_ptab[ptab_half]) e = cudaEventCreateWithFlags(&ev_ptab[ptab_half], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_ptab[ptab_half], stream);
+        if (e != cudaSuccess) return undo(fail(LUMRAD_EDEVICE, std::string("pass table copy: ") + cudaGetErrorString(e)));
         ptab_half ^= 1;
         LaunchArgs la;
         std::memset(&la, 0, sizeof la);
