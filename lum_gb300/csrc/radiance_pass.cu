@@ -343,14 +343,18 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     }
 }
 
-int march_grid(bool record, int num_sms, int ctas_per_sm = 0) {
+// CTAs of a march launch: the occupancy limit (or ctas_per_sm) on every SM, but no more warps
+// than the largest round has tasks (a small world's launch would otherwise start hundreds of
+// CTAs that find the queue empty)
+int march_grid(bool record, int num_sms, long long round_tasks, int ctas_per_sm = 0) {
     int per_sm = 0;
     const cudaError_t e = record
         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<true>, kWarps * 32, 0)
         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<false>, kWarps * 32, 0);
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
-    return num_sms * per_sm;
+    const long long needed = (std::max(round_tasks, 1LL) + kWarps - 1) / kWarps;
+    return (int)std::min<long long>((long long)num_sms * per_sm, needed);
 }
 
 template <class Store, bool RECORD>
@@ -362,10 +366,10 @@ void launch_finalize(const LaunchArgs& args, int n, bool in_cta, cudaStream_t st
 
 template <class Store, bool RECORD>
 cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
-    const int blocks = march_grid(RECORD, num_sms, a.march_ctas);
+    const long long round = a.round_tasks > 0 ? a.round_tasks : kChunkTasks;
+    const int blocks = march_grid(RECORD, num_sms, std::min(a.n_tasks, round), a.march_ctas);
     LaunchArgs args = a;
     args.total_warps = blocks * kWarps;
-    const long long round = a.round_tasks > 0 ? a.round_tasks : kChunkTasks;
     for (long long c0 = 0; c0 < a.n_tasks; c0 += round) {
         args.chunk_begin = (int)c0;
         args.chunk_end = (int)min(c0 + round, a.n_tasks);
@@ -380,7 +384,7 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
 template <class Store>
 cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, size_t vol_bytes, int num_sms,
                      cudaStream_t stream) {
-    const int blocks = march_grid(false, num_sms, a.march_ctas);
+    const int blocks = march_grid(false, num_sms, a.n_tasks, a.march_ctas);
     LaunchArgs args = a;
     args.total_warps = blocks * kWarps;
     args.chunk_begin = 0;
@@ -669,7 +673,7 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     la.queue = queue;
     la.error = error;
     la.ray_res = reinterpret_cast<uint2*>(base + kNaRayRes);
-    const int blocks = march_grid(false, nd->num_sms);
+    const int blocks = march_grid(false, nd->num_sms, std::min<long long>(n_tasks, kNoAllocRoundTasks));
     la.total_warps = blocks * kWarps;
     for (long long c0 = 0; c0 < n_tasks; c0 += kNoAllocRoundTasks) {
         la.chunk_begin = (int)c0;
