@@ -140,3 +140,30 @@ def test_full_server_world_alone_equals_mix():
     mixed = serve(list(range(64)))
     for i in (0, 17, 42, 63):
         assert serve([i])[i].tobytes() == mixed[i].tobytes()
+
+
+def test_demo_step_in_one_call_equals_single_passes():
+    """The headline step: the demo world's 8 passes (6,554 probes x 256 rays each) through one
+    several-pass call, bit for bit the 8 single passes, counters included."""
+    import lum_gb300
+    w = worldgen.demo_world(SEED)
+    lists = _demo_lists(w.dims)
+    params = [lum_gb300.pass_params(rays=256, max_dist=256.0, blend=0.1, time_seed=p) for p in range(8)]
+    out, stats = [], []
+    for multi in (False, True):
+        with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+            rw.load(w)
+            if multi:
+                rw.radiance_passes(lists, params)
+                st = rw.pass_stats()
+                stats.append((st["steps"], st["hits"], st["probes"]))
+            else:
+                s = [0, 0, 0]
+                for l, p in zip(lists, params):
+                    rw.radiance_pass(l, p)
+                    st = rw.pass_stats()
+                    s = [s[0] + st["steps"], s[1] + st["hits"], s[2] + st["probes"]]
+                stats.append(tuple(s))
+            out.append(rw.get_radiance())
+    assert out[0].tobytes() == out[1].tobytes()
+    assert stats[0] == stats[1]
