@@ -114,9 +114,20 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
     int rc = w.sync_inputs(c->stream);   // the origin world and palette as loaded
     if (rc) return rc;
 
+    // page-locked staging (see Context::h_blk), made on the first call
+    const size_t off_cgrid = w.W * sizeof(int16_t), off_cslot = off_cgrid + w.W * sizeof(uint16_t);
+    const size_t n_cslot = (size_t)w.n_slots + 128;
+    const size_t off_copies = off_cslot + n_cslot * sizeof(int);
+    if (!c->h_blk) {
+        LUMRAD_TRY(cudaMallocHost(&c->h_blk, off_copies + (size_t)w.n_slots * sizeof(int2)));
+        LUMRAD_TRY(cudaMalloc(&c->d_blk_copies, (size_t)w.n_slots * sizeof(int2)));
+    }
+    int16_t* cur = reinterpret_cast<int16_t*>(c->h_blk);   // the previous call's uploads are done
+    int2* copies = reinterpret_cast<int2*>(c->h_blk + off_copies);
+    std::memcpy(cur, w.h_grid.data(), w.W * sizeof(int16_t));
+    int n_copies = 0;
+
     // blockify (host): temporary slots from static_blocks up, in mesh order
-    std::vector<int16_t> cur = w.h_grid;
-    std::vector<int2> copies;
     int counter = static_blocks;
     for (int i = 0; i < n_meshes; i++) {
         float r[3][3];
@@ -139,7 +150,7 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
                         return fail(LUMRAD_ENOMEM, "temporary blocks exceed max_block_types");
                     // copy the static block's voxels; a negative id has no source block (the
                     // reference's copy would start at a negative palette offset)
-                    if (b > 0) copies.push_back(make_int2(b, counter));
+                    if (b > 0) copies[n_copies++] = make_int2(b, counter);
                     b = (int16_t)counter++;
                 }
     }
@@ -186,14 +197,12 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
         LUMRAD_TRY(cudaMemsetAsync(w.d_pal + (size_t)static_blocks * 4096, 0, (size_t)(clear_end - static_blocks) * 4096,
                                    c->stream));
     w.pal_dirty_end = used_end;
-    int2* d_copies = nullptr;
-    if (!copies.empty()) {
-        LUMRAD_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_copies), copies.size() * sizeof(int2), c->stream));
-        LUMRAD_TRY(cudaMemcpyAsync(d_copies, copies.data(), copies.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
-        LUMRAD_TRY(launch_palette_copies(w.d_pal, d_copies, (int)copies.size(), c->stream));
-        LUMRAD_TRY(cudaFreeAsync(d_copies, c->stream));
+    if (n_copies > 0) {
+        LUMRAD_TRY(cudaMemcpyAsync(c->d_blk_copies, copies, (size_t)n_copies * sizeof(int2), cudaMemcpyHostToDevice,
+                                   c->stream));
+        LUMRAD_TRY(launch_palette_copies(w.d_pal, c->d_blk_copies, n_copies, c->stream));
     }
-    LUMRAD_TRY(cudaMemcpyAsync(w.d_grid, cur.data(), w.W * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(w.d_grid, cur, w.W * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream));
 
     // map (device), mesh by mesh; writes claimed in the owner words (one per voxel of the slots
     // in use: the map writes only into blocks of the grid), then resolved
@@ -218,7 +227,7 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
         LUMRAD_TRY(launch_map_resolve(w.d_pal + (size_t)static_blocks * 4096, c->d_map_owner, n_tmp, c->stream));
 
     // compact world of the blockified grid; occupancy masks from the device palette
-    w.build_compact(cur.data(), false);   // the occupancy masks come from the device palette below
+    w.build_compact(cur, false);   // the occupancy masks come from the device palette below
     const size_t cap = std::max<size_t>((size_t)w.n_compact, (size_t)w.n_slots + 64);
     if (cap > w.cbits_cap) {
         LUMRAD_TRY(cudaStreamSynchronize(c->stream));
@@ -231,12 +240,19 @@ int lumrad_blockify(LumRadContext ctx, int static_blocks, const int* models, con
         LUMRAD_TRY(cudaMalloc(&w.d_cslot, cap * sizeof(int)));
         w.cbits_cap = cap;
     }
-    LUMRAD_TRY(cudaMemcpyAsync(w.d_cslot, w.h_cslot.data(), w.h_cslot.size() * sizeof(int), cudaMemcpyHostToDevice,
-                               c->stream));
+    // the compact grid and slots through the staging area (both fit: at most W uint16 ids, and
+    // at most n_slots + 66 compact ids)
+    const void* cslot_src = w.h_cslot.data();
+    if (w.h_cslot.size() <= n_cslot) {
+        std::memcpy(c->h_blk + off_cslot, w.h_cslot.data(), w.h_cslot.size() * sizeof(int));
+        cslot_src = c->h_blk + off_cslot;
+    }
+    std::memcpy(c->h_blk + off_cgrid, w.h_cgrid.data(), w.h_cgrid.size());
+    LUMRAD_TRY(cudaMemcpyAsync(w.d_cslot, cslot_src, w.h_cslot.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     LUMRAD_TRY(launch_compact_bits(w.d_pal, w.d_cslot, w.n_compact, w.d_cbits, c->stream));
-    LUMRAD_TRY(cudaMemcpyAsync(w.d_cgrid, w.h_cgrid.data(), w.h_cgrid.size(), cudaMemcpyHostToDevice, c->stream));
-    LUMRAD_TRY(cudaStreamSynchronize(c->stream));   // host vectors are reused by the next call
-    w.h_cur.swap(cur);
+    LUMRAD_TRY(cudaMemcpyAsync(w.d_cgrid, c->h_blk + off_cgrid, w.h_cgrid.size(), cudaMemcpyHostToDevice, c->stream));
+    w.h_cur.assign(cur, cur + w.W);
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));   // the staging area is reused by the next call
     return LUMRAD_OK;
 }
 

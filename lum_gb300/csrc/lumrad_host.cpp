@@ -654,6 +654,8 @@ void Context::release() {
     for (auto& m : models) cudaFree(m.d_vox);
     models.clear();
     cudaFree(d_map_owner);
+    if (h_blk) cudaFreeHost(h_blk);
+    cudaFree(d_blk_copies);
     if (h_err) cudaFreeHost(h_err);
     if (ev_req) cudaEventDestroy(ev_req);
     for (int i = 0; i < kRing; i++) {

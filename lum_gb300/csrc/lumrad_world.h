@@ -157,6 +157,11 @@ struct Context {
     std::vector<Model> models;
     unsigned long long* d_map_owner = nullptr;   // one word per voxel of the temporary palette slots
     size_t map_owner_cap = 0;
+    // blockify staging, page-locked so the frame's uploads do not block the host: the working
+    // grid (W int16), compact grid (W uint16 at most), compact slots (n_slots + 128 ints) and
+    // palette copies (n_slots int2); and the copies' device buffer
+    uint8_t* h_blk = nullptr;
+    int2* d_blk_copies = nullptr;
     // device update-list builder
     ListScratch list{};
     short4* d_specials = nullptr;
