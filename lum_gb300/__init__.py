@@ -122,10 +122,15 @@ class RadianceWorld:
 
     # ---- passes
     def build_update_list(self) -> np.ndarray:
+        """The update list (27-neighbour rule, then the queued specials); one build when it fits
+        every block plus 4,096 specials, else a second with the exact size."""
         n = C.c_int()
-        check(self.lib.lumrad_build_update_list(self.h, None, 0, C.byref(n)))
-        out = np.zeros((max(n.value, 1), 4), dtype=np.int16)
-        check(self.lib.lumrad_build_update_list(self.h, ptr(out), n.value, C.byref(n)))
+        cap = self.n_blocks + 4096
+        out = np.empty((cap, 4), dtype=np.int16)
+        check(self.lib.lumrad_build_update_list(self.h, ptr(out), cap, C.byref(n)))
+        if n.value > cap:
+            out = np.empty((n.value, 4), dtype=np.int16)
+            check(self.lib.lumrad_build_update_list(self.h, ptr(out), n.value, C.byref(n)))
         return out[: n.value]
 
     def build_dirty_list(self, edits, radius: int = 2) -> np.ndarray:
