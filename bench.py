@@ -469,7 +469,7 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
     return out
 
 
-def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 10000.0, 20000.0)):
+def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 10000.0, 20000.0), inflight: int = 4):
     """Continuous batching of relight requests over 64 resident worlds, at each arrival rate and
     saturated (every request due at once); the plain form (one request per launch, one launch
     at a time) saturated, for comparison."""
@@ -499,7 +499,7 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
                           world_blocks_total=int(sum(w.n_blocks for w in worlds)),
                           l2="inputs resident; no flush (a serving loop runs warm)")}
     budget = SERVE_WORKLOAD["hbm_budget_gb"] * 1e9
-    srv = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=3)
+    srv = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=inflight)
     for rw in rws:
         srv.add_world(rw)
     # warm-up: a short saturated trace
@@ -523,7 +523,8 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
     out.update({"value": sat["probe_rays_per_s"], "unit": "probe-rays/s", "sweep": sweep, "saturated": sat,
                 "plain_saturated": psat, "speedup_vs_plain": sat["probe_rays_per_s"] / psat["probe_rays_per_s"],
                 "launches": st["launches"], "max_requests_in_launch": st["max_requests_in_launch"],
-                "resident_gb": st["resident_bytes"] / 1e9, "peak_inflight_mb": st["peak_inflight_bytes"] / 1e6})
+                "resident_gb": st["resident_bytes"] / 1e9, "peak_inflight_mb": st["peak_inflight_bytes"] / 1e6,
+                "max_inflight": inflight})
     return out
 
 

@@ -312,7 +312,8 @@ typedef struct {
     int    device;
     int    precision;             /* LUMRAD_PRECISION_*; every world must match */
     double hbm_budget_bytes;      /* device bytes for resident worlds plus launches (0 = no limit) */
-    int    max_inflight;          /* launches on the GPU at once, 1..8 (0 = 2) */
+    int    max_inflight;          /* launches on the GPU at once, 1..8 (0 = 4: on 64 mixed worlds
+                                     4 slots served 30% more than 2, 6 no more than 4) */
     int    max_requests_per_launch;   /* 0 = no limit */
     int    radius;                /* dirty-probe radius around each edit, in blocks (0..15) */
 } LumRadServerSettings;

@@ -332,7 +332,7 @@ class RadianceServer:
     """Relight requests over resident worlds, continuously batched (lumrad_server_*)."""
 
     def __init__(self, device: int = 0, precision: str = "fp32", hbm_budget_bytes: float = 0.0,
-                 max_inflight: int = 2, max_requests_per_launch: int = 0, radius: int = 2):
+                 max_inflight: int = 4, max_requests_per_launch: int = 0, radius: int = 2):
         from ._native import ServerSettings
         self.lib = load()
         s = ServerSettings(int(device), PRECISION[precision], float(hbm_budget_bytes), int(max_inflight),

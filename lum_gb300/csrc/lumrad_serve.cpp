@@ -551,7 +551,7 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
     if (s->hbm_budget_bytes < 0 || s->max_requests_per_launch < 0) return fail(LUMRAD_EINVAL, "negative limit");
     Server* sv = new Server();
     sv->s = *s;
-    if (sv->s.max_inflight == 0) sv->s.max_inflight = 2;
+    if (sv->s.max_inflight == 0) sv->s.max_inflight = 4;
     sv->t0 = clock_s();
     auto attempt = [&]() -> int {
         LUMRAD_TRY(cudaSetDevice(s->device));
