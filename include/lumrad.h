@@ -156,7 +156,9 @@ int  lumrad_request_update(LumRadContext ctx, int x, int y, int z);
  * (internal_render.cpp:1129-1214): builds the update list on the device (consuming the special
  * requests) and runs one pass.  With params->size == 0 the time slicing adapts as the reference
  * does (magicSize in [1,10], 1.8-2.2 ms target) and time_seed/shift follow the context's frame
- * counter. */
+ * counter.  The call does not wait for the GPU: the pass is launched for the longest possible list
+ * and its kernels read the list's length on the device (only hit records, sized by the length,
+ * and adaptive slicing, which reads the previous pass's time, wait for the device). */
 int  lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params);
 
 /* shift_radiance (internal_render.cpp:1218-1335), applied now: the volume becomes

@@ -413,7 +413,7 @@ int Context::handle_error(int e) {
     return LUMRAD_OK;
 }
 
-int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in) {
+int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in, const int* dev_count) {
     NvtxRange range("lumrad radiance pass");
     if (int rc = check_unowned(this)) return rc;
     LumRadPassParams p = *p_in;
@@ -439,6 +439,14 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in)
     if ((rc = ensure_rays(la.n_tasks))) return rc;
     la.ray_res = d_ray_res;
     la.ray_blk = d_ray_blk;
+    la.dev_count = dev_count;
+    last_count_on_device = dev_count != nullptr;
+    if (dev_count) {
+        if (!d_last_count) LUMRAD_TRY(cudaMalloc(&d_last_count, sizeof(int)));
+        LUMRAD_TRY(cudaMemcpyAsync(d_last_count, dev_count, sizeof(int), cudaMemcpyDeviceToDevice, stream));
+        last_size = p.size;
+        last_R = p.rays_per_probe;
+    }
     const int slot = (int)(n_passes % kRing);
     LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
     LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream));
@@ -568,6 +576,7 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     world.hits_n = 0;
     last.probes = probes;
     last.rays = rays;
+    last_count_on_device = false;
     return LUMRAD_OK;
 }
 
@@ -603,10 +612,11 @@ int Context::build_list_device(bool consume, int* n) {
     if (ns) LUMRAD_TRY(cudaMemcpyAsync(d_specials, specials.data(), ns * sizeof(short4), cudaMemcpyHostToDevice, stream));
     LUMRAD_TRY(launch_update_list(world.d_grid, world.X, world.Y, world.Z, d_specials, (int)ns, list, d_req,
                                   d_list_count, stream));
-    LUMRAD_TRY(cudaMemcpyAsync(h_list_count, d_list_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    LUMRAD_TRY(cudaStreamSynchronize(stream));   // the pass's size is needed on the host
-    *n = *h_list_count;
     if (consume) specials.clear();
+    if (!n) return LUMRAD_OK;   // the length stays on the device
+    LUMRAD_TRY(cudaMemcpyAsync(h_list_count, d_list_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    *n = *h_list_count;
     return LUMRAD_OK;
 }
 
@@ -655,6 +665,7 @@ void Context::release() {
     models.clear();
     cudaFree(d_map_owner);
     if (h_blk) cudaFreeHost(h_blk);
+    cudaFree(d_last_count);
     cudaFree(d_blk_copies);
     if (h_err) cudaFreeHost(h_err);
     if (ev_req) cudaEventDestroy(ev_req);
@@ -971,9 +982,17 @@ int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
     if ((rc = check_unowned(c))) return rc;
     // a frame of Renderer::submitFrame: shift_radiance, then update_radiance (renderer.cpp:436-438)
     if ((rc = c->shift_volume(c->shift[0], c->shift[1], c->shift[2]))) return rc;
-    int n = 0;
-    if ((rc = c->build_list_device(true, &n))) return rc;
-    return c->run_pass(c->d_req, n, params);
+    if (params->record_hits) {   // hit records are sized by the list's length: wait for it
+        int n = 0;
+        if ((rc = c->build_list_device(true, &n))) return rc;
+        return c->run_pass(c->d_req, n, params);
+    }
+    // the pass is launched for the longest list (every block plus the queued specials) and reads
+    // the list's length on the device: the call does not wait for the GPU
+    const long long longest = (long long)c->world.W + (long long)(c->specials.size() / 4);
+    if (longest >= (1LL << 31)) return fail(LUMRAD_EINVAL, "update list too long");
+    if ((rc = c->build_list_device(true, nullptr))) return rc;
+    return c->run_pass(c->d_req, (int)longest, params, c->d_list_count);
 }
 
 int lumrad_shift_radiance(LumRadContext ctx, int dx, int dy, int dz) {
@@ -1216,11 +1235,18 @@ int lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out) {
     if (!c->have_pass) return fail(LUMRAD_ESTATE, "no pass has run");
     LUMRAD_TRY(cudaSetDevice(c->device));
     unsigned long long h[2];
+    int count = 0;
     LUMRAD_TRY(cudaMemcpyAsync(h, c->world.d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    if (c->last_count_on_device)
+        LUMRAD_TRY(cudaMemcpyAsync(&count, c->d_last_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     float ms = 0.0f;
     LUMRAD_TRY(cudaEventElapsedTime(&ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
     *out = c->last;
+    if (c->last_count_on_device) {
+        out->probes = (uint64_t)(count / c->last_size);
+        out->rays = out->probes * (uint64_t)c->last_R;
+    }
     out->steps = h[0];
     out->hits = h[1];
     out->gpu_ms = ms;

@@ -81,6 +81,9 @@ struct LaunchArgs {
     int round_tasks;             // tasks per march/finalize round (0: kChunkTasks); ray_res holds one round
     int in_cta;                  // table launches: 1 if combines_in_cta holds for every world (the lean
                                  // finalize kernel), 0 for the general one
+    // single-world launches sized for the longest possible list: the list's length on the device
+    // (its tasks are (count / size) * R/32; the kernels leave the rest alone), or null
+    const int* dev_count;
     // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
     // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
     int guided_div, max_chunk, march_ctas;

@@ -145,6 +145,11 @@ struct Context {
     bool have_pass = false;
     bool req_copy_pending = false;
     LumRadPassStats last{};
+    // the last pass ran over a device-built list: its probe count is read back when asked for
+    // (d_last_count, copied from the list's length in stream order), in groups of last_size
+    bool last_count_on_device = false;
+    int* d_last_count = nullptr;
+    int last_size = 1, last_R = 0;
 
     // adaptive time slicing state (internal_render.cpp:1190-1203)
     int frame = 0;
@@ -188,15 +193,18 @@ struct Context {
     int ensure_req_capacity(size_t n);
     int ensure_rays(long long n_tasks, long long cap_tasks = kChunkTasks);
     int stage_requests(const int16_t* req, size_t n);
-    int run_pass(const short4* d_req, int n, const LumRadPassParams* p);
+    // One pass over n requests at d_req.  With dev_count, n is the longest the list can be and
+    // the pass covers the first *dev_count requests (a list built on the device, not waited for).
+    int run_pass(const short4* d_req, int n, const LumRadPassParams* p, const int* dev_count = nullptr);
     // n passes in order (requests reqs[i], ns[i] of them, params ps[i], all validated, size >= 1,
     // no hit records): marches of consecutive passes share launches
     int run_passes(const short4* const* reqs, const int* ns, const LumRadPassParams* ps, int n);
     int ensure_pass_table(int n);
     int check_error();
     int handle_error(int e);              // resets the launch counters after a reported error
-    // Builds update_radiance's list on the device into d_req; *n = its length.  The queued
-    // specials are consumed when `consume` is set.
+    // Builds update_radiance's list on the device into d_req; *n = its length (waited for; with
+    // a null n the length stays in d_list_count).  The queued specials are consumed when `consume`
+    // is set.
     int build_list_device(bool consume, int* n);
     int ensure_list_scratch();
     int shift_volume(int dx, int dy, int dz);

@@ -45,7 +45,11 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
     float4* sd = s_ray[wib][1];
     float4* si = s_ray[wib][2];
     const unsigned lt_mask = (1u << lane) - 1u;
-    const int n_round = la.chunk_end - la.chunk_begin;
+    int n_round = la.chunk_end - la.chunk_begin;
+    if (la.dev_count) {   // a list built on the device: its own length bounds the round
+        const long long real = (long long)(__ldcg(la.dev_count) / la.single.size) * (la.single.R >> 5);
+        n_round = (int)max(0LL, min((long long)n_round, real - la.chunk_begin));
+    }
 
     // current world (warp-uniform)
     const WorldPass* wp = &la.single;
@@ -277,7 +281,9 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     const int t = t0 + w;
     const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
     const int t_local = t - (int)wp->task_begin;
-    const bool valid = t < la.chunk_end && t_local < wp->n_tasks;
+    bool valid = t < la.chunk_end && t_local < wp->n_tasks;
+    if (la.dev_count)   // a list built on the device (single world): its own length bounds the tasks
+        valid = valid && t_local < (__ldcg(la.dev_count) / wp->size) * (wp->R >> 5);
     const int nsub = wp->R >> 5;
     const int g = t_local / nsub;
     const int k = t_local - g * nsub;

@@ -228,3 +228,42 @@ def test_blockify_frames_of_different_sizes():
             ref_g, ref_p = oracle.blockify(w.grid, pal, static, models, meshes)
             assert np.array_equal(rw.get_world(), ref_g)
             assert np.array_equal(rw.get_block_palette(), ref_p)
+
+
+def test_update_radiance_frames_without_waiting():
+    """update_radiance launches the pass for the longest list and reads the list's length on the
+    device (no host wait): frames back to back, sliced (size 2), adaptive (size 0) and with
+    specials, equal passes over the oracle's list; the frame's counters survive a later list build."""
+    import lum_gb300
+    import oracle
+    w = _world((10, 9, 7), seed=5)
+    prev = random_prev(w)
+    full = oracle.update_list(w)
+    with _rw(w) as a, _rw(w) as b:
+        a.set_radiance(prev)
+        b.set_radiance(prev)
+        frames = [dict(rays=64, blend=0.1, time_seed=3), dict(rays=128, blend=0.2, time_seed=4, size=2, shift=1),
+                  dict(rays=32, blend=0.1, time_seed=5)]
+        for f in frames:
+            a.update_radiance(lum_gb300.pass_params(**f))
+        for f in frames:
+            b.radiance_pass(full, lum_gb300.pass_params(**f))
+        assert a.get_radiance().tobytes() == b.get_radiance().tobytes()
+        # a special request; the counters of the frame, then another list build
+        a.request_update(2, 3, 1)
+        a.request_update(0, 0, 6)
+        with_specials = oracle.update_list(w, np.array([[2, 3, 1, 0], [0, 0, 6, 0]], np.int16))
+        a.update_radiance(lum_gb300.pass_params(rays=64, blend=0.1, time_seed=6))
+        b.radiance_pass(with_specials, lum_gb300.pass_params(rays=64, blend=0.1, time_seed=6))
+        sa = a.pass_stats()
+        a.build_update_list()   # another list on the device after the frame
+        assert a.pass_stats()["probes"] == sa["probes"] == with_specials.shape[0]
+        sb = b.pass_stats()
+        assert (sa["steps"], sa["hits"], sa["rays"]) == (sb["steps"], sb["hits"], sb["rays"])
+        assert a.get_radiance().tobytes() == b.get_radiance().tobytes()
+    # adaptive slicing (size 0): on a small world every frame stays at size 1, seeded by its index
+    with _rw(w) as a, _rw(w) as b:
+        for k in range(3):
+            a.update_radiance(lum_gb300.pass_params(rays=64, blend=0.1, size=0))
+            b.radiance_pass(full, lum_gb300.pass_params(rays=64, blend=0.1, time_seed=k))
+        assert a.get_radiance().tobytes() == b.get_radiance().tobytes()
