@@ -12,9 +12,14 @@ Workload (one "step"): the 64x64x16-block terrain world plus 2000 random blocks 
   single_pass  the same step as 8 lumrad_radiance_pass_resident calls (one frame's update each).
   e2e        the same metric through the C ABI with host buffers: each step copies its 8 request
              lists host->device (lumrad_radiance_passes) and reads the radiance volume back.
-  roofline   algorithmic bytes of one step (3 B per grid+palette lookup, 16+8*12 B per hit,
-             8+2*12 B per probe; counts exact from the kernels' counters) over the step's kernels'
-             own event-timed duration (march + 8 finalize), against the measured HBM copy peak.
+  roofline   the bound that limits the step's kernels (march + 8 finalize launches): instruction
+             issue.  achieved = warp instructions per step (ncu's smsp__inst_executed.sum over the
+             same 9 launches, NCU_WARP_INST_PER_STEP) / the kernels' own event-timed duration;
+             peak = one warp instruction per cycle on each of the 4 schedulers of every SM at the SM
+             clock sampled during the timed region.  Beside it, the memory rooflines: algorithmic
+             bytes of one step (3 B per grid+palette lookup, 16+8*12 B per hit, 8+2*12 B per probe;
+             counts exact from the kernels' counters) over the same duration, against the
+             measured HBM copy peak and an L2-resident read rate measured in the run.
   cpu_baseline  the CPU oracle (port, OpenMP over all host cores) on whole steps, ~12 s.
 
 --impl reference times the reference's implementation of the same workload on the host cores:
@@ -58,6 +63,10 @@ NCU_DRAM_BYTES_PER_STEP = 165.32e6
 # L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 636.2 MB,
 # finalizes 987.9 MB)
 NCU_L2_BYTES_PER_STEP = 1624.0e6
+# Warp instructions (smsp__inst_executed.sum) of the same 9 launches: the march over the 8 passes
+# and the 8 finalize launches (deterministic up to the march queue's task order)
+NCU_WARP_INST_PER_STEP = 572.0e6 + 8 * 51.5e6
+SCHEDULERS_PER_SM = 4
 
 
 def pass_lists(dims):
@@ -585,7 +594,8 @@ def run_reference(args, rank, world_size, pg):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded value-noise terrain, splitmix64)", "impl": "reference",
-            "config": dict(WORKLOAD, sample=sample),
+            "config": dict(WORKLOAD, l2="flushed between steps (256 MiB write)",
+                           parallelism="replicas" if world_size > 1 else "single GPU"),
             "cpu_baseline": {"value": value, "unit": "probe-rays/s", "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "probe-rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": ("Lum's shaders/radiance.comp compiled as C++ from its source, one process per host core; "
@@ -709,6 +719,7 @@ def main():
 
     hbm_peak, peak_kind = load_peaks()
     l2_peak = l2_read_gbs(local)
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
     bytes_per_launch = float(np.sum(pass_bytes))       # the step's 8 passes: one march launch
     kern_avg_s = float(np.mean(kernel_ms)) / 1000.0    # march + 8 finalize launches of a step
     achieved = bytes_per_launch / kern_avg_s / 1e9
@@ -752,6 +763,10 @@ def main():
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(world, lists)
 
+    clk = clocks.summary()
+    sm_hz = (clk["sm_mhz"] or clk["sm_max_mhz"] or 2070.0) * 1e6
+    issue_peak = SCHEDULERS_PER_SM * num_sms * sm_hz              # warp instructions per second
+    issue_achieved = NCU_WARP_INST_PER_STEP / kern_avg_s
     if rank == 0:
         line = {
             "metric": "probe-rays/s", "value": value, "unit": "probe-rays/s", "n_gpus": world_size,
@@ -762,21 +777,25 @@ def main():
                            parallelism="replicas" if world_size > 1 else "single GPU"),
             "e2e": {"value": e2e_value, "unit": "probe-rays/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": NCU_DRAM_BYTES_PER_STEP, "peak_kind": peak_kind,
-                         "bytes_per_launch": bytes_per_launch, "kernel_ms_avg": kern_avg_s * 1e3,
+            "roofline": {"bound": "issue", "achieved": issue_achieved, "peak": issue_peak, "unit": "warp-inst/s",
+                         "frac": issue_achieved / issue_peak, "traffic": NCU_DRAM_BYTES_PER_STEP,
+                         "peak_kind": f"4 schedulers x {num_sms} SMs x the sampled SM clock",
+                         "warp_inst_per_step": NCU_WARP_INST_PER_STEP, "kernel_ms_avg": kern_avg_s * 1e3,
                          "launch": "one step: a march launch over its 8 passes + 8 finalize launches",
-                         "ray_steps_per_s": float(np.sum(pass_steps)) / kern_avg_s},
-            "l2_roofline": {"achieved": achieved, "peak": l2_peak, "unit": "GB/s", "frac": achieved / l2_peak,
-                            "peak_kind": "measured in this run: L2-resident read (64 row sums over one 24 MiB "
-                                         "array, one launch, best of 5)",
-                            "traffic": NCU_L2_BYTES_PER_STEP},
+                         "ray_steps_per_s": float(np.sum(pass_steps)) / kern_avg_s,
+                         "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                                 "peak_kind": peak_kind, "bytes_per_launch": bytes_per_launch,
+                                 "traffic": NCU_DRAM_BYTES_PER_STEP},
+                         "l2": {"achieved": achieved, "peak": l2_peak, "unit": "GB/s", "frac": achieved / l2_peak,
+                                "peak_kind": "measured in this run: L2-resident read (64 row sums over one 24 MiB "
+                                             "array, one launch, best of 5)",
+                                "traffic": NCU_L2_BYTES_PER_STEP}},
             "single_pass": {"value": job_value(args.steps * rays_per_step, world_size, single_total_ms / 1000.0),
                             "unit": "probe-rays/s", "ms_per_step": single_total_ms / args.steps,
                             "kernel_ms_per_pass": float(np.mean(single_kernel_ms)) / PASSES,
                             "path": "lumrad_radiance_pass_resident once per pass (one frame's update)"},
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
+            "clocks": clk,
             "gpu_launches": (1 + PASSES) * args.steps,   # one march + a finalize per pass, per step
             "batched": batched,
             "serving": serving,

@@ -392,17 +392,41 @@ int  lumrad_dirty_probes(const int* world_size, const LumRadEdit* edits, int n_e
  *   d_palette   n_slots * 4096 uint8 voxels, voxel (x,y,z) at x + 16y + 256z
  *   d_materials 256 * 4 floats: r, g, b, emission
  *   d_requests  n * 4 int16 (x, y, z, w)
- *   d_prev      X*Y*Z * 4 floats (rgb + pad), read;  d_next: same layout, written
+ *   d_prev      X*Y*Z * 4 floats (rgb + pad), read;  d_next: same layout, written; the two must
+ *               not overlap (LUMRAD_EINVAL)
  *   params      rays_per_probe 32, 64, 128 or 256; size >= 1; record_hits 0
  *   stream      a cudaStream_t (NULL = default stream); the pass is enqueued, not awaited
- * The first call on a device looks up the array's device address; make that first call before
- * capturing a stream into a CUDA graph.  All calls share the array: calls that overlap on the
- * GPU (different streams, or threads) race and give wrong results. */
+ * The first call on a device looks up the array's device address and uploads the direction
+ * tables into it (a synchronous copy); make that first call before capturing a stream into a
+ * CUDA graph.  All calls share the array: calls that overlap on the GPU (different streams, or
+ * threads) race and give wrong results.  The call returns before the GPU runs the pass, so it
+ * cannot report a device-side failure itself: the kernels record one in an error word in the
+ * array, which lumrad_radiance_pass_noalloc_status reads. */
 #define LUMRAD_NOALLOC_MAX_BLOCKS (1 << 19)
 int  lumrad_radiance_pass_noalloc(const int* world_size, const int16_t* d_grid, const uint8_t* d_palette,
                                   int n_slots, const float* d_materials, const int16_t* d_requests, int n,
                                   const float* d_prev, float* d_next, const LumRadPassParams* params,
                                   void* stream);
+/* Waits for `stream`, then reads and clears the no-allocation passes' error word of the current
+ * device (allocates nothing): LUMRAD_OK with *device_error = 0 if every such pass since the last
+ * status call completed; else LUMRAD_EDEVICE with the word's bits in *device_error (1: the march
+ * kernel's scheduler stopped making progress; the outputs of those passes are incomplete). */
+int  lumrad_radiance_pass_noalloc_status(void* stream, int* device_error);
+
+/* ---- test hooks (host-side fault injection for this library's own tests) ------------------
+ * Not for production use; no counterpart in the reference.  Each hook changes only what the host
+ * launches or reads for later calls on ctx; nothing faults or waits on the GPU.
+ *   LUMRAD_TEST_LEAN_FINALIZE  value != 0: later passes launch the finalize kernel variant without
+ *       the cross-CTA combine even when a probe's subgroups span CTAs (R/32 not dividing 8, e.g.
+ *       R = 96).  That kernel stores nothing for such probes and sets its error word, so the next
+ *       call that checks it (lumrad_synchronize, lumrad_get_radiance, lumrad_get_pass_stats)
+ *       returns LUMRAD_EDEVICE and the context stays usable.  value 0: normal launches again.
+ *   LUMRAD_TEST_PASS_MS  value >= 0: lumrad_update_radiance's adaptive slicing (size 0) takes
+ *       value as the previous pass's device time in ms instead of measuring it (the reference's
+ *       timestamp query, internal_render.cpp:1190-1203); value < 0: measured again. */
+#define LUMRAD_TEST_LEAN_FINALIZE 1
+#define LUMRAD_TEST_PASS_MS       2
+int  lumrad_test_hook(LumRadContext ctx, int hook, double value);
 
 /* Direction table used for rays_per_probe = R (sphericalFibonacci, radiance.comp:293-314):
  * R*3 floats.  cos/sin are evaluated in double and rounded to float. */

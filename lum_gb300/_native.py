@@ -20,6 +20,8 @@ LUMRAD_EDEVICE = -3
 LUMRAD_ETIMEOUT = -4
 LUMRAD_ESTATE = -5
 LUMRAD_ECANCELED = -6
+LUMRAD_TEST_LEAN_FINALIZE = 1
+LUMRAD_TEST_PASS_MS = 2
 
 PRECISION = {"fp32": 0, "fp16": 1, "bf16": 2}
 
@@ -118,6 +120,8 @@ _SIGS = {
     "lumrad_gather_radiance_device": (C.c_int, [_P, _P, C.c_int, _P]),
     "lumrad_radiance_pass_noalloc": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, C.c_int, _P, _P, C.POINTER(PassParams),
                                                _P]),
+    "lumrad_radiance_pass_noalloc_status": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "lumrad_test_hook": (C.c_int, [_P, C.c_int, C.c_double]),
     "lumrad_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     "lumrad_batch_destroy": (None, [_P]),
     "lumrad_batch_set_requests": (C.c_int, [_P, C.c_int, _P, C.c_int, C.POINTER(PassParams)]),

@@ -172,6 +172,7 @@ int run_graph(Batch* b, int time_seed) {
         dw.cur = 1 - dw.cur;
         dw.hits_recorded = false;
         bw.ctx->have_pass = true;
+        bw.ctx->last_count_on_device = false;   // this pass's list length is known on the host
         bw.ctx->last.probes = (uint64_t)(bw.n / bw.p.size);
         bw.ctx->last.rays = bw.ctx->last.probes * (uint64_t)bw.p.rays_per_probe;
     }

@@ -440,6 +440,7 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
     la.ray_res = d_ray_res;
     la.ray_blk = d_ray_blk;
     la.dev_count = dev_count;
+    la.force_lean = test_lean_finalize ? 1 : 0;
     last_count_on_device = dev_count != nullptr;
     if (dev_count) {
         if (!d_last_count) LUMRAD_TRY(cudaMalloc(&d_last_count, sizeof(int)));
@@ -975,9 +976,13 @@ int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
     if (rc) return rc;
     LUMRAD_TRY(cudaSetDevice(c->device));
     if (params->size == 0 && c->have_pass) {
-        LUMRAD_TRY(cudaEventSynchronize(c->ring1[c->last_slot]));
-        LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
-        c->last_ms /= (float)c->last_slot_passes;   // a frame's pass time after a several-pass call
+        if (c->test_pass_ms >= 0.0f) {
+            c->last_ms = c->test_pass_ms;
+        } else {
+            LUMRAD_TRY(cudaEventSynchronize(c->ring1[c->last_slot]));
+            LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
+            c->last_ms /= (float)c->last_slot_passes;   // a frame's pass time after a several-pass call
+        }
     }
     if ((rc = check_unowned(c))) return rc;
     // a frame of Renderer::submitFrame: shift_radiance, then update_radiance (renderer.cpp:436-438)
@@ -1251,6 +1256,16 @@ int lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out) {
     out->hits = h[1];
     out->gpu_ms = ms;
     return c->check_error();
+}
+
+int lumrad_test_hook(LumRadContext ctx, int hook, double value) {
+    Context* c = as_ctx(ctx);
+    if (!c) return fail(LUMRAD_EINVAL, "null context");
+    switch (hook) {
+        case LUMRAD_TEST_LEAN_FINALIZE: c->test_lean_finalize = value != 0.0; return LUMRAD_OK;
+        case LUMRAD_TEST_PASS_MS: c->test_pass_ms = value >= 0.0 ? (float)value : -1.0f; return LUMRAD_OK;
+        default: return fail(LUMRAD_EINVAL, "unknown test hook");
+    }
 }
 
 int lumrad_get_stream(LumRadContext ctx, void** stream) {

@@ -81,6 +81,8 @@ struct LaunchArgs {
     int round_tasks;             // tasks per march/finalize round (0: kChunkTasks); ray_res holds one round
     int in_cta;                  // table launches: 1 if combines_in_cta holds for every world (the lean
                                  // finalize kernel), 0 for the general one
+    int force_lean;              // test hook: the lean finalize kernel even where a probe's subgroups span
+                                 // CTAs; the kernel then stores nothing for them and sets error bit 2
     // single-world launches sized for the longest possible list: the list's length on the device
     // (its tasks are (count / size) * R/32; the kernels leave the rest alone), or null
     const int* dev_count;

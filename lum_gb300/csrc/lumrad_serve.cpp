@@ -464,6 +464,7 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
         sw.last_slot = k;
         sw.ctx->world.cur = 1 - sw.ctx->world.cur;
         sw.ctx->have_pass = true;
+        sw.ctx->last_count_on_device = false;
     }
     sl.busy = true;
     sl.start = now;

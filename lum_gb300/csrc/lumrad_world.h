@@ -155,6 +155,10 @@ struct Context {
     int frame = 0;
     int magic_size = 1;
     float last_ms = 0.0f;
+    // test hooks (lumrad_test_hook): the lean finalize kernel on every pass; a fixed previous-pass
+    // time for adaptive slicing (< 0: measured)
+    bool test_lean_finalize = false;
+    float test_pass_ms = -1.0f;
     // radiance shift applied before each lumrad_update_radiance (Renderer::stored_radiance_shift)
     int shift[3] = {0, 0, 0};
     // voxel models for blockify / map (InternalMeshModel::voxels)

@@ -125,6 +125,15 @@ __device__ __forceinline__ int voxel_value(const WorldPass& w, int ix, int iy, i
     return __ldg(w.pal + ((slot << 12) | ((iz & 15) << 8) | ((iy & 15) << 4) | (ix & 15)));
 }
 
+// t / nsub for t >= 0 (nsub = R/32: a power of two for the usual ray counts, a shift then)
+__device__ __forceinline__ int div_nsub(int t, int nsub) {
+#if LUMRAD_OPT_NSUB
+    return (nsub & (nsub - 1)) == 0 ? t >> (__ffs(nsub) - 1) : t / nsub;
+#else
+    return t / nsub;
+#endif
+}
+
 // ---------------------------------------------------------------- ray setup (:362-381)
 __device__ __forceinline__ float3 hash33(uint32_t x, uint32_t y, uint32_t z) {
     const uint32_t k = 1103515245u;
@@ -141,7 +150,11 @@ __device__ __forceinline__ float3 hash33(uint32_t x, uint32_t y, uint32_t z) {
 
 __device__ __forceinline__ float3 normalize3(float3 v) {
     const float dd = fadd(fadd(fmul(v.x, v.x), fmul(v.y, v.y)), fmul(v.z, v.z));
+#if LUMRAD_OPT_RCP
+    const float s = __frcp_rn(__fsqrt_rn(dd));   // 1/x rounded once == the reciprocal rounded once
+#else
     const float s = fdiv(1.0f, __fsqrt_rn(dd));
+#endif
     return make_float3(fmul(v.x, s), fmul(v.y, s), fmul(v.z, s));
 }
 

@@ -97,11 +97,24 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         }
         return tb;
     };
+#if LUMRAD_OPT_MAGIC
+    // the far corner's offset in a block (16 or 0 per axis) plus the bits of 1.5 * 2^23: the
+    // float with bits m + v is 12582912 + v exactly for |v| < 2^22 (every block coordinate a ray
+    // reaches: |position| < 2^20), so a block corner is one integer add and one float subtract
+    // (no int -> float conversion)
+    int cxm = 0, cym = 0, czm = 0;
+    auto corner = [&]() {
+        cxm = 0x4B400000 + (dx > 0.0f ? 16 : 0);
+        cym = 0x4B400000 + (dy > 0.0f ? 16 : 0);
+        czm = 0x4B400000 + (dz > 0.0f ? 16 : 0);
+    };
+#else
     auto corner = [&]() {
         cx = dx > 0.0f ? 16.0f : 0.0f;
         cy = dy > 0.0f ? 16.0f : 0.0f;
         cz = dz > 0.0f ? 16.0f : 0.0f;
     };
+#endif
     // hand the next rays in ring order to the lanes in `need`
     auto assign = [&](unsigned need) {
         const int avail = loaded - issued;
@@ -161,7 +174,7 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             // lane i builds ray i of the task (subgroup k of workgroup g)
             const int t_local = t - w_begin;
             const int nsub = wp->R >> 5;
-            const int g = t_local / nsub;
+            const int g = div_nsub(t_local, nsub);
             float3 o, d;
             setup_ray(*wp, g, (t_local - g * nsub) * kTaskRays + lane, o, d);
             const int base = (t - la.chunk_begin) * kTaskRays;
@@ -208,9 +221,15 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                     const bool solid = solid_at(mv, ix, iy, iz, cid);
                     if (cid == 0) {
                         // empty block: skip to its far corner (radiance.comp:215-226)
+#if LUMRAD_OPT_MAGIC
+                        const float bx = fsub(__int_as_float((ix / 16) * 16 + cxm), 12582912.0f);
+                        const float by = fsub(__int_as_float((iy / 16) * 16 + cym), 12582912.0f);
+                        const float bz = fsub(__int_as_float((iz / 16) * 16 + czm), 12582912.0f);
+#else
                         const float bx = fadd((float)((ix / 16) * 16), cx);
                         const float by = fadd((float)((iy / 16) * 16), cy);
                         const float bz = fadd((float)((iz / 16) * 16), cz);
+#endif
                         const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
                         const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
                         const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
@@ -285,7 +304,7 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
     if (la.dev_count)   // a list built on the device (single world): its own length bounds the tasks
         valid = valid && t_local < (__ldcg(la.dev_count) / wp->size) * (wp->R >> 5);
     const int nsub = wp->R >> 5;
-    const int g = t_local / nsub;
+    const int g = div_nsub(max(t_local, 0), nsub);
     const int k = t_local - g * nsub;
     // a probe's subgroups share this CTA when R/32 divides 8 (task_begin is a multiple of 8)
     const bool local = nsub > 1 && (kFinWarps % nsub) == 0 && (wp->task_begin % kFinWarps) == 0;
@@ -382,7 +401,8 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
         args.ray_origin = args.chunk_begin;
         const int n = args.chunk_end - args.chunk_begin;
         march_kernel<RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
-        launch_finalize<Store, RECORD>(args, n, a.worlds ? a.in_cta != 0 : combines_in_cta(&a.single, 1), stream);
+        const bool lean = a.force_lean || (a.worlds ? a.in_cta != 0 : combines_in_cta(&a.single, 1));
+        launch_finalize<Store, RECORD>(args, n, lean, stream);
     }
     return cudaGetLastError();
 }
@@ -513,8 +533,10 @@ constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 constexpr size_t kNaCgrid = 0;                                                        // uint16 per block
 constexpr size_t kNaCbits = align256(kNaCgrid + 2 * (size_t)kNoAllocMaxBlocks);      // 512 B per compact id
 constexpr size_t kNaRayRes = align256(kNaCbits + (size_t)(LUMRAD_MAX_BLOCK_SLOTS + 2) * 512);
+// the direction tables for R = 32, 64, 128, 256 back to back (480 entries), uploaded once per device
 constexpr size_t kNaDirs = align256(kNaRayRes + (size_t)kNoAllocRoundTasks * kTaskRays * sizeof(uint2));
-constexpr size_t kNaQueue = align256(kNaDirs + 256 * sizeof(float4));
+constexpr int kNaDirEntries = 32 + 64 + 128 + 256;
+constexpr size_t kNaQueue = align256(kNaDirs + kNaDirEntries * sizeof(float4));
 constexpr size_t kNaError = kNaQueue + kQueueWords * sizeof(unsigned long long);
 constexpr size_t kNaStats = align256(kNaError + sizeof(int));
 constexpr size_t kNaBytes = align256(kNaStats + 2 * sizeof(unsigned long long));
@@ -564,8 +586,39 @@ struct NoAllocDevice {
 };
 std::mutex g_noalloc_mutex;
 NoAllocDevice g_noalloc_dev[64];
-float4 g_noalloc_dirs[4][256];       // host copies of the direction tables for R = 32, 64, 128, 256
-bool g_noalloc_dirs_ready = false;
+
+// Offset (entries) of the direction table for R rays in the array's table area.
+int noalloc_dir_offset(int R) { return R == 32 ? 0 : R == 64 ? 32 : R == 128 ? 96 : 224; }
+
+// The array's device address on the current device, set up on the first call there: the address
+// lookup, the SM count and the four direction tables (one synchronous upload, before any pass of
+// this device can read them).  Sets *out to null on failure (and returns the status).
+int noalloc_device(NoAllocDevice** out) {
+    *out = nullptr;
+    int dev = 0;
+    LUMRAD_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(LUMRAD_EINVAL, "device ordinal beyond 63");
+    NoAllocDevice* nd = &g_noalloc_dev[dev];
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!nd->ready) {
+        void* addr = nullptr;
+        LUMRAD_TRY(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
+        LUMRAD_TRY(cudaDeviceGetAttribute(&nd->num_sms, cudaDevAttrMultiProcessorCount, dev));
+        float4 tab[kNaDirEntries];
+        float xyz[3 * 256];
+        for (int R = 32; R <= 256; R *= 2) {
+            fibonacci_table(R, xyz);
+            for (int i = 0; i < R; i++)
+                tab[noalloc_dir_offset(R) + i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
+        }
+        unsigned char* base = static_cast<unsigned char*>(addr);
+        LUMRAD_TRY(cudaMemcpy(base + kNaDirs, tab, sizeof tab, cudaMemcpyHostToDevice));
+        nd->base = base;
+        nd->ready = true;
+    }
+    *out = nd;
+    return LUMRAD_OK;
+}
 
 }  // namespace
 }  // namespace lumrad
@@ -588,6 +641,11 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
         if (world_size[i] < 1 || world_size[i] > 2047) return fail(LUMRAD_EINVAL, "world_size must be in [1, 2047] per axis");
     const long long W = (long long)world_size[0] * world_size[1] * world_size[2];
     if (W > kNoAllocMaxBlocks) return fail(LUMRAD_EINVAL, "world larger than LUMRAD_NOALLOC_MAX_BLOCKS blocks");
+    {   // the pass reads prev while it writes next: the two volumes must not share bytes
+        const uintptr_t a = reinterpret_cast<uintptr_t>(d_prev), b = reinterpret_cast<uintptr_t>(d_next);
+        const uintptr_t bytes = (uintptr_t)W * sizeof(float4);
+        if (a < b + bytes && b < a + bytes) return fail(LUMRAD_EINVAL, "d_prev and d_next overlap");
+    }
     if (n_slots < 1 || n_slots > LUMRAD_MAX_BLOCK_SLOTS) return fail(LUMRAD_EINVAL, "n_slots must be in [1, 4096]");
     if (n < 0) return fail(LUMRAD_EINVAL, "negative request count");
     const long long groups = n / p->size;
@@ -595,46 +653,22 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     if (n_tasks >= (1LL << 31)) return fail(LUMRAD_EINVAL, "pass has too many subgroups (>= 2^31)");
     cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_handle);
 
-    // set-up, once per device: the array's device address (first call on a device; make that
-    // call before capturing a stream into a graph)
-    int dev = 0;
-    LUMRAD_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return fail(LUMRAD_EINVAL, "device ordinal beyond 63");
-    NoAllocDevice* nd = &g_noalloc_dev[dev];
-    {
-        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!nd->ready) {
-            void* addr = nullptr;
-            LUMRAD_TRY(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
-            LUMRAD_TRY(cudaDeviceGetAttribute(&nd->num_sms, cudaDevAttrMultiProcessorCount, dev));
-            nd->base = static_cast<unsigned char*>(addr);
-            nd->ready = true;
-        }
-        if (!g_noalloc_dirs_ready) {
-            const int rs[4] = {32, 64, 128, 256};
-            float xyz[3 * 256];
-            for (int k = 0; k < 4; k++) {
-                fibonacci_table(rs[k], xyz);
-                for (int i = 0; i < rs[k]; i++)
-                    g_noalloc_dirs[k][i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
-            }
-            g_noalloc_dirs_ready = true;
-        }
-    }
+    // set-up, once per device (the first call there; make that call before capturing a stream
+    // into a graph): the array's device address and the direction tables
+    NoAllocDevice* nd = nullptr;
+    if ((rc = noalloc_device(&nd))) return rc;
     unsigned char* base = nd->base;
     uint16_t* cgrid = reinterpret_cast<uint16_t*>(base + kNaCgrid);
     uint32_t* cbits = reinterpret_cast<uint32_t*>(base + kNaCbits);
-    float4* dirs = reinterpret_cast<float4*>(base + kNaDirs);
+    const float4* dirs = reinterpret_cast<const float4*>(base + kNaDirs) + noalloc_dir_offset(R);
     unsigned long long* queue = reinterpret_cast<unsigned long long*>(base + kNaQueue);
     int* error = reinterpret_cast<int*>(base + kNaError);
     unsigned long long* stats = reinterpret_cast<unsigned long long*>(base + kNaStats);
-    const int r_index = R == 32 ? 0 : R == 64 ? 1 : R == 128 ? 2 : 3;
 
-    // everything that must start at zero, and this call's inputs derived into the array
+    // what must start at zero (the error word is kept until lumrad_radiance_pass_noalloc_status
+    // reads it), and this call's inputs derived into the array
     LUMRAD_TRY(cudaMemsetAsync(queue, 0, kQueueWords * sizeof(unsigned long long), stream));
-    LUMRAD_TRY(cudaMemsetAsync(error, 0, sizeof(int), stream));
     LUMRAD_TRY(cudaMemsetAsync(stats, 0, 2 * sizeof(unsigned long long), stream));
-    LUMRAD_TRY(cudaMemcpyAsync(dirs, g_noalloc_dirs[r_index], R * sizeof(float4), cudaMemcpyHostToDevice, stream));
     noalloc_compact_grid<<<256, 256, 0, stream>>>(d_grid, (int)W, n_slots, cgrid);
     noalloc_compact_bits<<<256, 256, 0, stream>>>(d_palette, n_slots, cbits);
     LUMRAD_TRY(cudaGetLastError());
@@ -691,4 +725,22 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     }
     LUMRAD_TRY(cudaGetLastError());
     return LUMRAD_OK;
+}
+
+extern "C" int lumrad_radiance_pass_noalloc_status(void* stream_handle, int* device_error) {
+    if (!device_error) return fail(LUMRAD_EINVAL, "null argument");
+    *device_error = 0;
+    NoAllocDevice* nd = nullptr;
+    if (int rc = noalloc_device(&nd)) return rc;
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_handle);
+    int* error = reinterpret_cast<int*>(nd->base + kNaError);
+    int word = 0;
+    LUMRAD_TRY(cudaMemcpyAsync(&word, error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    if (word == 0) return LUMRAD_OK;
+    LUMRAD_TRY(cudaMemsetAsync(error, 0, sizeof(int), stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    *device_error = word;
+    return fail(LUMRAD_EDEVICE, "a no-allocation pass since the last status call did not complete (radiance "
+                                "kernel scheduler stopped making progress, code " + std::to_string(word) + ")");
 }

@@ -27,7 +27,9 @@ BLEND = 0.1
 FLOOR = 1e-3
 
 
-def main(dims=DIMS, passes=PASSES) -> int:
+def measure(dims=DIMS, passes=PASSES, precisions=("fp32", "fp16", "bf16")):
+    """Runs the workload; returns {"rows": {prec: [(max rel, RMS rel, max abs) per pass]},
+    "hits_ok": {prec: bool}, "probes", "subset", "oracle_s", "threads"}."""
     import lum_gb300
     import oracle
     w = worldgen.terrain_world(dims, seed=1234, n_types=32)
@@ -48,7 +50,7 @@ def main(dims=DIMS, passes=PASSES) -> int:
 
     rows = {}
     hits_ok = {}
-    for prec in ("fp32", "fp16", "bf16"):
+    for prec in precisions:
         with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], precision=prec) as rw:
             rw.load(w)
             rw.radiance_pass(sub, lum_gb300.pass_params(rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=0,
@@ -63,10 +65,16 @@ def main(dims=DIMS, passes=PASSES) -> int:
                 rel = d / np.maximum(np.abs(ref[p]), FLOOR)
                 out.append((float(rel.max()), float(np.sqrt(np.mean(rel ** 2))), float(d.max())))
             rows[prec] = out
+    return {"rows": rows, "hits_ok": hits_ok, "probes": int(req.shape[0]), "subset": int(sub.shape[0]),
+            "oracle_s": t_oracle, "threads": oracle.max_threads()}
 
-    print(f"World {dims[0]}x{dims[1]}x{dims[2]} blocks, {req.shape[0]} probes x {RAYS} rays, max_dist {MAX_DIST:g}, "
-          f"blend {BLEND}, {passes} passes from zero; FP64 oracle {t_oracle:.1f} s on {oracle.max_threads()} threads.")
-    print(f"Hit records bit-exact vs the FP64 oracle on {sub.shape[0]} probes: "
+
+def main(dims=DIMS, passes=PASSES) -> int:
+    m = measure(dims, passes)
+    rows, hits_ok, t_oracle = m["rows"], m["hits_ok"], m["oracle_s"]
+    print(f"World {dims[0]}x{dims[1]}x{dims[2]} blocks, {m['probes']} probes x {RAYS} rays, max_dist {MAX_DIST:g}, "
+          f"blend {BLEND}, {passes} passes from zero; FP64 oracle {t_oracle:.1f} s on {m['threads']} threads.")
+    print(f"Hit records bit-exact vs the FP64 oracle on {m['subset']} probes: "
           + ", ".join(f"{k} {'yes' if v else 'NO'}" for k, v in hits_ok.items()))
     print()
     print("| pass | FP32 max rel | FP32 RMS rel | FP16 max rel | FP16 RMS rel | BF16 max rel | BF16 RMS rel |")

@@ -22,3 +22,7 @@ def test_reference_arm_line():
     cb = line["cpu_baseline"]
     assert cb["value"] == line["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # the same config object as the GPU arm's line, so the two lines compare as one workload
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == dict(bench.WORKLOAD, l2="flushed between steps (256 MiB write)", parallelism="single GPU")

@@ -267,3 +267,37 @@ def test_update_radiance_frames_without_waiting():
             a.update_radiance(lum_gb300.pass_params(rays=64, blend=0.1, size=0))
             b.radiance_pass(full, lum_gb300.pass_params(rays=64, blend=0.1, time_seed=k))
         assert a.get_radiance().tobytes() == b.get_radiance().tobytes()
+
+
+def test_adaptive_slicing_grows_and_shrinks():
+    """magicSize adaptation of update_radiance (internal_render.cpp:1190-1203): a previous pass
+    slower than 2.2 ms grows the slice by one, faster than 1.8 ms shrinks it, in between keeps it,
+    clamped to [1, 10]; frame k then updates requests shift = k % size, shift + size, ... with
+    time seed k.  The previous pass's time is set through the test hook (the reference reads its
+    timestamp query), so the sequence of slices is known; every frame equals lumrad_radiance_pass
+    with that size, shift and seed over the oracle's update list."""
+    import lum_gb300
+    import oracle
+    from lum_gb300 import _native as N
+    w = _world((10, 9, 7), seed=6)
+    full = oracle.update_list(w)
+    prev = random_prev(w)
+    # (previous pass ms as the hook reports it, slice size the frame must use); frame 0 has no
+    # previous pass (0 ms: size stays 1)
+    plan = [(None, 1), (3.0, 2), (2.5, 3), (2.0, 3), (1.9, 3), (1.0, 2), (0.5, 1), (0.5, 1)]
+    plan += [(9.0, s) for s in range(2, 11)] + [(9.0, 10), (2.2, 10), (1.8, 10), (1.79, 9)]
+    with _rw(w) as a, _rw(w) as b:
+        a.set_radiance(prev)
+        b.set_radiance(prev)
+        for k, (ms, size) in enumerate(plan):
+            if ms is not None:
+                N.check(a.lib.lumrad_test_hook(a.h, N.LUMRAD_TEST_PASS_MS, ms))
+            a.update_radiance(lum_gb300.pass_params(rays=32, blend=0.2, size=0))
+            b.radiance_pass(full, lum_gb300.pass_params(rays=32, blend=0.2, size=size, shift=k % size, time_seed=k))
+            assert a.pass_stats()["probes"] == b.pass_stats()["probes"] == full.shape[0] // size, k
+            assert a.get_radiance().tobytes() == b.get_radiance().tobytes(), (k, ms, size)
+        N.check(a.lib.lumrad_test_hook(a.h, N.LUMRAD_TEST_PASS_MS, -1.0))   # measured again
+        a.update_radiance(lum_gb300.pass_params(rays=32, blend=0.2, size=0))   # a small pass: < 1.8 ms
+        b.radiance_pass(full, lum_gb300.pass_params(rays=32, blend=0.2, size=8, shift=len(plan) % 8,
+                                                    time_seed=len(plan)))
+        assert a.get_radiance().tobytes() == b.get_radiance().tobytes()

@@ -79,3 +79,40 @@ def test_batch_and_server_reject_bad_requests():
             assert srv.cancel(12345) is False
         with pytest.raises(Exception):
             lum_gb300.RadianceServer(precision="fp32", max_inflight=9)
+
+
+def test_finalize_error_word_reported_and_context_recovers():
+    """The finalize kernel's error path, driven from the host: a pass whose probes span finalize
+    CTAs (R = 96: 3 subgroups, 8 per CTA) launched with the variant that has no cross-CTA combine.
+    That kernel stores nothing for such probes and sets bit 2 of the context's error word; the next
+    call that reads the word returns LUMRAD_EDEVICE, resets it, and the context's next pass equals
+    the oracle (on the volume the failed pass left: its copy of the previous one)."""
+    import lum_gb300
+    import oracle
+    from lum_gb300 import _native as N
+    w = worldgen.terrain_world((7, 6, 5), seed=53, n_types=8)
+    req = worldgen.all_probes(w.dims)
+    prev = random_prev(w)
+    p = dict(rays=96, max_dist=128.0, blend=0.1)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        rw.set_radiance(prev)
+        N.check(rw.lib.lumrad_test_hook(rw.h, N.LUMRAD_TEST_LEAN_FINALIZE, 1.0))
+        rw.radiance_pass(req, lum_gb300.pass_params(time_seed=1, **p))   # enqueued; not awaited
+        with pytest.raises(lum_gb300.LumRadError) as ei:
+            rw.synchronize()
+        assert ei.value.code == N.LUMRAD_EDEVICE and "spanning CTAs" in str(ei.value)
+        rw.synchronize()   # the word was reset
+        assert np.array_equal(rw.get_radiance(), np.clip(prev, 0, 1))   # nothing was stored
+        N.check(rw.lib.lumrad_test_hook(rw.h, N.LUMRAD_TEST_LEAN_FINALIZE, 0.0))
+        rw.radiance_pass(req, lum_gb300.pass_params(time_seed=2, **p))
+        got = rw.get_radiance()
+    ref, _, _ = oracle.radiance_pass(w, req, prev=prev, time_seed=2, **p)
+    assert rel_err(got, ref).max() <= RTOL
+
+
+def test_unknown_test_hook_rejected():
+    import lum_gb300
+    from lum_gb300 import _native as N
+    with lum_gb300.RadianceWorld((2, 2, 2), max_block_types=2) as rw:
+        assert rw.lib.lumrad_test_hook(rw.h, 99, 1.0) == N.LUMRAD_EINVAL
