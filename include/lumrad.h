@@ -21,7 +21,8 @@
  *   - a pass reads the previous volume and writes a new one (ping-pong): the shader binds the
  *     same image for read and write (internal_render.cpp:240-241), which races;
  *   - radiance is stored as FP32 (or FP16/BF16) RGB clamped to [0,1] — the clamp of the
- *     A2B10G10R10_UNORM image, without its 10-bit quantisation;
+ *     A2B10G10R10_UNORM image, without its 10-bit quantisation — or, with
+ *     LUMRAD_PRECISION_RGB10A2, in that format itself (round to nearest even);
  *   - world size and rays per probe are runtime values (consts.glsl:1, radiance.comp:37);
  *   - the trilinear radiance fetch uses exact FP32 weights (hardware uses 8-bit weights);
  *   - the subgroup sum is a fixed xor-butterfly order; the coarse march stops after
@@ -56,6 +57,11 @@ extern "C" {
 #define LUMRAD_PRECISION_FP32 0
 #define LUMRAD_PRECISION_FP16 1
 #define LUMRAD_PRECISION_BF16 2
+/* The reference's own volume format, A2B10G10R10_UNORM_PACK32 (radiance.comp:20-21,
+ * internal_render.cpp:128-135), 4 B per probe: each channel clamped to [0,1] and stored as the
+ * round-to-nearest-even of v * 1023 in FP32 (alpha bits = 3); read back as code / 1023 rounded
+ * once to FP32.  With it the drop-in's volume is the reference's, format included. */
+#define LUMRAD_PRECISION_RGB10A2 3
 
 typedef void* LumRadContext;
 

@@ -23,7 +23,7 @@ LUMRAD_ECANCELED = -6
 LUMRAD_TEST_LEAN_FINALIZE = 1
 LUMRAD_TEST_PASS_MS = 2
 
-PRECISION = {"fp32": 0, "fp16": 1, "bf16": 2}
+PRECISION = {"fp32": 0, "fp16": 1, "bf16": 2, "rgb10a2": 3}
 
 
 class Settings(C.Structure):

@@ -59,7 +59,7 @@ int DeviceWorld::init(int X_, int Y_, int Z_, int slots, int precision_, cudaStr
     W = (size_t)X * Y * Z;
     n_slots = slots;
     precision = precision_;
-    rad_stride = precision == LUMRAD_PRECISION_FP32 ? 16 : 8;
+    rad_stride = radiance_stride(precision);
     h_grid.assign(W, 0);
     h_pal.assign((size_t)n_slots * 4096, 0);
     h_pal_dev.assign((size_t)n_slots * 4096, 0);
@@ -712,7 +712,7 @@ int lumrad_create(const LumRadSettings* s, LumRadContext* out) {
     if (W >= (1ull << 31)) return fail(LUMRAD_EINVAL, "world has too many blocks (>= 2^31)");
     if (s->max_block_types < 1 || s->max_block_types > LUMRAD_MAX_BLOCK_SLOTS)
         return fail(LUMRAD_EINVAL, "max_block_types must be in [1, 4096]");
-    if (s->precision < 0 || s->precision > 2) return fail(LUMRAD_EINVAL, "unknown precision");
+    if (s->precision < 0 || s->precision > LUMRAD_PRECISION_RGB10A2) return fail(LUMRAD_EINVAL, "unknown precision");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(LUMRAD_EDEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
@@ -890,6 +890,12 @@ int lumrad_set_radiance(LumRadContext ctx, const float* rgb) {
         for (size_t i = 0; i < w.W; i++)
             h[i] = make_float4(unorm_clamp(rgb[3 * i]), unorm_clamp(rgb[3 * i + 1]), unorm_clamp(rgb[3 * i + 2]), 1.0f);
         LUMRAD_TRY(cudaMemcpyAsync(w.d_rad[w.cur], h.data(), w.W * 16, cudaMemcpyHostToDevice, c->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    } else if (w.precision == LUMRAD_PRECISION_RGB10A2) {
+        std::vector<uint32_t> h(w.W);
+        for (size_t i = 0; i < w.W; i++)
+            h[i] = rgb10a2_pack_host(unorm_clamp(rgb[3 * i]), unorm_clamp(rgb[3 * i + 1]), unorm_clamp(rgb[3 * i + 2]));
+        LUMRAD_TRY(cudaMemcpyAsync(w.d_rad[w.cur], h.data(), w.W * 4, cudaMemcpyHostToDevice, c->stream));
         LUMRAD_TRY(cudaStreamSynchronize(c->stream));
     } else {
         std::vector<uint16_t> h(w.W * 4);

@@ -546,7 +546,7 @@ int lumrad_dirty_probes(const int* world_size, const LumRadEdit* edits, int n_ed
 int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
     if (!s || !out) return fail(LUMRAD_EINVAL, "null argument");
     *out = nullptr;
-    if (s->precision < 0 || s->precision > 2) return fail(LUMRAD_EINVAL, "unknown precision");
+    if (s->precision < 0 || s->precision > LUMRAD_PRECISION_RGB10A2) return fail(LUMRAD_EINVAL, "unknown precision");
     if (s->max_inflight < 0 || s->max_inflight > 8) return fail(LUMRAD_EINVAL, "max_inflight must be in [0, 8]");
     if (s->radius < 0 || s->radius > 15) return fail(LUMRAD_EINVAL, "radius must be in [0, 15]");
     if (s->hbm_budget_bytes < 0 || s->max_requests_per_launch < 0) return fail(LUMRAD_EINVAL, "negative limit");
@@ -725,6 +725,10 @@ int lumrad_server_get_radiance(LumRadServer server, int world, float* rgb) {
                 float v;
                 if (dw.precision == LUMRAD_PRECISION_FP32) {
                     std::memcpy(&v, dw.h_rad_saved.data() + 16 * i + 4 * k, 4);
+                } else if (dw.precision == LUMRAD_PRECISION_RGB10A2) {
+                    uint32_t word;
+                    std::memcpy(&word, dw.h_rad_saved.data() + 4 * i, 4);
+                    v = unorm10_decode_host((word >> (10 * k)) & 1023u);
                 } else {
                     uint16_t bits;
                     std::memcpy(&bits, dw.h_rad_saved.data() + 8 * i + 2 * k, 2);

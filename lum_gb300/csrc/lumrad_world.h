@@ -5,6 +5,7 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
+#include <cmath>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -23,6 +24,18 @@ struct NvtxRange {
     NvtxRange(const NvtxRange&) = delete;
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
+
+// Host side of the A2B10G10R10_UNORM format (the device side: StoreRGB10A2): a clamped value's
+// code is the round-to-nearest-even of v * 1023 in FP32; a code reads back as code / 1023.
+inline uint32_t unorm10_encode_host(float v) { return (uint32_t)std::nearbyint(v * 1023.0f); }
+inline float unorm10_decode_host(uint32_t q) { return (float)q / 1023.0f; }
+inline uint32_t rgb10a2_pack_host(float r, float g, float b) {
+    return unorm10_encode_host(r) | (unorm10_encode_host(g) << 10) | (unorm10_encode_host(b) << 20) | (3u << 30);
+}
+// Bytes per probe of a radiance volume stored at `precision`.
+inline size_t radiance_stride(int precision) {
+    return precision == LUMRAD_PRECISION_FP32 ? 16 : precision == LUMRAD_PRECISION_RGB10A2 ? 4 : 8;
+}
 
 extern thread_local std::string g_error;
 int fail(int code, const std::string& msg);

@@ -373,6 +373,9 @@ cudaError_t launch_pack_rgb(const void* rad, int precision, long long W, float* 
         case LUMRAD_PRECISION_BF16:
             pack_rgb_kernel<StoreBF16><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(rad), out, W);
             break;
+        case LUMRAD_PRECISION_RGB10A2:
+            pack_rgb_kernel<StoreRGB10A2><<<blocks, 256, 0, stream>>>(static_cast<const unsigned*>(rad), out, W);
+            break;
         default:
             pack_rgb_kernel<StoreF32><<<blocks, 256, 0, stream>>>(static_cast<const float4*>(rad), out, W);
     }
@@ -447,6 +450,9 @@ cudaError_t launch_shift_radiance(const void* src, void* dst, int X, int Y, int 
     if (precision == LUMRAD_PRECISION_FP32)
         shift_kernel<uint4><<<blocks, 256, 0, stream>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), X, Y,
                                                         Z, sx, sy, sz, W);
+    else if (precision == LUMRAD_PRECISION_RGB10A2)
+        shift_kernel<unsigned><<<blocks, 256, 0, stream>>>(static_cast<const unsigned*>(src), static_cast<unsigned*>(dst),
+                                                           X, Y, Z, sx, sy, sz, W);
     else
         shift_kernel<uint2><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(src), static_cast<uint2*>(dst), X, Y,
                                                         Z, sx, sy, sz, W);
@@ -463,6 +469,10 @@ cudaError_t launch_gather(const void* rad, int X, int Y, int Z, int precision, c
             break;
         case LUMRAD_PRECISION_BF16:
             gather_kernel<StoreBF16><<<blocks, 256, 0, stream>>>(static_cast<const uint2*>(rad), X, Y, Z, pts, n, out);
+            break;
+        case LUMRAD_PRECISION_RGB10A2:
+            gather_kernel<StoreRGB10A2><<<blocks, 256, 0, stream>>>(static_cast<const unsigned*>(rad), X, Y, Z, pts, n,
+                                                                    out);
             break;
         default:
             gather_kernel<StoreF32><<<blocks, 256, 0, stream>>>(static_cast<const float4*>(rad), X, Y, Z, pts, n, out);

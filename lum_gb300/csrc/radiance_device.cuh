@@ -78,6 +78,30 @@ struct StoreBF16 {
     }
 };
 
+// The reference's own volume format, A2B10G10R10_UNORM_PACK32 (radiance.comp:20-21,
+// internal_render.cpp:128-135): R in bits 0-9, G 10-19, B 20-29, alpha 30-31 (stored as 3).
+// Store: clamp to [0,1] (NaN -> 0; the caller has clamped), code = round-to-nearest-even of
+// v * 1023 in FP32.  Load: code / 1023 rounded once to FP32, as r0 = code * RN(1/1023) and one
+// FMA correction step (exact for every one of the 1024 codes; a test checks them all).
+__device__ __forceinline__ unsigned unorm10_encode(float v) { return __float2uint_rn(fmul(v, 1023.0f)); }
+__device__ __forceinline__ float unorm10_decode(unsigned q) {
+    const float c = __uint_as_float(0x3a802008u);   // RN(1/1023)
+    const float qf = (float)q;                      // exact: q < 1024
+    const float r0 = fmul(qf, c);
+    const float e = __fmaf_rn(-r0, 1023.0f, qf);    // q - r0 * 1023, exact
+    return __fmaf_rn(e, c, r0);
+}
+struct StoreRGB10A2 {
+    typedef unsigned T;
+    static __device__ __forceinline__ float3 load(const T* p, int i) {
+        const unsigned v = __ldg(p + i);
+        return make_float3(unorm10_decode(v & 1023u), unorm10_decode((v >> 10) & 1023u), unorm10_decode((v >> 20) & 1023u));
+    }
+    static __device__ __forceinline__ void store(T* p, int i, float3 v) {
+        p[i] = unorm10_encode(v.x) | (unorm10_encode(v.y) << 10) | (unorm10_encode(v.z) << 20) | (3u << 30);
+    }
+};
+
 // ---------------------------------------------------------------- voxel lookups
 // GetVoxel (radiance.comp:121-143) on integer voxel coordinates.  Block coordinate = ix/16
 // truncated (OpSDiv); voxel in block = ix mod 16 floored (OpSMod) = ix & 15.  The grid fetch is
@@ -112,6 +136,18 @@ __device__ __forceinline__ bool solid_at(const MarchView& m, int ix, int iy, int
     return (word >> (((iy & 1) << 4) | (ix & 15))) & 1u;
 }
 
+// The same with the compact id's width known at compile time (WIDE: uint16 ids, else uint8).
+template <bool WIDE>
+__device__ __forceinline__ bool solid_at_w(const MarchView& m, int ix, int iy, int iz, int& cid) {
+    int idx;
+    int c = 0;
+    if (grid_index(m.X, m.Y, m.Z, ix, iy, iz, idx))
+        c = WIDE ? (int)__ldg(reinterpret_cast<const uint16_t*>(m.cgrid) + idx) : (int)__ldg(m.cgrid + idx);
+    cid = c;
+    const uint32_t word = __ldg(m.cbits + ((c << 7) | ((iz & 15) << 3) | ((iy & 15) >> 1)));
+    return (word >> (((iy & 1) << 4) | (ix & 15))) & 1u;
+}
+
 // Original lookup (voxel value and block id): block id b addresses palette slot
 // (b mod 64) + 64*(b/64) (voxel_in_palette :105-110 on the 64x64-slot image): slot b for
 // b >= 0, slot b+64 for -63 <= b < 0, nothing past the loaded slots.
@@ -127,11 +163,7 @@ __device__ __forceinline__ int voxel_value(const WorldPass& w, int ix, int iy, i
 
 // t / nsub for t >= 0 (nsub = R/32: a power of two for the usual ray counts, a shift then)
 __device__ __forceinline__ int div_nsub(int t, int nsub) {
-#if LUMRAD_OPT_NSUB
     return (nsub & (nsub - 1)) == 0 ? t >> (__ffs(nsub) - 1) : t / nsub;
-#else
-    return t / nsub;
-#endif
 }
 
 // ---------------------------------------------------------------- ray setup (:362-381)
@@ -150,11 +182,7 @@ __device__ __forceinline__ float3 hash33(uint32_t x, uint32_t y, uint32_t z) {
 
 __device__ __forceinline__ float3 normalize3(float3 v) {
     const float dd = fadd(fadd(fmul(v.x, v.x), fmul(v.y, v.y)), fmul(v.z, v.z));
-#if LUMRAD_OPT_RCP
-    const float s = __frcp_rn(__fsqrt_rn(dd));   // 1/x rounded once == the reciprocal rounded once
-#else
-    const float s = fdiv(1.0f, __fsqrt_rn(dd));
-#endif
+    const float s = __frcp_rn(__fsqrt_rn(dd));   // 1/x rounded once: the reciprocal rounded once
     return make_float3(fmul(v.x, s), fmul(v.y, s), fmul(v.z, s));
 }
 

@@ -28,15 +28,36 @@
 
 #include "radiance_device.cuh"
 
+#include <type_traits>
+
 namespace lumrad {
 namespace {
 
 // ---------------------------------------------------------------- march kernel
+// A ray is regular when each reciprocal of its direction is at most 2^100 in magnitude: no zero
+// component (only an exact cancellation in the set-up gives one, or one of a tiny magnitude).
+// Such a ray's march never meets a NaN or an infinity: its positions stay below 2^21 in
+// magnitude, its block corners within 32 of them, and its fraction grows by at least 0.5 - 2^-8
+// per step.  Hence, for it:
+//   (a) GLSL's min/max (y < x ? y : x) equal the hardware's min/max: they differ only on NaN and
+//       on the sign of a zero, and the skip's 0.01 floor maps both zeros alike;
+//   (b) a position lies outside [0, 16*size) exactly when its bits, read as unsigned, are at
+//       least those of 16*size (no position is -0: no origin is, and a sum is -0 only if both
+//       terms are);
+//   (c) the 2*max_dist+2 step bound is never reached: the fraction passes max_dist first.
+// A warp whose rays are all regular marches with those forms (fewer compares and selects on the
+// integer/compare pipe, the one that limits this kernel); any other warp with the exact forms of
+// the general case.  Both give the same bits for a regular ray.
+__device__ __forceinline__ bool regular_ray(float ivx, float ivy, float ivz) {
+    const float lim = 1.2676506002282294e30f;   // 2^100
+    return fabsf(ivx) <= lim && fabsf(ivy) <= lim && fabsf(ivz) <= lim;
+}
+
 template <bool RECORD>
 __global__ void __launch_bounds__(kWarps * 32, 4)
 march_kernel(const __grid_constant__ LaunchArgs la) {
     constexpr int kRingRays = 2 * kTaskRays;
-    __shared__ float4 s_ray[kWarps][3][kRingRays];    // set-up rays: origin, direction, 1/direction
+    __shared__ float4 s_ray[kWarps][3][kRingRays];    // set-up rays: origin, direction, (1/direction, regular)
     __shared__ float4 s_park[kWarps][3][kTaskRays];   // in-flight ray state while the warp sets up
 
     const int lane = threadIdx.x & 31;
@@ -68,6 +89,7 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
     int my = -1;                 // round-relative index of the lane's ray, -1 if idle
     float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, ivx = 0, ivy = 0, ivz = 0, cx = 0, cy = 0, cz = 0, frac = 0;
     int steps = 0;
+    bool reg = true;             // the lane's ray is regular (see regular_ray)
 
     // Tasks are claimed in guided chunks: remaining / (2 * warps), clamped to [1, 16].  (Claiming
     // the next chunk ahead of time hides the atomic's latency but holds work back from idle
@@ -97,24 +119,11 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         }
         return tb;
     };
-#if LUMRAD_OPT_MAGIC
-    // the far corner's offset in a block (16 or 0 per axis) plus the bits of 1.5 * 2^23: the
-    // float with bits m + v is 12582912 + v exactly for |v| < 2^22 (every block coordinate a ray
-    // reaches: |position| < 2^20), so a block corner is one integer add and one float subtract
-    // (no int -> float conversion)
-    int cxm = 0, cym = 0, czm = 0;
-    auto corner = [&]() {
-        cxm = 0x4B400000 + (dx > 0.0f ? 16 : 0);
-        cym = 0x4B400000 + (dy > 0.0f ? 16 : 0);
-        czm = 0x4B400000 + (dz > 0.0f ? 16 : 0);
-    };
-#else
     auto corner = [&]() {
         cx = dx > 0.0f ? 16.0f : 0.0f;
         cy = dy > 0.0f ? 16.0f : 0.0f;
         cz = dz > 0.0f ? 16.0f : 0.0f;
     };
-#endif
     // hand the next rays in ring order to the lanes in `need`
     auto assign = [&](unsigned need) {
         const int avail = loaded - issued;
@@ -127,6 +136,7 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             ox = o4.x; oy = o4.y; oz = o4.z;
             dx = d4.x; dy = d4.y; dz = d4.z;
             ivx = i4.x; ivy = i4.y; ivz = i4.z;
+            reg = i4.w != 0.0f;
             corner();
             frac = 0.0f;
             steps = 0;
@@ -135,13 +145,87 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
     };
     auto more_tasks = [&]() { return pending < 0 && !(exhausted && tb >= te); };
 
+    // The coarse march (CastRay_fast, radiance.comp:198-244) of the lanes' rays, two coarse steps
+    // per iteration (a lane whose ray ends in the first takes no second: the warp's vote and
+    // hand-out run once per two steps), until a ring half is free while tasks may remain, or no
+    // lane has a ray; a FAST loop also ends when a lane takes a ray that is not regular.
+    auto march = [&](auto fast_tag, auto wide_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        constexpr bool WIDE = decltype(wide_tag)::value;
+        const uint32_t uwx = __float_as_uint(wx), uwy = __float_as_uint(wy), uwz = __float_as_uint(wz);
+        while (true) {
+            bool fin = false;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                if (my >= 0) {
+                    frac = fadd(frac, 0.5f);
+                    steps++;
+                    const float px = fadd(ox, fmul(dx, frac));
+                    const float py = fadd(oy, fmul(dy, frac));
+                    const float pz = fadd(oz, fmul(dz, frac));
+                    const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
+                    int cid;
+                    const bool solid = solid_at_w<WIDE>(mv, ix, iy, iz, cid);
+                    if (cid == 0) {
+                        // empty block: skip to its far corner (radiance.comp:215-226).  The block's
+                        // low corner (ix/16)*16 with ix = trunc(px) is trunc(px/16)*16, formed in
+                        // FP32 (exact: px/16 and the product by 16 are exact, |px| < 2^21; a NaN
+                        // px gives a NaN skip either way)
+                        const float bx = fadd(fmul(truncf(fmul(px, 0.0625f)), 16.0f), cx);
+                        const float by = fadd(fmul(truncf(fmul(py, 0.0625f)), 16.0f), cy);
+                        const float bz = fadd(fmul(truncf(fmul(pz, 0.0625f)), 16.0f), cz);
+                        const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
+                        const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
+                        const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
+                        if (FAST) frac = fadd(frac, fmaxf(fminf(tx, fminf(ty, tz)), 0.01f));
+                        else frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
+                    }
+                    uint32_t info = 0;
+                    bool out;
+                    if (FAST)
+                        out = __float_as_uint(px) >= uwx || __float_as_uint(py) >= uwy || __float_as_uint(pz) >= uwz ||
+                              frac >= max_dist;
+                    else
+                        out = px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz ||
+                              frac >= max_dist;
+                    if (solid) {
+                        fin = true;
+                        info = (uint32_t)steps | (1u << 24);
+                    } else if (out) {
+                        fin = true;
+                        info = (uint32_t)steps;
+                    } else if (!FAST && steps >= max_steps) {
+                        fin = true;
+                        info = (uint32_t)steps | (1u << 25);
+                    }
+                    if (fin) {
+                        if (RECORD) {
+                            int blk;
+                            const int v = voxel_value(*wp, ix, iy, iz, blk);
+                            if (solid) info |= (uint32_t)v << 16;
+                            la.ray_blk[my] = blk;
+                        }
+                        __stcg(la.ray_res + my, make_uint2(__float_as_uint(frac), info));
+                        my = -1;
+                    }
+                }
+            }
+            const unsigned fm = __ballot_sync(kFull, fin);
+            if (fm) {
+                assign(fm);
+                if (!__any_sync(kFull, my >= 0) || (loaded - issued <= kTaskRays && more_tasks())) break;
+                if (FAST && !__all_sync(kFull, reg || my < 0)) break;
+            }
+        }
+    };
+
     while (true) {
         // 1. set up tasks into free ring halves (a half is free once its rays are handed out)
         const bool refill = loaded - issued <= kTaskRays && (pending >= 0 || more_tasks());
         if (refill && my >= 0) {   // park: the setup needs the registers
             s_park[wib][0][lane] = make_float4(ox, oy, oz, frac);
             s_park[wib][1][lane] = make_float4(dx, dy, dz, __int_as_float(steps));
-            s_park[wib][2][lane] = make_float4(ivx, ivy, ivz, 0.0f);
+            s_park[wib][2][lane] = make_float4(ivx, ivy, ivz, reg ? 1.0f : 0.0f);
         }
         bool loaded_now = false;
         while (refill && loaded - issued <= kTaskRays) {
@@ -182,7 +266,8 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             const float4 o4 = make_float4(o.x, o.y, o.z, 0.0f), d4 = make_float4(d.x, d.y, d.z, 0.0f);
             so[slot] = o4;
             sd[slot] = d4;
-            si[slot] = make_float4(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z), 0.0f);
+            const float rx = __frcp_rn(d.x), ry = __frcp_rn(d.y), rz = __frcp_rn(d.z);
+            si[slot] = make_float4(rx, ry, rz, regular_ray(rx, ry, rz) ? 1.0f : 0.0f);
             if (loaded & kTaskRays) base1 = base; else base0 = base;
             loaded += kTaskRays;
             loaded_now = true;
@@ -192,7 +277,7 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             const float4 a = s_park[wib][0][lane], b = s_park[wib][1][lane], c = s_park[wib][2][lane];
             ox = a.x; oy = a.y; oz = a.z; frac = a.w;
             dx = b.x; dy = b.y; dz = b.z; steps = __float_as_int(b.w);
-            ivx = c.x; ivy = c.y; ivz = c.z;
+            ivx = c.x; ivy = c.y; ivz = c.z; reg = c.w != 0.0f;
             corner();
         }
         // 2. idle lanes take rays
@@ -203,67 +288,14 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             if ((pending >= 0 || loaded_now) && lane == 0) atomicOr(la.error, 1);
             break;
         }
-        // 3. march; leave to set up more when a ring half is free and tasks may remain
-        while (true) {
-            // two coarse steps per iteration (a lane whose ray ends in the first takes no second):
-            // the warp's vote and hand-out below run once per two steps
-            bool fin = false;
-#pragma unroll
-            for (int u = 0; u < 2; u++) {
-                if (my >= 0) {
-                    frac = fadd(frac, 0.5f);
-                    steps++;
-                    const float px = fadd(ox, fmul(dx, frac));
-                    const float py = fadd(oy, fmul(dy, frac));
-                    const float pz = fadd(oz, fmul(dz, frac));
-                    const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
-                    int cid;
-                    const bool solid = solid_at(mv, ix, iy, iz, cid);
-                    if (cid == 0) {
-                        // empty block: skip to its far corner (radiance.comp:215-226)
-#if LUMRAD_OPT_MAGIC
-                        const float bx = fsub(__int_as_float((ix / 16) * 16 + cxm), 12582912.0f);
-                        const float by = fsub(__int_as_float((iy / 16) * 16 + cym), 12582912.0f);
-                        const float bz = fsub(__int_as_float((iz / 16) * 16 + czm), 12582912.0f);
-#else
-                        const float bx = fadd((float)((ix / 16) * 16), cx);
-                        const float by = fadd((float)((iy / 16) * 16), cy);
-                        const float bz = fadd((float)((iz / 16) * 16), cz);
-#endif
-                        const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
-                        const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
-                        const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
-                        frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
-                    }
-                    uint32_t info = 0;
-                    if (solid) {
-                        fin = true;
-                        info = (uint32_t)steps | (1u << 24);
-                    } else if (px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz ||
-                               frac >= max_dist) {
-                        fin = true;
-                        info = (uint32_t)steps;
-                    } else if (steps >= max_steps) {
-                        fin = true;
-                        info = (uint32_t)steps | (1u << 25);
-                    }
-                    if (fin) {
-                        if (RECORD) {
-                            int blk;
-                            const int v = voxel_value(*wp, ix, iy, iz, blk);
-                            if (solid) info |= (uint32_t)v << 16;
-                            la.ray_blk[my] = blk;
-                        }
-                        __stcg(la.ray_res + my, make_uint2(__float_as_uint(frac), info));
-                        my = -1;
-                    }
-                }
-            }
-            const unsigned fm = __ballot_sync(kFull, fin);
-            if (fm) {
-                assign(fm);
-                if (!__any_sync(kFull, my >= 0) || (loaded - issued <= kTaskRays && more_tasks())) break;
-            }
+        // 3. march
+        const bool fast = __all_sync(kFull, reg || my < 0);
+        if (mv.wide) {
+            if (fast) march(std::true_type{}, std::true_type{});
+            else march(std::false_type{}, std::true_type{});
+        } else {
+            if (fast) march(std::true_type{}, std::false_type{});
+            else march(std::false_type{}, std::false_type{});
         }
     }
 
@@ -439,6 +471,8 @@ cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_
     switch (precision) {
         case LUMRAD_PRECISION_FP16: return passes_t<StoreF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
         case LUMRAD_PRECISION_BF16: return passes_t<StoreBF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
+        case LUMRAD_PRECISION_RGB10A2:
+            return passes_t<StoreRGB10A2>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
         default: return passes_t<StoreF32>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
     }
 }
@@ -450,6 +484,9 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
             return record ? launch_t<StoreF16, true>(args, num_sms, stream) : launch_t<StoreF16, false>(args, num_sms, stream);
         case LUMRAD_PRECISION_BF16:
             return record ? launch_t<StoreBF16, true>(args, num_sms, stream) : launch_t<StoreBF16, false>(args, num_sms, stream);
+        case LUMRAD_PRECISION_RGB10A2:
+            return record ? launch_t<StoreRGB10A2, true>(args, num_sms, stream)
+                          : launch_t<StoreRGB10A2, false>(args, num_sms, stream);
         default:
             return record ? launch_t<StoreF32, true>(args, num_sms, stream) : launch_t<StoreF32, false>(args, num_sms, stream);
     }
@@ -479,6 +516,7 @@ cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, 
     if (n_worlds <= 0) return cudaSuccess;
     const dim3 grid(32, n_worlds);
     if (precision == LUMRAD_PRECISION_FP32) prep_kernel<uint4><<<grid, 256, 0, stream>>>(d_worlds);
+    else if (precision == LUMRAD_PRECISION_RGB10A2) prep_kernel<unsigned><<<grid, 256, 0, stream>>>(d_worlds);
     else prep_kernel<uint2><<<grid, 256, 0, stream>>>(d_worlds);
     return cudaGetLastError();
 }

@@ -31,7 +31,7 @@ class OWorld(C.Structure):
 
 class OParams(C.Structure):
     _fields_ = [("rays", C.c_int), ("max_dist", C.c_float), ("blend", C.c_float), ("time_seed", C.c_int),
-                ("size", C.c_int), ("shift", C.c_int)]
+                ("size", C.c_int), ("shift", C.c_int), ("unorm10", C.c_int)]
 
 
 class OStats(C.Structure):
@@ -95,9 +95,11 @@ def world_struct(world) -> _Keep:
 def radiance_pass(world, requests: np.ndarray, rays: int = 64, max_dist: float = 128.0, blend: float = 0.01,
                   time_seed: int = 0, size: int = 1, shift: int = 0, prev: np.ndarray | None = None,
                   precision: str = "f32", record_hits: bool = False, threads: int = 0,
-                  ray_light: np.ndarray | None = None):
+                  ray_light: np.ndarray | None = None, unorm10: bool = False):
     """One pass; returns (next radiance (Z,Y,X,3), hits or None, stats dict).
-    ray_light, if given, receives each ray's light ((groups*rays, 3), the pass's precision)."""
+    ray_light, if given, receives each ray's light ((groups*rays, 3), the pass's precision).
+    unorm10: the volume is stored as A2B10G10R10_UNORM (prev must hold such values already,
+    e.g. quantize_unorm10's)."""
     lib = load()
     k = world_struct(world)
     Z, Y, X = k.grid.shape
@@ -107,7 +109,7 @@ def radiance_pass(world, requests: np.ndarray, rays: int = 64, max_dist: float =
     prev = np.ascontiguousarray(prev, dtype=dt)
     nxt = np.empty_like(prev)
     req = np.ascontiguousarray(requests, dtype=np.int16)
-    p = OParams(rays, max_dist, blend, time_seed, size, shift)
+    p = OParams(rays, max_dist, blend, time_seed, size, shift, 1 if unorm10 else 0)
     groups = req.shape[0] // size
     hits = np.zeros(groups * rays, dtype=HIT_DTYPE) if record_hits else None
     st = OStats()
@@ -118,6 +120,14 @@ def radiance_pass(world, requests: np.ndarray, rays: int = 64, max_dist: float =
     if rc != 0:
         raise ValueError("oracle rejected the arguments")
     return nxt, hits, {"probes": st.probes, "rays": st.rays, "steps": st.steps, "hits": st.hits}
+
+
+def quantize_unorm10(rgb: np.ndarray) -> np.ndarray:
+    """Float RGB as an A2B10G10R10_UNORM image holds it: clamped to [0, 1] (NaN -> 0), code = round
+    to nearest even of v * 1023 in FP32, read back as code / 1023 in FP32."""
+    v = np.nan_to_num(np.asarray(rgb, dtype=np.float32), nan=0.0)
+    v = np.clip(v, np.float32(0), np.float32(1))
+    return (np.rint(v * np.float32(1023)) / np.float32(1023)).astype(np.float32)
 
 
 def hash33(x: int, y: int, z: int) -> np.ndarray:

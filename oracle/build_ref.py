@@ -163,14 +163,20 @@ def load(rays: int) -> C.CDLL:
         P = C.c_void_p
         lib.lumref_pass.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, P, P, P, P,
                                     C.c_int, C.c_int]
+        lib.lumref_set_unorm10.argtypes = [C.c_int]
+        lib.lumref_set_unorm10.restype = None
         _libs[rays] = lib
     return _libs[rays]
 
 
 def run_pass(world, requests_i8: np.ndarray, rays: int = 64, max_dist: float = 128.0, blend: float = 0.01,
-             time_seed: int = 0, size: int = 1, shift: int = 0, prev: np.ndarray | None = None):
-    """One dispatch of the reference shader.  Returns (next, ray_light, ray_info, abandoned)."""
+             time_seed: int = 0, size: int = 1, shift: int = 0, prev: np.ndarray | None = None,
+             unorm10: bool = False):
+    """One dispatch of the reference shader.  Returns (next, ray_light, ray_info, abandoned).
+    unorm10: the written volume takes the rgb10_a2 image's 10-bit codes (prev must hold such
+    values already)."""
     lib = load(rays)
+    lib.lumref_set_unorm10(1 if unorm10 else 0)
     grid = np.ascontiguousarray(world.grid, dtype=np.int16)
     pal = np.ascontiguousarray(world.palette, dtype=np.uint8)
     mats = np.ascontiguousarray(world.materials, dtype=np.float32)

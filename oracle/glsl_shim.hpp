@@ -14,7 +14,9 @@
 //   - texel fetches out of range return 0;
 //   - textureLod on the radiance volume: LINEAR + REPEAT, texel coordinate u*size-0.5, exact
 //     FP32 weights, lerp in x, then y, then z;
-//   - imageStore to the rgb10_a2 volume clamps to [0,1] (NaN -> 0), no 10-bit quantisation;
+//   - imageStore to the rgb10_a2 volume clamps to [0,1] (NaN -> 0); with the 10-bit storage
+//     switched on (lumref_set_unorm10) it also rounds each channel to the format's code,
+//     round-to-nearest-even of v*1023, and keeps code/1023 (the value a later fetch returns);
 //   - subgroupAdd sums the 32 lanes in xor-butterfly order (16, 8, 4, 2, 1).
 #pragma once
 
@@ -239,6 +241,7 @@ struct ShimState {
     long long fetch_limit = 0;
     ivec3 last_block;
     ivec3 last_palette;
+    bool unorm10 = false;      // imageStore rounds to the 10-bit UNORM codes
 };
 inline ShimState g_shim;
 
@@ -308,6 +311,8 @@ inline void imageStore(const image3D& im, ivec3 p, vec4 v) {
     if (p.x < 0 || p.y < 0 || p.z < 0 || p.x >= im.X || p.y >= im.Y || p.z >= im.Z) return;
     float* t = im.rgb + 3 * ((size_t)p.x + (size_t)im.X * ((size_t)p.y + (size_t)im.Y * (size_t)p.z));
     t[0] = unorm(v.x); t[1] = unorm(v.y); t[2] = unorm(v.z);
+    if (g_shim.unorm10)
+        for (int c = 0; c < 3; c++) t[c] = std::nearbyint(t[c] * 1023.0f) / 1023.0f;
 }
 
 // ---------------------------------------------------------------- compute built-ins

@@ -46,6 +46,7 @@ typedef struct {
     int time_seed;
     int size;                  // magicSize
     int shift;
+    int unorm10;               // 1: store as A2B10G10R10_UNORM (each channel rounded to code/1023)
 } OracleParams;
 
 typedef struct {               // same 24-byte layout as LumRadHit in include/lumrad.h
@@ -440,7 +441,11 @@ int run_pass(const OracleWorld* ow, const int16_t* req, int n_req, const OracleP
             old = old < (T)0 ? (T)0 : old;              // clamp(old, 0, 1) = min(max(x,0),1)
             old = (T)1 < old ? (T)1 : old;
             T nv = old * one_minus_a + accv[c] * a;     // mix(x,y,a) = x*(1-a) + y*a
-            next[pi + c] = clamp01(nv);
+            nv = clamp01(nv);
+            // imageStore into the rgb10_a2 image: code = round to nearest even of v*1023, read
+            // back as code/1023
+            if (p->unorm10) nv = std::nearbyint(nv * (T)1023) / (T)1023;
+            next[pi + c] = nv;
         }
     }
     if (stats) {

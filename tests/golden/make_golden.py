@@ -11,6 +11,10 @@ reference tree; the GPU machine only reads the committed .npz files).
   terrain_c1.npz   the 8x8x8 seeded terrain world, all probes, 64 rays, blend 0.1, one pass
   slicing_r256.npz a 12x10x6 terrain world, 256 rays, max_dist 256, size 2 / shift 1
   odd_ids.npz      negative, unloaded and special block ids and a non-empty slot 0, 32 rays
+  demo_scene_rgb10a2.npz  the demo scene's first three frames with the volume stored in the
+                   rgb10_a2 image's own 10-bit format (the reference's RADIANCE_FORMAT)
+  terrain_rgb10a2.npz     a 10x8x6 terrain world, 128 rays, blend 0.3, three chained passes in
+                   the 10-bit format
 
 Run:  python tests/golden/make_golden.py
 """
@@ -44,24 +48,27 @@ def demo_world():
     return worldgen.World(grid=grid, palette=pal, materials=mats)
 
 
-def run_reference(world, req, prev, passes, **p):
+def run_reference(world, req, prev, passes, unorm10=False, **p):
     outs = []
     cur = prev
     for i in range(passes):
         q = dict(p)
         q["time_seed"] = p.get("time_seed", 0) + i
-        cur, _, _, abandoned = build_ref.run_pass(world, req.astype(np.int8), prev=cur, **q)
+        cur, _, _, abandoned = build_ref.run_pass(world, req.astype(np.int8), prev=cur, unorm10=unorm10, **q)
         assert abandoned == 0
         outs.append(cur)
     return np.stack(outs)
 
 
-def save(name, world, req, prev, passes, **p):
-    out = run_reference(world, req, prev, passes, **p)
+def save(name, world, req, prev, passes, unorm10=False, **p):
+    if unorm10:
+        prev = oracle.quantize_unorm10(prev)   # the image holds 10-bit codes from the start
+    out = run_reference(world, req, prev, passes, unorm10=unorm10, **p)
+    extra = {"storage": np.array("rgb10a2")} if unorm10 else {}
     np.savez_compressed(os.path.join(HERE, name + ".npz"), grid=world.grid, palette=world.palette,
                         materials=world.materials, requests=req, prev=prev, expected=out,
                         params=np.array([p["rays"], p["max_dist"], p["blend"], p.get("time_seed", 0),
-                                         p.get("size", 1), p.get("shift", 0), passes], dtype=np.float64))
+                                         p.get("size", 1), p.get("shift", 0), passes], dtype=np.float64), **extra)
     print(f"{name}: {req.shape[0]} requests, {passes} pass(es), mean radiance {out[-1].mean():.5f}")
 
 
@@ -91,6 +98,16 @@ def main():
     w = worldgen.World(grid=g.reshape(w.grid.shape), palette=pal, materials=w.materials)
     prev = (worldgen.uniform(9, 99, w.n_blocks * 3).reshape(w.grid.shape + (3,)) * 0.5).astype(np.float32)
     save("odd_ids", w, worldgen.all_probes(w.dims), prev, 1, rays=32, max_dist=160.0, blend=0.2, time_seed=4)
+
+    # the reference's own volume format
+    w = demo_world()
+    req = oracle.update_list(w)
+    save("demo_scene_rgb10a2", w, req, np.zeros(w.grid.shape + (3,), np.float32), 3, unorm10=True,
+         rays=64, max_dist=128.0, blend=0.01, time_seed=0)
+    w = worldgen.terrain_world((10, 8, 6), seed=23, extra_blocks=20)
+    prev = (worldgen.uniform(10, 99, w.n_blocks * 3).reshape(w.grid.shape + (3,)) * 0.7).astype(np.float32)
+    save("terrain_rgb10a2", w, worldgen.all_probes(w.dims), prev, 3, unorm10=True, rays=128, max_dist=128.0,
+         blend=0.3, time_seed=2)
 
 
 if __name__ == "__main__":

@@ -1,5 +1,6 @@
-"""Radiance storage precision at full size: FP32, FP16 and BF16 storage (FP32 arithmetic) against
-the FP64 oracle (FP32 traversal, FP64 shading), per pass.
+"""Radiance storage precision at full size: FP32, FP16, BF16 and the reference's own 10-bit UNORM
+(A2B10G10R10) storage, all with FP32 arithmetic, against the FP64 oracle (FP32 traversal, FP64
+shading, no storage rounding), per pass.
 
 Workload: the 64x64x32-block terrain world (32 block types), every probe updated each pass,
 256 rays per probe, max_dist 256, blend 0.1, 16 successive passes from a zero volume.  Hit records
@@ -27,7 +28,7 @@ BLEND = 0.1
 FLOOR = 1e-3
 
 
-def measure(dims=DIMS, passes=PASSES, precisions=("fp32", "fp16", "bf16")):
+def measure(dims=DIMS, passes=PASSES, precisions=("fp32", "fp16", "bf16", "rgb10a2")):
     """Runs the workload; returns {"rows": {prec: [(max rel, RMS rel, max abs) per pass]},
     "hits_ok": {prec: bool}, "probes", "subset", "oracle_s", "threads"}."""
     import lum_gb300
@@ -77,14 +78,17 @@ def main(dims=DIMS, passes=PASSES) -> int:
     print(f"Hit records bit-exact vs the FP64 oracle on {m['subset']} probes: "
           + ", ".join(f"{k} {'yes' if v else 'NO'}" for k, v in hits_ok.items()))
     print()
-    print("| pass | FP32 max rel | FP32 RMS rel | FP16 max rel | FP16 RMS rel | BF16 max rel | BF16 RMS rel |")
-    print("|---:|---:|---:|---:|---:|---:|---:|")
+    precs = list(rows)
+    print("| pass | " + " | ".join(f"{k.upper()} max rel | {k.upper()} RMS rel" for k in precs) + " |")
+    print("|---:|" + "---:|---:|" * len(precs))
     for p in range(passes):
         cells = []
-        for prec in ("fp32", "fp16", "bf16"):
+        for prec in precs:
             mx, rms, _ = rows[prec][p]
             cells += [f"{mx:.2e}", f"{rms:.2e}"]
         print(f"| {p + 1} | " + " | ".join(cells) + " |")
+    print()
+    print("Max absolute error, worst pass: " + ", ".join(f"{k} {max(r[2] for r in rows[k]):.2e}" for k in precs))
     worst = {k: max(r[0] for r in v) for k, v in rows.items()}
     print()
     print("Worst over all passes (max rel): " + ", ".join(f"{k} {v:.2e}" for k, v in worst.items()))

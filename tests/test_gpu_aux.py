@@ -68,7 +68,7 @@ def test_update_radiance_uses_the_list():
         assert np.array_equal(a.build_update_list(), oracle.update_list(w))
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16", "rgb10a2"])
 def test_shift_matches_oracle(precision):
     import oracle
     w = _world((9, 8, 6), negative=False)
@@ -100,7 +100,7 @@ def test_stored_shift_applies_before_each_update():
         assert a.get_radiance().tobytes() == b.get_radiance().tobytes()
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16", "rgb10a2"])
 def test_gather_matches_oracle(precision):
     import oracle
     w = _world((7, 6, 5), negative=False)

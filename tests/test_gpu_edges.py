@@ -54,7 +54,7 @@ def test_uniform_worlds(fill):
     _check(w, req, random_prev(w), rays=64, max_dist=128.0, blend=0.1, time_seed=0)
 
 
-@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+@pytest.mark.parametrize("precision", ["fp16", "bf16", "rgb10a2"])
 def test_low_precision_batch_and_server(precision):
     """FP16/BF16 contexts in a batch and in a server: identical to the same passes run one
     context at a time (the storage type rounds identically on every path)."""

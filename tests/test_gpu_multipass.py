@@ -68,7 +68,7 @@ def test_passes_equal_single_passes_and_oracle(mode):
     assert rel_err(got, cur).max() <= RTOL
 
 
-@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+@pytest.mark.parametrize("precision", ["fp16", "bf16", "rgb10a2"])
 def test_passes_low_precision(precision):
     w = worldgen.terrain_world((9, 8, 5), seed=43, n_types=10)
     lists, spec = _passes(w)

@@ -109,3 +109,35 @@ def test_low_precision_storage_vs_fp64(precision):
     tol = 2e-3 if precision == "fp16" else 1.6e-2
     err = rel_err(got, ref, floor=1e-3)
     assert err.max() <= tol, (precision, err.max())
+
+
+@pytest.mark.parametrize("rays,odd", [(64, False), (96, True), (256, False)])
+def test_rgb10a2_storage_matches_oracle(rays, odd):
+    """The reference's own volume format (A2B10G10R10_UNORM): three chained passes, hit records and
+    volumes bit for bit against the oracle storing the same 10-bit codes; R = 96 combines a probe's
+    subgroups across finalize CTAs; odd block ids and a non-empty slot 0."""
+    import lum_gb300
+    import oracle
+    w = worldgen.terrain_world((9, 8, 6), seed=61, extra_blocks=20)
+    if odd:
+        g = w.grid.reshape(-1).copy()
+        idx = worldgen.randint(62, 1, 40, 0, g.size)
+        vals = np.array([-1, -5, -63, -64, 9, 40, 32767, 12], dtype=np.int16)
+        g[idx] = vals[np.arange(40) % vals.size]
+        pal = w.palette.copy()
+        pal[0, 3:5, :, 6:9] = 17
+        w = worldgen.World(grid=g.reshape(w.grid.shape), palette=pal, materials=w.materials)
+    req = worldgen.probe_subset(w.dims, 0.7, seed=63)
+    prev = random_prev(w, scale=0.9)
+    p = dict(rays=rays, max_dist=128.0, blend=0.3)
+    ref = oracle.quantize_unorm10(prev)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0], precision="rgb10a2") as rw:
+        rw.load(w)
+        rw.set_radiance(prev)
+        assert rw.get_radiance().tobytes() == ref.tobytes()   # the upload quantises like the oracle
+        for s in range(3):
+            rw.radiance_pass(req, lum_gb300.pass_params(time_seed=s, record_hits=True, **p))
+            ref, ref_hits, _ = oracle.radiance_pass(w, req, prev=ref, time_seed=s, record_hits=True, unorm10=True, **p)
+            assert_hits_equal(rw.get_hits(), ref_hits)
+            got = rw.get_radiance()
+            assert got.tobytes() == ref.tobytes(), (s, np.abs(got - ref).max())

@@ -25,16 +25,18 @@ def ref_libs():
     build_ref.build()
 
 
-def compare(world, req, rays=64, max_dist=128.0, blend=0.1, seed=0, size=1, shift=0, prev=None):
+def compare(world, req, rays=64, max_dist=128.0, blend=0.1, seed=0, size=1, shift=0, prev=None, unorm10=False):
     if prev is None:
         prev = random_prev(world)
     rn, rl, ri, abandoned = build_ref.run_pass(world, req.astype(np.int8), rays=rays, max_dist=max_dist,
-                                               blend=blend, time_seed=seed, size=size, shift=shift, prev=prev)
+                                               blend=blend, time_seed=seed, size=size, shift=shift, prev=prev,
+                                               unorm10=unorm10)
     assert abandoned == 0
     groups = req.shape[0] // size
     ol = np.zeros((groups * rays, 3), dtype=np.float32)
     on, oh, _ = oracle.radiance_pass(world, req, rays=rays, max_dist=max_dist, blend=blend, time_seed=seed,
-                                     size=size, shift=shift, prev=prev, record_hits=True, ray_light=ol)
+                                     size=size, shift=shift, prev=prev, record_hits=True, ray_light=ol,
+                                     unorm10=unorm10)
     assert on.tobytes() == rn.tobytes(), "radiance differs from the reference shader"
     bad = np.nonzero((ol.view(np.uint32) != rl.view(np.uint32)).any(axis=1))[0]
     assert bad.size == 0, f"{bad.size} rays' light differs, first {bad[:5]}"
@@ -100,3 +102,17 @@ def test_out_of_world_requests():
     req = worldgen.probe_subset(w.dims, 0.2, seed=1)
     req = np.concatenate([req, np.array([[-1, 2, 2, 0], [8, 0, 0, 0], [3, 3, 40, 0]], dtype=np.int16)])
     compare(w, req, rays=32, blend=0.5, seed=1)
+
+
+def test_rgb10a2_storage_chain():
+    """The volume stored in the rgb10_a2 image's own format: every written channel is a 10-bit
+    code (code/1023), and three chained passes read the rounded volume back through the
+    trilinear fetch; the oracle equals the reference shader bit for bit."""
+    w = worldgen.terrain_world((7, 6, 5), seed=19, extra_blocks=12)
+    req = worldgen.all_probes(w.dims)
+    cur = oracle.quantize_unorm10(random_prev(w))
+    for s in range(3):
+        cur = compare(w, req, rays=64, max_dist=128.0, blend=0.3, seed=s, prev=cur, unorm10=True)
+        codes = cur * np.float32(1023)
+        assert np.array_equal(codes, np.rint(codes)), "stored values are not 10-bit codes"
+    assert np.unique(cur).size > 50
