@@ -58,14 +58,14 @@ S_R = 12            # bytes of FP32 RGB radiance per probe
 BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches) in an ncu capture of this workload; ncu replays with cold caches
-# (march 1.08 + 46.01 MB, finalizes 118.24 + 0 MB)
-NCU_DRAM_BYTES_PER_STEP = 165.32e6
-# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 636.2 MB,
-# finalizes 987.9 MB)
-NCU_L2_BYTES_PER_STEP = 1624.0e6
+# (march 1.09 + 46.04 MB, finalizes 118.25 + 0.00 MB)
+NCU_DRAM_BYTES_PER_STEP = 165.38e6
+# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 634.9 MB,
+# finalizes 987.3 MB)
+NCU_L2_BYTES_PER_STEP = 1622.1e6
 # Warp instructions (smsp__inst_executed.sum) of the same 9 launches: the march over the 8 passes
-# and the 8 finalize launches (deterministic up to the march queue's task order)
-NCU_WARP_INST_PER_STEP = 572.0e6 + 8 * 51.5e6
+# (508.7 M) and the 8 finalize launches (409.7 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 508.7e6 + 409.7e6
 SCHEDULERS_PER_SM = 4
 
 
@@ -311,7 +311,7 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
       blockify     one frame of blockify + map of 8 rotated 32^3 models into the demo world
       frame        lumrad_update_radiance: one frame of the drop-in (device update list of the demo
                    world, then the pass over it) at the reference's 64 rays, max_dist 128
-      precision    the demo step (8 passes in one call) with FP32, FP16 and BF16 radiance storage,
+      precision    the demo step (8 passes in one call) with FP32, FP16, BF16 and RGB10A2 storage,
                    steps back to back (L2 not flushed)
     Device times are CUDA events on the context's stream around enqueued calls (shift, gather);
     calls that return a host result (lists, blockify) are timed wall-clock, synchronising."""
@@ -457,7 +457,7 @@ def aux_leg(local: int, reps: int, with_cpu: bool):
     plist = [lum_gb300.pass_params(rays=RAYS, max_dist=MAX_DIST, blend=BLEND, time_seed=p) for p in range(PASSES)]
     rays_step = sum(l.shape[0] for l in lists) * RAYS
     prec = {}
-    for name in ("fp32", "fp16", "bf16"):
+    for name in ("fp32", "fp16", "bf16", "rgb10a2"):
         with lum_gb300.RadianceWorld(world.dims, max_block_types=world.palette.shape[0], precision=name,
                                      device=local) as rp:
             rp.load(world)
