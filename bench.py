@@ -527,13 +527,28 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
     _serve_trace(plain, reqs[:200], np.zeros(200), params_of)
     psat = summary(*_serve_trace(plain, reqs, np.zeros(n_requests), params_of))
     plain.close()
+    # the same trace through the device-resident request loop (one CUDA graph polling a ring)
+    dev = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, device_loop=True)
+    for rw in rws:
+        dev.add_world(rw)
+    _serve_trace(dev, reqs[:200], np.zeros(200), params_of)
+    dsweep = []
+    for rate in rates:
+        arr = worldgen.poisson_arrivals(n_requests, rate, seed=SEED + int(rate))
+        dsweep.append(dict(summary(*_serve_trace(dev, reqs, arr, params_of)), rate_per_s=rate))
+    dsat = summary(*_serve_trace(dev, reqs, np.zeros(n_requests), params_of))
+    dst = dev.stats()
+    dev.close()
     for rw in rws:
         rw.close()
     out.update({"value": sat["probe_rays_per_s"], "unit": "probe-rays/s", "sweep": sweep, "saturated": sat,
                 "plain_saturated": psat, "speedup_vs_plain": sat["probe_rays_per_s"] / psat["probe_rays_per_s"],
                 "launches": st["launches"], "max_requests_in_launch": st["max_requests_in_launch"],
                 "resident_gb": st["resident_bytes"] / 1e9, "peak_inflight_mb": st["peak_inflight_bytes"] / 1e6,
-                "max_inflight": inflight})
+                "max_inflight": inflight,
+                "device_loop": {"sweep": dsweep, "saturated": dsat, "graph_launches": dst["launches"],
+                                "how": "one CUDA graph (WHILE node) per busy period: admit -> edits -> dirty "
+                                       "lists -> pass -> completions, polling a page-locked request ring"}})
     return out
 
 

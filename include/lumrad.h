@@ -313,7 +313,16 @@ int  lumrad_batch_stats(LumRadBatch batch, LumRadPassStats* out);
  * Under the HBM budget the server evicts idle worlds, least recently used first, when a world
  * or a request does not fit: an evicted world's device buffers are released and its grid,
  * palette, materials and volume kept on the host; it is uploaded again when a request for it
- * comes due.  Results do not depend on evictions. */
+ * comes due.  Results do not depend on evictions.
+ * With device_loop = 1 the request loop runs on the GPU instead: lumrad_server_progress only
+ * publishes due requests (in submission order) into a ring in page-locked memory and reads the
+ * completions the GPU writes back; one CUDA graph with a conditional WHILE node polls the ring
+ * (a bounded wait of poll_ms), takes the oldest requests of distinct worlds, applies their
+ * edits, derives the dirty probes, runs the pass over all of them and writes completions, and
+ * ends when no request came within poll_ms (the host starts it again when one is published).
+ * Results are the same as the host loop's.  Limits of that mode: every world stays resident
+ * (no eviction; each must fit the budget when added), a world has at most 192 block types
+ * (max_block_types), its probes times R/32 are at most 2^20, and R is 32, 64, 128 or 256. */
 typedef void* LumRadServer;
 
 typedef struct {
@@ -324,6 +333,9 @@ typedef struct {
                                      4 slots served 30% more than 2, 6 no more than 4) */
     int    max_requests_per_launch;   /* 0 = no limit */
     int    radius;                /* dirty-probe radius around each edit, in blocks (0..15) */
+    int    device_loop;           /* 1 = the request loop runs on the device (see below) */
+    float  poll_ms;               /* device loop: how long it waits for a request before it ends
+                                     (the host starts it again on the next request); 0 = 2 ms */
 } LumRadServerSettings;
 
 typedef struct { int16_t x, y, z, block; } LumRadEdit;

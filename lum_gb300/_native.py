@@ -56,7 +56,8 @@ class Tuning(C.Structure):
 
 class ServerSettings(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget_bytes", C.c_double),
-                ("max_inflight", C.c_int), ("max_requests_per_launch", C.c_int), ("radius", C.c_int)]
+                ("max_inflight", C.c_int), ("max_requests_per_launch", C.c_int), ("radius", C.c_int),
+                ("device_loop", C.c_int), ("poll_ms", C.c_float)]
 
 
 class ServerStats(C.Structure):

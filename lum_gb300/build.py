@@ -22,8 +22,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", INCLUDE,
           "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math"]
 DEVICE = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
 
-SOURCES = ["radiance_pass.cu", "radiance_aux.cu", "lumrad_host.cpp", "lumrad_batch.cpp", "lumrad_serve.cpp",
-           "lumrad_blockify.cpp"]
+SOURCES = ["radiance_pass.cu", "radiance_aux.cu", "radiance_serve.cu", "lumrad_host.cpp", "lumrad_batch.cpp",
+           "lumrad_serve.cpp", "lumrad_blockify.cpp"]
 
 
 def _nvcc() -> str:

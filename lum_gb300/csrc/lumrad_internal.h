@@ -86,6 +86,10 @@ struct LaunchArgs {
     // single-world launches sized for the longest possible list: the list's length on the device
     // (its tasks are (count / size) * R/32; the kernels leave the rest alone), or null
     const int* dev_count;
+    // table launches sized on the device (the device-resident serving loop): the tasks of all worlds
+    // and the number of worlds in the table, read by the kernels; null otherwise
+    const long long* dev_total;
+    const int* dev_n_worlds;
     // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
     // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
     int guided_div, max_chunk, march_ctas;
@@ -123,7 +127,9 @@ cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_
 
 // Start of a multi-world pass: copies every world's prev volume into its next volume and clears
 // its counters (descriptors already on the device).
-cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream);
+// dev_n (optional): the number of worlds in the table, read on the device (n_worlds: its capacity).
+cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream,
+                        const int* dev_n = nullptr);
 
 // Device scratch of the update-list builder for a world of W blocks: ceil(W/32) flag words,
 // ceil(W/256) CTA counts and offsets, and the count of rule-listed blocks.

@@ -20,6 +20,7 @@
 // and every result equals the result of the same requests run alone.
 
 #include "lumrad_world.h"
+#include "lumrad_devloop.h"
 
 #include <algorithm>
 #include <atomic>
@@ -164,6 +165,8 @@ struct Server {
     size_t resident = 0, fixed = 0, inflight = 0;
     LumRadServerStats st{};
     Tuning tuning;
+    // the device-resident request loop (settings.device_loop), or null
+    struct DevLoopHost* dl = nullptr;
     // per-launch host scratch
     std::vector<EditRecord> erec;
     std::vector<short4> lists;
@@ -479,7 +482,10 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     return LUMRAD_OK;
 }
 
+int devloop_progress(Server* sv);
+
 int progress(Server* sv) {
+    if (sv->dl) return devloop_progress(sv);
     int rc = retire(sv);
     if (rc) return rc;
     int free_slots = 0;
@@ -494,8 +500,352 @@ int progress(Server* sv) {
     return LUMRAD_OK;
 }
 
+// ---------------------------------------------------------------- device-resident loop
+// The host side of the loop of radiance_serve.cu: requests wait here in submission order until
+// due, then are copied into the page-locked ring (their edits into the edit arena) and the ring's
+// head is published; the GPU's completion records are read back from the other ring.  The host
+// makes no CUDA call per request: it starts the loop's graph again only when the loop has ended
+// (no request within poll_ms) and a published request waits.
+struct DevLoopHost {
+    struct Published {
+        long long id;
+        int world, rays;
+        double arrival, start;
+    };
+    long long ring_cap = 1 << 16, edit_cap = 1 << 22;
+    DevRequest* ring = nullptr;          // page-locked, mapped (host pointers; the device's below)
+    LumRadEdit* edits = nullptr;
+    DevCompletion* done = nullptr;
+    long long* ctl = nullptr;            // [0] head, [1] tail (completed), [2] done head, [3] stop
+    DevRequest* d_ring = nullptr;
+    LumRadEdit* d_edits = nullptr;
+    DevCompletion* d_done = nullptr;
+    long long* d_ctl = nullptr;
+    long long head = 0, done_read = 0, edit_head = 0, edit_tail = 0;
+    std::deque<long long> edit_ends;     // arena position after each published request's edits
+    std::deque<SRequest> queue;          // submitted, not yet published
+    std::deque<Published> published;     // published, not yet completed (ring order)
+    std::vector<int> outstanding;        // per world: published, not completed
+    DevLoop* d_loop = nullptr;
+    DevWorld* d_worlds = nullptr;
+    std::vector<void*> bufs;             // per-world device buffers of the loop
+    int* d_chunk_count = nullptr;
+    int* d_chunk_off = nullptr;
+    long long chunk_cap = 0, chunks_total = 0;
+    int* d_error = nullptr;
+    unsigned long long* d_queue = nullptr;
+    uint2* d_ray_res = nullptr;
+    long long max_tasks = 1 << 20;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_end = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool running = false;
+    double offset_s = 0.0;               // host clock = %globaltimer * 1e-9 - offset_s
+    unsigned long long* h_timer = nullptr;
+};
+
+template <class T>
+int host_mapped(T** h, T** d, size_t n) {
+    LUMRAD_TRY(cudaHostAlloc(reinterpret_cast<void**>(h), n * sizeof(T), cudaHostAllocMapped));
+    std::memset(static_cast<void*>(*h), 0, n * sizeof(T));
+    LUMRAD_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(d), *h, 0));
+    return LUMRAD_OK;
+}
+
+volatile long long& ctl_word(DevLoopHost& dl, int k) { return reinterpret_cast<volatile long long*>(dl.ctl)[k]; }
+
+int devloop_create(Server* sv) {
+    DevLoopHost* dl = new DevLoopHost();
+    sv->dl = dl;
+    int rc;
+    if ((rc = host_mapped(&dl->ring, &dl->d_ring, (size_t)dl->ring_cap))) return rc;
+    if ((rc = host_mapped(&dl->edits, &dl->d_edits, (size_t)dl->edit_cap))) return rc;
+    if ((rc = host_mapped(&dl->done, &dl->d_done, (size_t)dl->ring_cap))) return rc;
+    if ((rc = host_mapped(&dl->ctl, &dl->d_ctl, 8))) return rc;
+    unsigned long long* d_timer = nullptr;
+    if ((rc = host_mapped(&dl->h_timer, &d_timer, 1))) return rc;
+    LUMRAD_TRY(cudaStreamCreateWithFlags(&dl->stream, cudaStreamNonBlocking));
+    LUMRAD_TRY(cudaEventCreateWithFlags(&dl->ev_end, cudaEventDisableTiming));
+    LUMRAD_TRY(cudaMalloc(&dl->d_loop, sizeof(DevLoop)));
+    LUMRAD_TRY(cudaMalloc(&dl->d_worlds, kDevMaxWorlds * sizeof(DevWorld)));
+    LUMRAD_TRY(cudaMalloc(&dl->d_error, sizeof(int)));
+    LUMRAD_TRY(cudaMalloc(&dl->d_queue, kQueueWords * sizeof(unsigned long long)));
+    LUMRAD_TRY(cudaMalloc(&dl->d_ray_res, (size_t)dl->max_tasks * kTaskRays * sizeof(uint2)));
+    LUMRAD_TRY(cudaMemsetAsync(dl->d_error, 0, sizeof(int), dl->stream));
+    LUMRAD_TRY(cudaMemsetAsync(dl->d_queue, 0, kQueueWords * sizeof(unsigned long long), dl->stream));
+    std::unique_ptr<DevLoop> h(new DevLoop());
+    std::memset(static_cast<void*>(h.get()), 0, sizeof(DevLoop));
+    h->ring = dl->d_ring;
+    h->ring_cap = dl->ring_cap;
+    h->head = dl->d_ctl;
+    h->tail_host = dl->d_ctl + 1;
+    h->edits = dl->d_edits;
+    h->edit_cap = dl->edit_cap;
+    h->done = dl->d_done;
+    h->done_head = dl->d_ctl + 2;
+    h->stop = reinterpret_cast<const int*>(dl->d_ctl + 3);
+    h->worlds = dl->d_worlds;
+    h->poll_ns = (unsigned long long)((sv->s.poll_ms > 0.0f ? sv->s.poll_ms : 2.0f) * 1e6);
+    h->max_tasks = dl->max_tasks;
+    h->radius = sv->s.radius;
+    h->error = dl->d_error;
+    h->queue = dl->d_queue;
+    h->iteration = 1;
+    LUMRAD_TRY(cudaMemcpyAsync(dl->d_loop, h.get(), sizeof(DevLoop), cudaMemcpyHostToDevice, dl->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(dl->stream));
+
+    // the graph: one WHILE node whose body is one iteration of the loop
+    LUMRAD_TRY(cudaGraphCreate(&dl->graph, 0));
+    cudaGraphConditionalHandle cond;
+    LUMRAD_TRY(cudaGraphConditionalHandleCreate(&cond, dl->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    LUMRAD_TRY(cudaGraphAddNode(&node, dl->graph, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    DevLoopLaunch a;
+    std::memset(static_cast<void*>(&a), 0, sizeof a);
+    char* base = reinterpret_cast<char*>(dl->d_loop);
+    a.table = reinterpret_cast<const WorldPass*>(base + offsetof(DevLoop, table));
+    a.n_table = reinterpret_cast<const int*>(base + offsetof(DevLoop, n_table));
+    a.precision = sv->s.precision;
+    a.num_sms = sv->num_sms;
+    LaunchArgs& la = a.pass;
+    la.worlds = a.table;
+    la.n_worlds = kDevBatch;
+    la.dev_n_worlds = a.n_table;
+    la.dev_total = reinterpret_cast<const long long*>(base + offsetof(DevLoop, total_tasks));
+    la.n_tasks = dl->max_tasks;
+    la.queue = dl->d_queue;
+    la.error = dl->d_error;
+    la.ray_res = dl->d_ray_res;
+    la.in_cta = 1;
+    LUMRAD_TRY(cudaStreamBeginCaptureToGraph(dl->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t ce = capture_devloop_body(dl->d_loop, a, cond, dl->stream);
+    const cudaError_t ee = cudaStreamEndCapture(dl->stream, &body);
+    LUMRAD_TRY(ce);
+    LUMRAD_TRY(ee);
+    LUMRAD_TRY(cudaGraphInstantiate(&dl->exec, dl->graph, 0));
+
+    // the device clock against the host's: the read with the shortest round trip
+    double best = 1e9;
+    for (int i = 0; i < 20; i++) {
+        const double t0 = clock_s();
+        LUMRAD_TRY(launch_read_globaltimer(d_timer, dl->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(dl->stream));
+        const double t1 = clock_s();
+        if (t1 - t0 < best) {
+            best = t1 - t0;
+            dl->offset_s = (double)*reinterpret_cast<volatile unsigned long long*>(dl->h_timer) * 1e-9 - 0.5 * (t0 + t1);
+        }
+    }
+    sv->fixed += (size_t)dl->max_tasks * kTaskRays * sizeof(uint2) + sizeof(DevLoop) + kDevMaxWorlds * sizeof(DevWorld);
+    return LUMRAD_OK;
+}
+
+// Ends the loop (it stops at its next admit) and waits for it; the flag is cleared again.
+int devloop_halt(DevLoopHost* dl) {
+    if (!dl->running) return LUMRAD_OK;
+    ctl_word(*dl, 3) = 1;
+    const cudaError_t e = cudaStreamSynchronize(dl->stream);
+    ctl_word(*dl, 3) = 0;
+    dl->running = false;
+    LUMRAD_TRY(e);
+    return LUMRAD_OK;
+}
+
+int devloop_add_world(Server* sv, Context* c, int id, size_t* bytes) {
+    DevLoopHost& dl = *sv->dl;
+    DeviceWorld& dw = c->world;
+    if (id >= kDevMaxWorlds) return fail(LUMRAD_EINVAL, "the device loop holds at most 1024 worlds");
+    if (dw.n_slots > 192) return fail(LUMRAD_EINVAL, "the device loop needs max_block_types <= 192");
+    if ((long long)dw.W > dl.max_tasks) return fail(LUMRAD_EINVAL, "world too large for the device loop (2^20 blocks)");
+    if (dw.cgrid_wide) return fail(LUMRAD_EINVAL, "the device loop needs at most 256 distinct block ids");
+    int rc = devloop_halt(&dl);
+    if (rc) return rc;
+    // every id with a palette slot, and the shared empty id, gets its compact id now: the loop's
+    // edits then only look ids up
+    bool assigned = false;
+    for (int b = -63; b < dw.n_slots; b++)
+        if (b != 0 && dw.compact_of((int16_t)b, &assigned) < 0) return fail(LUMRAD_EINVAL, "too many block ids");
+    if (dw.compact_of((int16_t)-64, &assigned) < 0) return fail(LUMRAD_EINVAL, "too many block ids");
+    LUMRAD_TRY(cudaMemcpyAsync(dw.d_cbits, dw.h_cbits.data(), dw.h_cbits.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(dw.d_cslot, dw.h_cslot.data(), dw.h_cslot.size() * sizeof(int), cudaMemcpyHostToDevice,
+                               c->stream));
+    std::vector<int16_t> cmap((size_t)dw.n_slots + 64);
+    for (int b = -64; b < dw.n_slots; b++) cmap[(size_t)(b + 64)] = (int16_t)dw.id_to_c[(uint16_t)(int16_t)b];
+    int16_t* d_cmap = nullptr;
+    uint8_t* d_mask = nullptr;
+    unsigned long long* d_stamp = nullptr;
+    short4* d_list = nullptr;
+    LUMRAD_TRY(cudaMalloc(&d_cmap, cmap.size() * sizeof(int16_t)));
+    dl.bufs.push_back(d_cmap);
+    LUMRAD_TRY(cudaMalloc(&d_mask, dw.W));
+    dl.bufs.push_back(d_mask);
+    LUMRAD_TRY(cudaMalloc(&d_stamp, dw.W * sizeof(unsigned long long)));
+    dl.bufs.push_back(d_stamp);
+    LUMRAD_TRY(cudaMalloc(&d_list, dw.W * sizeof(short4)));
+    dl.bufs.push_back(d_list);
+    LUMRAD_TRY(cudaMemcpyAsync(d_cmap, cmap.data(), cmap.size() * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_mask, 0, dw.W, c->stream));
+    LUMRAD_TRY(cudaMemsetAsync(d_stamp, 0, dw.W * sizeof(unsigned long long), c->stream));
+    DevWorld w;
+    std::memset(static_cast<void*>(&w), 0, sizeof w);
+    LumRadPassParams p{64, 128.0f, 0.1f, 0, 1, 0, 0};
+    if ((rc = dw.fill_pass(nullptr, 0, p, c->stream, &w.pass))) return rc;
+    const int rs[4] = {32, 64, 128, 256};
+    for (int k = 0; k < 4; k++) {
+        const float4* d = nullptr;
+        if ((rc = dw.ensure_dirs(rs[k], c->stream, &d))) return rc;
+        w.dirs[k] = d;
+    }
+    w.cmap = d_cmap;
+    w.n_cmap = (int)cmap.size();
+    w.empty_c = dw.id_to_c[(uint16_t)(int16_t)-64];
+    w.mask = d_mask;
+    w.stamp = d_stamp;
+    w.list = d_list;
+    w.rad[0] = dw.d_rad[0];
+    w.rad[1] = dw.d_rad[1];
+    w.cur = dw.cur;
+    LUMRAD_TRY(cudaMemcpyAsync(dl.d_worlds + id, &w, sizeof w, cudaMemcpyHostToDevice, c->stream));
+    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    // chunk arrays for every world's chunks (a batch holds each world at most once)
+    dl.chunks_total += ((long long)dw.W + kDevChunk - 1) / kDevChunk;
+    if (dl.chunks_total > dl.chunk_cap) {
+        const long long cap = std::max(dl.chunks_total, 2 * dl.chunk_cap);
+        cudaFree(dl.d_chunk_count);
+        cudaFree(dl.d_chunk_off);
+        dl.d_chunk_count = dl.d_chunk_off = nullptr;
+        LUMRAD_TRY(cudaMalloc(&dl.d_chunk_count, cap * sizeof(int)));
+        LUMRAD_TRY(cudaMalloc(&dl.d_chunk_off, cap * sizeof(int)));
+        dl.chunk_cap = cap;
+        int* ptrs[2] = {dl.d_chunk_count, dl.d_chunk_off};
+        LUMRAD_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(dl.d_loop) + offsetof(DevLoop, chunk_count), ptrs,
+                                   sizeof ptrs, cudaMemcpyHostToDevice, dl.stream));
+        LUMRAD_TRY(cudaStreamSynchronize(dl.stream));
+    }
+    dl.outstanding.resize((size_t)id + 1, 0);
+    *bytes = dw.W * (1 + sizeof(unsigned long long) + sizeof(short4)) + cmap.size() * sizeof(int16_t);
+    return LUMRAD_OK;
+}
+
+int devloop_progress(Server* sv) {
+    DevLoopHost& dl = *sv->dl;
+    // completions the GPU wrote
+    const long long dh = ctl_word(dl, 2);
+    std::atomic_thread_fence(std::memory_order_acquire);
+    for (; dl.done_read < dh; dl.done_read++) {
+        const DevCompletion& c = dl.done[dl.done_read % dl.ring_cap];
+        const DevLoopHost::Published pr = dl.published.front();
+        dl.published.pop_front();
+        LumRadCompletion o{};
+        o.request = pr.id;
+        o.world = pr.world;
+        o.status = c.id == pr.id ? c.status : LUMRAD_EDEVICE;
+        o.probes = c.probes;
+        o.rays_per_probe = pr.rays;
+        o.arrival_s = pr.arrival;
+        o.start_s = pr.start;
+        o.done_s = (double)c.t_done_ns * 1e-9 - dl.offset_s - sv->t0;
+        sv->done.push_back(o);
+        sv->pending--;
+        dl.outstanding[pr.world]--;
+        sv->st.requests++;
+        sv->st.probes += (unsigned long long)c.probes;
+        sv->st.rays += (unsigned long long)c.probes * (unsigned long long)pr.rays;
+        dl.edit_tail = dl.edit_ends.front();
+        dl.edit_ends.pop_front();
+    }
+    // due requests into the ring, in submission order
+    const double now = sv->now();
+    bool published = false;
+    while (!dl.queue.empty()) {
+        SRequest& r = dl.queue.front();
+        if (r.arrival > now) break;
+        const long long ne = (long long)r.edits.size();
+        if (dl.head - dl.done_read >= dl.ring_cap || ne > dl.edit_cap - (dl.edit_head - dl.edit_tail)) break;
+        for (long long k = 0; k < ne; k++) dl.edits[(dl.edit_head + k) % dl.edit_cap] = r.edits[(size_t)k];
+        DevRequest& q = dl.ring[dl.head % dl.ring_cap];
+        q.id = r.id;
+        q.edit_off = dl.edit_head % dl.edit_cap;
+        q.world = r.world;
+        q.n_edits = (int)ne;
+        q.rays = r.p.rays_per_probe;
+        q.time_seed = r.p.time_seed;
+        q.max_dist = r.p.max_dist;
+        q.blend = r.p.blend;
+        dl.edit_head += ne;
+        dl.edit_ends.push_back(dl.edit_head);
+        dl.published.push_back(DevLoopHost::Published{r.id, r.world, r.p.rays_per_probe, r.arrival, now});
+        dl.outstanding[r.world]++;
+        dl.head++;
+        dl.queue.pop_front();
+        published = true;
+    }
+    if (published) {
+        std::atomic_thread_fence(std::memory_order_release);   // the entries before the head
+        ctl_word(dl, 0) = dl.head;
+    }
+    // the loop ended (no request within poll_ms): start it again if a published request waits
+    if (dl.running) {
+        const cudaError_t q = cudaEventQuery(dl.ev_end);
+        if (q == cudaSuccess) dl.running = false;
+        else if (q != cudaErrorNotReady) LUMRAD_TRY(q);
+    }
+    if (!dl.running && dl.head > dl.done_read) {
+        LUMRAD_TRY(cudaGraphLaunch(dl.exec, dl.stream));
+        LUMRAD_TRY(cudaEventRecord(dl.ev_end, dl.stream));
+        dl.running = true;
+        sv->st.launches++;
+    }
+    return LUMRAD_OK;
+}
+
+void devloop_destroy(Server* sv) {
+    DevLoopHost* dl = sv->dl;
+    if (!dl) return;
+    if (dl->ctl) {
+        ctl_word(*dl, 3) = 1;
+        if (dl->stream) cudaStreamSynchronize(dl->stream);
+    }
+    // the worlds go back to their contexts as the loop left them: volume side and grid
+    for (size_t w = 0; w < sv->worlds.size() && dl->d_worlds && w < dl->outstanding.size(); w++) {
+        DeviceWorld& dw = sv->worlds[w].ctx->world;
+        int cur = dw.cur;
+        if (cudaMemcpy(&cur, &dl->d_worlds[w].cur, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess) dw.cur = cur;
+        if (cudaMemcpy(dw.h_grid.data(), dw.d_grid, dw.W * sizeof(int16_t), cudaMemcpyDeviceToHost) == cudaSuccess)
+            dw.grid_dirty = true;
+    }
+    if (dl->exec) cudaGraphExecDestroy(dl->exec);
+    if (dl->graph) cudaGraphDestroy(dl->graph);
+    for (void* p : dl->bufs) cudaFree(p);
+    cudaFree(dl->d_chunk_count);
+    cudaFree(dl->d_chunk_off);
+    cudaFree(dl->d_ray_res);
+    cudaFree(dl->d_queue);
+    cudaFree(dl->d_error);
+    cudaFree(dl->d_worlds);
+    cudaFree(dl->d_loop);
+    if (dl->ring) cudaFreeHost(dl->ring);
+    if (dl->edits) cudaFreeHost(dl->edits);
+    if (dl->done) cudaFreeHost(dl->done);
+    if (dl->ctl) cudaFreeHost(dl->ctl);
+    if (dl->h_timer) cudaFreeHost(dl->h_timer);
+    if (dl->ev_end) cudaEventDestroy(dl->ev_end);
+    if (dl->stream) cudaStreamDestroy(dl->stream);
+    delete dl;
+    sv->dl = nullptr;
+}
+
 void destroy_server(Server* sv) {
     cudaSetDevice(sv->s.device);
+    devloop_destroy(sv);
     for (auto& slp : sv->slots) {
         Slot& sl = *slp;
         if (sl.stream) cudaStreamSynchronize(sl.stream);
@@ -550,6 +900,8 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
     if (s->max_inflight < 0 || s->max_inflight > 8) return fail(LUMRAD_EINVAL, "max_inflight must be in [0, 8]");
     if (s->radius < 0 || s->radius > 15) return fail(LUMRAD_EINVAL, "radius must be in [0, 15]");
     if (s->hbm_budget_bytes < 0 || s->max_requests_per_launch < 0) return fail(LUMRAD_EINVAL, "negative limit");
+    if (s->device_loop != 0 && s->device_loop != 1) return fail(LUMRAD_EINVAL, "device_loop must be 0 or 1");
+    if (!(s->poll_ms >= 0.0f && s->poll_ms <= 1000.0f)) return fail(LUMRAD_EINVAL, "poll_ms must be in [0, 1000]");
     Server* sv = new Server();
     sv->s = *s;
     if (sv->s.max_inflight == 0) sv->s.max_inflight = 4;
@@ -557,6 +909,12 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
     auto attempt = [&]() -> int {
         LUMRAD_TRY(cudaSetDevice(s->device));
         LUMRAD_TRY(cudaDeviceGetAttribute(&sv->num_sms, cudaDevAttrMultiProcessorCount, s->device));
+        if (s->device_loop) {
+            int rc = devloop_create(sv);
+            if (rc) return rc;
+            if (sv->fixed > sv->budget()) return fail(LUMRAD_ENOMEM, "the loop's buffers alone exceed the HBM budget");
+            return LUMRAD_OK;
+        }
         const size_t rays = (size_t)kChunkTasks * kTaskRays;
         for (int k = 0; k < sv->s.max_inflight; k++) {
             sv->slots.emplace_back(new Slot());
@@ -612,11 +970,19 @@ int lumrad_server_add_world(LumRadServer server, LumRadContext world, int* id) {
     int rc = dw.sync_inputs(c->stream);
     if (rc) return rc;
     if ((rc = prepare_world(dw, c->stream))) return rc;
-    const size_t bytes = dw.footprint();
-    if (sv->fixed + bytes > sv->budget()) return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget");
-    bool fits = true;
-    if ((rc = make_room(sv, bytes, std::vector<char>(sv->worlds.size(), 0), &fits))) return rc;
-    if (!fits) return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget beside the busy worlds");
+    size_t bytes = dw.footprint();
+    if (sv->dl) {   // the device loop keeps every world resident
+        size_t extra = 0;
+        if (sv->resident + sv->fixed + bytes > sv->budget())
+            return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget (the device loop does not evict)");
+        if ((rc = devloop_add_world(sv, c, (int)sv->worlds.size(), &extra))) return rc;
+        bytes += extra;
+    } else {
+        if (sv->fixed + bytes > sv->budget()) return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget");
+        bool fits = true;
+        if ((rc = make_room(sv, bytes, std::vector<char>(sv->worlds.size(), 0), &fits))) return rc;
+        if (!fits) return fail(LUMRAD_ENOMEM, "the world does not fit the HBM budget beside the busy worlds");
+    }
     SWorld w;
     w.ctx = c;
     w.bytes = bytes;
@@ -642,13 +1008,22 @@ int lumrad_server_submit(LumRadServer server, int world, const LumRadEdit* edits
         if (edits[k].x < 0 || edits[k].y < 0 || edits[k].z < 0 || edits[k].x >= dw.X || edits[k].y >= dw.Y ||
             edits[k].z >= dw.Z)
             return fail(LUMRAD_EINVAL, "edit outside the world");
+    if (sv->dl) {
+        const int R = params->rays_per_probe;
+        if (R != 32 && R != 64 && R != 128 && R != 256)
+            return fail(LUMRAD_EINVAL, "the device loop runs 32, 64, 128 or 256 rays per probe");
+        if ((long long)dw.W * (R / 32) > sv->dl->max_tasks)
+            return fail(LUMRAD_EINVAL, "the world's probes x R/32 exceed the device loop's 2^20 tasks");
+        if (n_edits > sv->dl->edit_cap) return fail(LUMRAD_EINVAL, "too many edits for the device loop's arena");
+    }
     SRequest r;
     r.id = sv->next_id++;
     r.world = world;
     r.arrival = arrival_s < 0.0 ? sv->now() : arrival_s;
     r.p = *params;
     r.edits.assign(edits, edits + n_edits);
-    sv->worlds[world].fifo.push_back(std::move(r));
+    if (sv->dl) sv->dl->queue.push_back(std::move(r));
+    else sv->worlds[world].fifo.push_back(std::move(r));
     sv->pending++;
     *request = sv->next_id - 1;
     return LUMRAD_OK;
@@ -679,6 +1054,17 @@ int lumrad_server_cancel(LumRadServer server, long long request, int* cancelled)
     Server* sv = as_server(server);
     if (!sv || !cancelled) return fail(LUMRAD_EINVAL, "null argument");
     *cancelled = 0;
+    if (sv->dl) {   // only requests not yet published into the ring
+        auto& q = sv->dl->queue;
+        for (auto it = q.begin(); it != q.end(); ++it)
+            if (it->id == request) {
+                complete_now(sv, *it, LUMRAD_ECANCELED);
+                q.erase(it);
+                *cancelled = 1;
+                return LUMRAD_OK;
+            }
+        return LUMRAD_OK;
+    }
     for (auto& sw : sv->worlds)
         for (auto it = sw.fifo.begin(); it != sw.fifo.end(); ++it)
             if (it->id == request) {
@@ -713,6 +1099,21 @@ int lumrad_server_get_radiance(LumRadServer server, int world, float* rgb) {
     if (world < 0 || world >= (int)sv->worlds.size()) return fail(LUMRAD_EINVAL, "unknown world");
     LUMRAD_TRY(cudaSetDevice(sv->s.device));
     SWorld& w = sv->worlds[world];
+    if (sv->dl) {   // after the world's published requests; its volume side is the loop's
+        DevLoopHost& dl = *sv->dl;
+        const double deadline = clock_s() + 60.0;
+        while (dl.outstanding[world] > 0) {
+            int rc = progress(sv);
+            if (rc) return rc;
+            if (clock_s() > deadline) return fail(LUMRAD_ETIMEOUT, "the world's requests did not complete");
+            std::this_thread::yield();
+        }
+        int cur = 0;
+        LUMRAD_TRY(cudaMemcpyAsync(&cur, &dl.d_worlds[world].cur, sizeof(int), cudaMemcpyDeviceToHost, w.ctx->stream));
+        LUMRAD_TRY(cudaStreamSynchronize(w.ctx->stream));
+        w.ctx->world.cur = cur;
+        return lumrad_get_radiance(w.ctx, rgb);
+    }
     if (w.busy) {
         LUMRAD_TRY(cudaEventSynchronize(sv->slots[w.last_slot]->ev_done));
         int rc = retire(sv);

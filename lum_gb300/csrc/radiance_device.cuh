@@ -403,8 +403,9 @@ __device__ __forceinline__ void subgroup_done(const WorldPass& w, int g, int k, 
 }
 
 __device__ __forceinline__ int world_of(const LaunchArgs& la, int t) {
-    if (la.n_worlds == 1) return 0;
-    int lo = 0, hi = la.n_worlds - 1;
+    const int n = la.dev_n_worlds ? *la.dev_n_worlds : la.n_worlds;
+    if (n <= 1) return 0;
+    int lo = 0, hi = n - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (la.worlds[mid].task_begin <= t) lo = mid; else hi = mid - 1;

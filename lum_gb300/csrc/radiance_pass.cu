@@ -27,6 +27,7 @@
 // up to 134 MB for several passes, 268 MB for a batch's round of 2^20.
 
 #include "radiance_device.cuh"
+#include "lumrad_devloop.h"
 
 #include <type_traits>
 
@@ -71,6 +72,8 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         const long long real = (long long)(__ldcg(la.dev_count) / la.single.size) * (la.single.R >> 5);
         n_round = (int)max(0LL, min((long long)n_round, real - la.chunk_begin));
     }
+    if (la.dev_total)     // a table built on the device: its task count bounds the round
+        n_round = (int)max(0LL, min((long long)n_round, __ldcg(la.dev_total) - la.chunk_begin));
 
     // current world (warp-uniform)
     const WorldPass* wp = &la.single;
@@ -156,7 +159,7 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         while (true) {
             bool fin = false;
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
+            for (int u = 0; u < 2; u++) {   // (3 or 4 steps per iteration measured 0.7% slower)
                 if (my >= 0) {
                     frac = fadd(frac, 0.5f);
                     steps++;
@@ -314,12 +317,10 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
 // then has no global-memory combine, which costs the general kernel 8 registers and spills, and
 // runs 6 CTAs per SM (40 registers): the kernel is latency-bound; against four CTAs, five measured
 // 4-6% faster and six 1% faster again (seven: slower on single passes).
+// One 8-task group (one CTA's work) of the finalize kernel.
 template <class Store, bool RECORD, bool IN_CTA>
-__global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? 6 : 4)
-finalize_kernel(const __grid_constant__ LaunchArgs la) {
-    __shared__ float4 s_mean[kFinWarps];
-    __shared__ int s_count[kFinWarps];
-    __shared__ unsigned s_stat[kFinWarps][2];
+__device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, float4* s_mean, int* s_count,
+                                               unsigned (*s_stat)[2]) {
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     if (threadIdx.x < kFinWarps) {
@@ -328,7 +329,7 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
         s_stat[threadIdx.x][1] = 0;
     }
     __syncthreads();
-    const int t0 = la.chunk_begin + (int)blockIdx.x * kFinWarps;   // worlds start at multiples of 8
+    const int t0 = la.chunk_begin + group * kFinWarps;   // worlds start at multiples of 8
     const int t = t0 + w;
     const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
     const int t_local = t - (int)wp->task_begin;
@@ -397,6 +398,26 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
         }
         if (a) atomicAdd(wp->stats, a);
         if (h) atomicAdd(wp->stats + 1, h);
+    }
+}
+
+// PERSIST (launches sized on the device): a fixed grid walks the 8-task groups of the device's
+// task count; otherwise one CTA per group.
+template <class Store, bool RECORD, bool IN_CTA, bool PERSIST = false>
+__global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? 6 : 4)
+finalize_kernel(const __grid_constant__ LaunchArgs la) {
+    __shared__ float4 s_mean[kFinWarps];
+    __shared__ int s_count[kFinWarps];
+    __shared__ unsigned s_stat[kFinWarps][2];
+    if (!PERSIST) {
+        finalize_group<Store, RECORD, IN_CTA>(la, (int)blockIdx.x, s_mean, s_count, s_stat);
+        return;
+    }
+    const long long total = la.dev_total ? __ldcg(la.dev_total) : (long long)la.chunk_end;
+    const int groups = (int)((min(total, (long long)la.chunk_end) - la.chunk_begin + kFinWarps - 1) / kFinWarps);
+    for (int g = (int)blockIdx.x; g < groups; g += (int)gridDim.x) {
+        finalize_group<Store, RECORD, IN_CTA>(la, g, s_mean, s_count, s_stat);
+        __syncthreads();   // thread 0 has read the counters before the next group clears them
     }
 }
 
@@ -477,6 +498,26 @@ cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_
     }
 }
 
+cudaError_t launch_table_pass(const LaunchArgs& a, int precision, int num_sms, cudaStream_t stream) {
+    const int blocks = march_grid(false, num_sms, a.n_tasks, a.march_ctas);
+    LaunchArgs args = a;
+    args.total_warps = blocks * kWarps;
+    args.chunk_begin = 0;
+    args.chunk_end = (int)a.n_tasks;
+    args.ray_origin = 0;
+    march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(args);
+    const int fin = num_sms * 6;   // the lean finalize's occupancy
+    switch (precision) {
+        case LUMRAD_PRECISION_FP16: finalize_kernel<StoreF16, false, true, true><<<fin, kFinWarps * 32, 0, stream>>>(args); break;
+        case LUMRAD_PRECISION_BF16: finalize_kernel<StoreBF16, false, true, true><<<fin, kFinWarps * 32, 0, stream>>>(args); break;
+        case LUMRAD_PRECISION_RGB10A2:
+            finalize_kernel<StoreRGB10A2, false, true, true><<<fin, kFinWarps * 32, 0, stream>>>(args);
+            break;
+        default: finalize_kernel<StoreF32, false, true, true><<<fin, kFinWarps * 32, 0, stream>>>(args);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream) {
     if (args.n_tasks <= 0) return cudaSuccess;
     switch (precision) {
@@ -500,7 +541,8 @@ namespace {
 // Start of a batched pass: each world's next volume becomes a copy of its previous one (probes
 // not in its list keep their value) and its counters are cleared.  blockIdx.y = world.
 template <typename V>
-__global__ void prep_kernel(const WorldPass* __restrict__ worlds) {
+__global__ void prep_kernel(const WorldPass* __restrict__ worlds, const int* dev_n) {
+    if (dev_n && (int)blockIdx.y >= __ldcg(dev_n)) return;   // a table built on the device
     const WorldPass& w = worlds[blockIdx.y];
     const long long n = (long long)w.X * w.Y * w.Z;
     const V* src = reinterpret_cast<const V*>(w.prev);
@@ -512,12 +554,12 @@ __global__ void prep_kernel(const WorldPass* __restrict__ worlds) {
 
 }  // namespace
 
-cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream) {
+cudaError_t launch_prep(const WorldPass* d_worlds, int n_worlds, int precision, cudaStream_t stream, const int* dev_n) {
     if (n_worlds <= 0) return cudaSuccess;
     const dim3 grid(32, n_worlds);
-    if (precision == LUMRAD_PRECISION_FP32) prep_kernel<uint4><<<grid, 256, 0, stream>>>(d_worlds);
-    else if (precision == LUMRAD_PRECISION_RGB10A2) prep_kernel<unsigned><<<grid, 256, 0, stream>>>(d_worlds);
-    else prep_kernel<uint2><<<grid, 256, 0, stream>>>(d_worlds);
+    if (precision == LUMRAD_PRECISION_FP32) prep_kernel<uint4><<<grid, 256, 0, stream>>>(d_worlds, dev_n);
+    else if (precision == LUMRAD_PRECISION_RGB10A2) prep_kernel<unsigned><<<grid, 256, 0, stream>>>(d_worlds, dev_n);
+    else prep_kernel<uint2><<<grid, 256, 0, stream>>>(d_worlds, dev_n);
     return cudaGetLastError();
 }
 

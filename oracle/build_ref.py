@@ -1,7 +1,7 @@
 """Compiles the reference shader, shaders/radiance.comp, as C++ — TEST INFRASTRUCTURE.
 
 The reference's GPU path is a Vulkan compute shader; no graphics stack exists here, so instead
-its own GLSL source (read where it lies, under /root/reference) is compiled on the CPU with g++
+its own GLSL source (read where it lies, in the reference tree) is compiled on the CPU with g++
 against oracle/glsl_shim.hpp.  The function bodies are compiled verbatim.  Only GLSL syntax that
 C++ cannot express is rewritten, each rewrite matched exactly and checked by count, so a change
 in the shader fails the build instead of silently drifting:
@@ -30,7 +30,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("LUM_REFERENCE", "/root/reference")
+# The reference tree: $LUM_REFERENCE, else a checkout named `reference` beside this repository
+# (absent on machines that only build from the generated source, see available())
+REFERENCE = os.environ.get("LUM_REFERENCE") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.realpath(HERE))), "reference")
 SHADER = os.path.join(REFERENCE, "shaders", "radiance.comp")
 CONSTS = os.path.join(REFERENCE, "shaders", "common", "consts.glsl")
 RAYS = (32, 64, 128, 256)
