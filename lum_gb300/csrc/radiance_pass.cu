@@ -159,58 +159,52 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         while (true) {
             bool fin = false;
 #pragma unroll
-            for (int u = 0; u < 2; u++) {   // (3 or 4 steps per iteration measured 0.7% slower)
-                if (my >= 0) {
-                    frac = fadd(frac, 0.5f);
-                    steps++;
-                    const float px = fadd(ox, fmul(dx, frac));
-                    const float py = fadd(oy, fmul(dy, frac));
-                    const float pz = fadd(oz, fmul(dz, frac));
-                    const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
-                    int cid;
-                    const bool solid = solid_at_w<WIDE>(mv, ix, iy, iz, cid);
-                    if (cid == 0) {
-                        // empty block: skip to its far corner (radiance.comp:215-226).  The block's
-                        // low corner (ix/16)*16 with ix = trunc(px) is trunc(px/16)*16, formed in
-                        // FP32 (exact: px/16 and the product by 16 are exact, |px| < 2^21; a NaN
-                        // px gives a NaN skip either way)
-                        const float bx = fadd(fmul(truncf(fmul(px, 0.0625f)), 16.0f), cx);
-                        const float by = fadd(fmul(truncf(fmul(py, 0.0625f)), 16.0f), cy);
-                        const float bz = fadd(fmul(truncf(fmul(pz, 0.0625f)), 16.0f), cz);
-                        const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
-                        const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
-                        const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
-                        if (FAST) frac = fadd(frac, fmaxf(fminf(tx, fminf(ty, tz)), 0.01f));
-                        else frac = fadd(frac, gmax(gmin(tx, gmin(ty, tz)), 0.01f));
+            for (int u = 0; u < 2; u++) {   // (3 or 4 steps per iteration measured 0.2-0.7% slower)
+                // Straight-line: every lane runs the step (an idle lane's stale ray reads only
+                // in-range cells and its results are dropped) and the empty-block skip
+                // (radiance.comp:215-226) is formed for every lane and selected where the block is
+                // air: no divergent branch per step (3% fewer instructions than branching).  The
+                // block's low corner (ix/16)*16 with ix = trunc(px) is trunc(px/16)*16, formed in
+                // FP32 (exact: px/16 and the product by 16 are exact, |px| < 2^21; a NaN px gives
+                // a NaN skip either way).
+                const bool act = my >= 0;
+                const float f1 = fadd(frac, 0.5f);
+                const int st = steps + 1;
+                const float px = fadd(ox, fmul(dx, f1));
+                const float py = fadd(oy, fmul(dy, f1));
+                const float pz = fadd(oz, fmul(dz, f1));
+                const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
+                int cid;
+                const bool solid = solid_at_w<WIDE>(mv, ix, iy, iz, cid);
+                const float bx = fadd(fmul(truncf(fmul(px, 0.0625f)), 16.0f), cx);
+                const float by = fadd(fmul(truncf(fmul(py, 0.0625f)), 16.0f), cy);
+                const float bz = fadd(fmul(truncf(fmul(pz, 0.0625f)), 16.0f), cz);
+                const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
+                const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
+                const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
+                const float sk = FAST ? fmaxf(fminf(tx, fminf(ty, tz)), 0.01f) : gmax(gmin(tx, gmin(ty, tz)), 0.01f);
+                const float f2 = cid == 0 ? fadd(f1, sk) : f1;
+                bool out;
+                if (FAST)
+                    out = __float_as_uint(px) >= uwx || __float_as_uint(py) >= uwy || __float_as_uint(pz) >= uwz ||
+                          f2 >= max_dist;
+                else
+                    out = px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz || f2 >= max_dist;
+                const bool capped = !FAST && st >= max_steps;
+                frac = f2;
+                steps = st;
+                const bool f = act && (solid || out || capped);
+                if (f) {
+                    uint32_t info = (uint32_t)st | (solid ? (1u << 24) : (out ? 0u : (1u << 25)));
+                    if (RECORD) {
+                        int blk;
+                        const int v = voxel_value(*wp, ix, iy, iz, blk);
+                        if (solid) info |= (uint32_t)v << 16;
+                        la.ray_blk[my] = blk;
                     }
-                    uint32_t info = 0;
-                    bool out;
-                    if (FAST)
-                        out = __float_as_uint(px) >= uwx || __float_as_uint(py) >= uwy || __float_as_uint(pz) >= uwz ||
-                              frac >= max_dist;
-                    else
-                        out = px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz ||
-                              frac >= max_dist;
-                    if (solid) {
-                        fin = true;
-                        info = (uint32_t)steps | (1u << 24);
-                    } else if (out) {
-                        fin = true;
-                        info = (uint32_t)steps;
-                    } else if (!FAST && steps >= max_steps) {
-                        fin = true;
-                        info = (uint32_t)steps | (1u << 25);
-                    }
-                    if (fin) {
-                        if (RECORD) {
-                            int blk;
-                            const int v = voxel_value(*wp, ix, iy, iz, blk);
-                            if (solid) info |= (uint32_t)v << 16;
-                            la.ray_blk[my] = blk;
-                        }
-                        __stcg(la.ray_res + my, make_uint2(__float_as_uint(frac), info));
-                        my = -1;
-                    }
+                    __stcg(la.ray_res + my, make_uint2(__float_as_uint(f2), info));
+                    my = -1;
+                    fin = true;
                 }
             }
             const unsigned fm = __ballot_sync(kFull, fin);
