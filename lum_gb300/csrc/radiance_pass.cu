@@ -45,7 +45,9 @@ namespace {
 //   (b) a position lies outside [0, 16*size) exactly when its bits, read as unsigned, are at
 //       least those of 16*size (no position is -0: no origin is, and a sum is -0 only if both
 //       terms are);
-//   (c) the 2*max_dist+2 step bound is never reached: the fraction passes max_dist first.
+//   (c) the 2*max_dist+2 step bound is never reached: the fraction passes max_dist first;
+//   (d) the grid lookup can take the block index and the range test from trunc(p/16) in FP32
+//       (solid_at_tb), which the empty-block skip needs anyway.
 // A warp whose rays are all regular marches with those forms (fewer compares and selects on the
 // integer/compare pipe, the one that limits this kernel); any other warp with the exact forms of
 // the general case.  Both give the same bits for a regular ray.
@@ -174,11 +176,13 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                 const float py = fadd(oy, fmul(dy, f1));
                 const float pz = fadd(oz, fmul(dz, f1));
                 const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
+                const float tbx = truncf(fmul(px, 0.0625f)), tby = truncf(fmul(py, 0.0625f)), tbz = truncf(fmul(pz, 0.0625f));
                 int cid;
-                const bool solid = solid_at_w<WIDE>(mv, ix, iy, iz, cid);
-                const float bx = fadd(fmul(truncf(fmul(px, 0.0625f)), 16.0f), cx);
-                const float by = fadd(fmul(truncf(fmul(py, 0.0625f)), 16.0f), cy);
-                const float bz = fadd(fmul(truncf(fmul(pz, 0.0625f)), 16.0f), cz);
+                const bool solid = FAST ? solid_at_tb<WIDE>(mv, tbx, tby, tbz, ix, iy, iz, cid)
+                                        : solid_at_w<WIDE>(mv, ix, iy, iz, cid);
+                const float bx = fadd(fmul(tbx, 16.0f), cx);
+                const float by = fadd(fmul(tby, 16.0f), cy);
+                const float bz = fadd(fmul(tbz, 16.0f), cz);
                 const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
                 const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
                 const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
