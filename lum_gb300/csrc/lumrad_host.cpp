@@ -313,6 +313,7 @@ int DeviceWorld::fill_pass(const short4* d_req, int n, const LumRadPassParams& p
     w.grid = d_grid;
     w.pal = d_pal;
     w.n_slots = n_slots;
+    w.n_compact = n_compact;
     w.mats = d_mats;
     w.prev = d_rad[cur];
     w.next = d_rad[1 - cur];

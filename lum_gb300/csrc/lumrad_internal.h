@@ -44,7 +44,7 @@ struct WorldPass {
     const int16_t* grid;         // X*Y*Z block ids
     const uint8_t* pal;          // n_slots * 4096 voxels, voxel (x,y,z) at x + 16y + 256z
     int n_slots;
-    int pad0;
+    int n_compact;               // compact ids in cbits (0: unknown)
     const float4* mats;          // 256 x (r, g, b, emission)
     const void* prev;            // radiance read
     void* next;                  // radiance written (holds a copy of prev before the pass)

@@ -138,16 +138,26 @@ __device__ __forceinline__ bool solid_at(const MarchView& m, int ix, int iy, int
     return (row >> (ix & 15)) & 1u;
 }
 
-// The same with the compact id's width known at compile time (WIDE: uint16 ids, else uint8).
-template <bool WIDE>
-__device__ __forceinline__ bool solid_at_w(const MarchView& m, int ix, int iy, int iz, int& cid) {
+// The same with the compact id's width known at compile time (WIDE: uint16 ids, else uint8), on
+// the compact grid `cg` and the masks' 16-bit rows `rows`, in global memory (read through the
+// read-only path) or, SMEM, staged in shared memory.
+template <bool WIDE, bool SMEM>
+__device__ __forceinline__ bool solid_at_p(const uint8_t* cg, const uint16_t* rows, int X, int Y, int Z, int ix,
+                                           int iy, int iz, int& cid) {
     int idx;
     int c = 0;
-    if (grid_index(m.X, m.Y, m.Z, ix, iy, iz, idx))
-        c = WIDE ? (int)__ldg(reinterpret_cast<const uint16_t*>(m.cgrid) + idx) : (int)__ldg(m.cgrid + idx);
+    if (grid_index(X, Y, Z, ix, iy, iz, idx)) {
+        if (SMEM) c = WIDE ? (int)reinterpret_cast<const uint16_t*>(cg)[idx] : (int)cg[idx];
+        else c = WIDE ? (int)__ldg(reinterpret_cast<const uint16_t*>(cg) + idx) : (int)__ldg(cg + idx);
+    }
     cid = c;
-    const unsigned row = __ldg(reinterpret_cast<const uint16_t*>(m.cbits) + ((c << 8) | ((iz & 15) << 4) | (iy & 15)));
+    const int r = (c << 8) | ((iz & 15) << 4) | (iy & 15);
+    const unsigned row = SMEM ? (unsigned)rows[r] : (unsigned)__ldg(rows + r);
     return (row >> (ix & 15)) & 1u;
+}
+template <bool WIDE>
+__device__ __forceinline__ bool solid_at_w(const MarchView& m, int ix, int iy, int iz, int& cid) {
+    return solid_at_p<WIDE, false>(m.cgrid, reinterpret_cast<const uint16_t*>(m.cbits), m.X, m.Y, m.Z, ix, iy, iz, cid);
 }
 
 // solid_at_w for a regular ray's position (finite, |p| < 2^21), from tb = trunc(p/16) per axis
@@ -155,19 +165,21 @@ __device__ __forceinline__ bool solid_at_w(const MarchView& m, int ix, int iy, i
 // when 0 <= trunc(p/16) < size (p in (-16, 0) gives -0, block 0 like OpSDiv).  The block index is
 // the float's integer through the bits of 1.5*2^23 + tb (an add; -0 becomes +0), and the range test
 // one unsigned compare per axis.
-template <bool WIDE>
-__device__ __forceinline__ bool solid_at_tb(const MarchView& m, float tbx, float tby, float tbz, int ix, int iy,
-                                            int iz, int& cid) {
+template <bool WIDE, bool SMEM>
+__device__ __forceinline__ bool solid_at_tbp(const uint8_t* cg, const uint16_t* rows, int X, int Y, int Z, float tbx,
+                                             float tby, float tbz, int ix, int iy, int iz, int& cid) {
     const int bx = __float_as_int(fadd(tbx, 12582912.0f)) - 0x4B400000;
     const int by = __float_as_int(fadd(tby, 12582912.0f)) - 0x4B400000;
     const int bz = __float_as_int(fadd(tbz, 12582912.0f)) - 0x4B400000;
     int c = 0;
-    if ((unsigned)bx < (unsigned)m.X && (unsigned)by < (unsigned)m.Y && (unsigned)bz < (unsigned)m.Z) {
-        const int idx = bx + m.X * (by + m.Y * bz);
-        c = WIDE ? (int)__ldg(reinterpret_cast<const uint16_t*>(m.cgrid) + idx) : (int)__ldg(m.cgrid + idx);
+    if ((unsigned)bx < (unsigned)X && (unsigned)by < (unsigned)Y && (unsigned)bz < (unsigned)Z) {
+        const int idx = bx + X * (by + Y * bz);
+        if (SMEM) c = WIDE ? (int)reinterpret_cast<const uint16_t*>(cg)[idx] : (int)cg[idx];
+        else c = WIDE ? (int)__ldg(reinterpret_cast<const uint16_t*>(cg) + idx) : (int)__ldg(cg + idx);
     }
     cid = c;
-    const unsigned row = __ldg(reinterpret_cast<const uint16_t*>(m.cbits) + ((c << 8) | ((iz & 15) << 4) | (iy & 15)));
+    const int r = (c << 8) | ((iz & 15) << 4) | (iy & 15);
+    const unsigned row = SMEM ? (unsigned)rows[r] : (unsigned)__ldg(rows + r);
     return (row >> (ix & 15)) & 1u;
 }
 
