@@ -58,14 +58,14 @@ S_R = 12            # bytes of FP32 RGB radiance per probe
 BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches) in an ncu capture of this workload; ncu replays with cold caches
-# (march 1.09 + 46.04 MB, finalizes 118.25 + 0.00 MB)
-NCU_DRAM_BYTES_PER_STEP = 165.38e6
-# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 634.9 MB,
-# finalizes 987.3 MB)
-NCU_L2_BYTES_PER_STEP = 1622.1e6
+# (march 1.04 + 46.23 MB, finalizes 118.23 + 0.00 MB)
+NCU_DRAM_BYTES_PER_STEP = 165.50e6
+# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 493.6 MB: its world
+# lookups are shared-memory loads, finalizes 986.7 MB)
+NCU_L2_BYTES_PER_STEP = 1480.3e6
 # Warp instructions (smsp__inst_executed.sum) of the same 9 launches: the march over the 8 passes
-# (508.7 M) and the 8 finalize launches (409.7 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 508.7e6 + 409.7e6
+# (463.0 M) and the 8 finalize launches (406.7 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 463.0e6 + 406.7e6
 SCHEDULERS_PER_SM = 4
 
 
