@@ -90,8 +90,9 @@ struct LaunchArgs {
     // and the number of worlds in the table, read by the kernels; null otherwise
     const long long* dev_total;
     const int* dev_n_worlds;
-    // scheduling (0 = default): a warp claims remaining / (guided_div * warps) tasks at a time,
-    // clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM (capped by occupancy)
+    // scheduling (0 = the kernel's defaults, 1 and 32): a warp claims remaining / (guided_div *
+    // warps) tasks at a time, clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM
+    // (capped by occupancy)
     int guided_div, max_chunk, march_ctas;
 };
 
@@ -105,7 +106,8 @@ inline bool combines_in_cta(const WorldPass* w, int n) {
     return true;
 }
 
-// Tunable scheduling of a launch (see LaunchArgs); the defaults are 2, 16 and the occupancy limit.
+// Tunable scheduling of a multi-world launch (see LaunchArgs): batches start from these and
+// autotune; servers use them as they are.
 struct Tuning {
     int guided_div = 2;
     int max_chunk = 16;
