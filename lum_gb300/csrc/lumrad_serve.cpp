@@ -502,17 +502,21 @@ int progress(Server* sv) {
 
 // ---------------------------------------------------------------- device-resident loop
 // The host side of the loop of radiance_serve.cu: requests wait here in submission order until
-// due, then are copied into the page-locked ring (their edits into the edit arena) and the ring's
-// head is published; the GPU's completion records are read back from the other ring.  The host
-// makes no CUDA call per request: it starts the loop's graph again only when the loop has ended
-// (no request within poll_ms) and a published request waits.
-struct DevLoopHost {
+// due, then are copied into a page-locked ring (their edits into an edit arena) and the ring's
+// head is published; the GPU's completion records are read back from another ring.  The host
+// makes no CUDA call per request: it starts a loop's graph again only when that loop has ended
+// (no request within poll_ms) and a published request waits.  Worlds are split over kDevLanes
+// independent loops (world w in lane w % kDevLanes), each with its own rings, stream, graph and
+// ray buffer, so one lane's small kernels and its pass's drain overlap the other's pass; a world's
+// requests stay in one lane, in order.
+constexpr int kDevLanes = 2;
+
+struct DevLane {
     struct Published {
         long long id;
         int world, rays;
         double arrival, start;
     };
-    long long ring_cap = 1 << 16, edit_cap = 1 << 22;
     DevRequest* ring = nullptr;          // page-locked, mapped (host pointers; the device's below)
     LumRadEdit* edits = nullptr;
     DevCompletion* done = nullptr;
@@ -523,24 +527,29 @@ struct DevLoopHost {
     long long* d_ctl = nullptr;
     long long head = 0, done_read = 0, edit_head = 0, edit_tail = 0;
     std::deque<long long> edit_ends;     // arena position after each published request's edits
-    std::deque<SRequest> queue;          // submitted, not yet published
     std::deque<Published> published;     // published, not yet completed (ring order)
-    std::vector<int> outstanding;        // per world: published, not completed
     DevLoop* d_loop = nullptr;
-    DevWorld* d_worlds = nullptr;
-    std::vector<void*> bufs;             // per-world device buffers of the loop
     int* d_chunk_count = nullptr;
     int* d_chunk_off = nullptr;
     long long chunk_cap = 0, chunks_total = 0;
     int* d_error = nullptr;
     unsigned long long* d_queue = nullptr;
     uint2* d_ray_res = nullptr;
-    long long max_tasks = 1 << 20;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_end = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool running = false;
+};
+
+struct DevLoopHost {
+    long long ring_cap = 1 << 16, edit_cap = 1 << 22;
+    long long max_tasks = 1 << 20;       // per lane and iteration
+    DevLane lanes[kDevLanes];
+    std::deque<SRequest> queue;          // submitted, not yet published
+    std::vector<int> outstanding;        // per world: published, not completed
+    DevWorld* d_worlds = nullptr;
+    std::vector<void*> bufs;             // per-world device buffers of the loop
     double offset_s = 0.0;               // host clock = %globaltimer * 1e-9 - offset_s
     unsigned long long* h_timer = nullptr;
 };
@@ -553,63 +562,58 @@ int host_mapped(T** h, T** d, size_t n) {
     return LUMRAD_OK;
 }
 
-volatile long long& ctl_word(DevLoopHost& dl, int k) { return reinterpret_cast<volatile long long*>(dl.ctl)[k]; }
+volatile long long& ctl_word(DevLane& ln, int k) { return reinterpret_cast<volatile long long*>(ln.ctl)[k]; }
 
-int devloop_create(Server* sv) {
-    DevLoopHost* dl = new DevLoopHost();
-    sv->dl = dl;
+int devloop_lane_create(Server* sv, DevLoopHost& dl, DevLane& ln) {
     int rc;
-    if ((rc = host_mapped(&dl->ring, &dl->d_ring, (size_t)dl->ring_cap))) return rc;
-    if ((rc = host_mapped(&dl->edits, &dl->d_edits, (size_t)dl->edit_cap))) return rc;
-    if ((rc = host_mapped(&dl->done, &dl->d_done, (size_t)dl->ring_cap))) return rc;
-    if ((rc = host_mapped(&dl->ctl, &dl->d_ctl, 8))) return rc;
-    unsigned long long* d_timer = nullptr;
-    if ((rc = host_mapped(&dl->h_timer, &d_timer, 1))) return rc;
-    LUMRAD_TRY(cudaStreamCreateWithFlags(&dl->stream, cudaStreamNonBlocking));
-    LUMRAD_TRY(cudaEventCreateWithFlags(&dl->ev_end, cudaEventDisableTiming));
-    LUMRAD_TRY(cudaMalloc(&dl->d_loop, sizeof(DevLoop)));
-    LUMRAD_TRY(cudaMalloc(&dl->d_worlds, kDevMaxWorlds * sizeof(DevWorld)));
-    LUMRAD_TRY(cudaMalloc(&dl->d_error, sizeof(int)));
-    LUMRAD_TRY(cudaMalloc(&dl->d_queue, kQueueWords * sizeof(unsigned long long)));
-    LUMRAD_TRY(cudaMalloc(&dl->d_ray_res, (size_t)dl->max_tasks * kTaskRays * sizeof(uint2)));
-    LUMRAD_TRY(cudaMemsetAsync(dl->d_error, 0, sizeof(int), dl->stream));
-    LUMRAD_TRY(cudaMemsetAsync(dl->d_queue, 0, kQueueWords * sizeof(unsigned long long), dl->stream));
+    if ((rc = host_mapped(&ln.ring, &ln.d_ring, (size_t)dl.ring_cap))) return rc;
+    if ((rc = host_mapped(&ln.edits, &ln.d_edits, (size_t)dl.edit_cap))) return rc;
+    if ((rc = host_mapped(&ln.done, &ln.d_done, (size_t)dl.ring_cap))) return rc;
+    if ((rc = host_mapped(&ln.ctl, &ln.d_ctl, 8))) return rc;
+    LUMRAD_TRY(cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking));
+    LUMRAD_TRY(cudaEventCreateWithFlags(&ln.ev_end, cudaEventDisableTiming));
+    LUMRAD_TRY(cudaMalloc(&ln.d_loop, sizeof(DevLoop)));
+    LUMRAD_TRY(cudaMalloc(&ln.d_error, sizeof(int)));
+    LUMRAD_TRY(cudaMalloc(&ln.d_queue, kQueueWords * sizeof(unsigned long long)));
+    LUMRAD_TRY(cudaMalloc(&ln.d_ray_res, (size_t)dl.max_tasks * kTaskRays * sizeof(uint2)));
+    LUMRAD_TRY(cudaMemsetAsync(ln.d_error, 0, sizeof(int), ln.stream));
+    LUMRAD_TRY(cudaMemsetAsync(ln.d_queue, 0, kQueueWords * sizeof(unsigned long long), ln.stream));
     std::unique_ptr<DevLoop> h(new DevLoop());
     std::memset(static_cast<void*>(h.get()), 0, sizeof(DevLoop));
-    h->ring = dl->d_ring;
-    h->ring_cap = dl->ring_cap;
-    h->head = dl->d_ctl;
-    h->tail_host = dl->d_ctl + 1;
-    h->edits = dl->d_edits;
-    h->edit_cap = dl->edit_cap;
-    h->done = dl->d_done;
-    h->done_head = dl->d_ctl + 2;
-    h->stop = reinterpret_cast<const int*>(dl->d_ctl + 3);
-    h->worlds = dl->d_worlds;
+    h->ring = ln.d_ring;
+    h->ring_cap = dl.ring_cap;
+    h->head = ln.d_ctl;
+    h->tail_host = ln.d_ctl + 1;
+    h->edits = ln.d_edits;
+    h->edit_cap = dl.edit_cap;
+    h->done = ln.d_done;
+    h->done_head = ln.d_ctl + 2;
+    h->stop = reinterpret_cast<const int*>(ln.d_ctl + 3);
+    h->worlds = dl.d_worlds;
     h->poll_ns = (unsigned long long)((sv->s.poll_ms > 0.0f ? sv->s.poll_ms : 2.0f) * 1e6);
-    h->max_tasks = dl->max_tasks;
+    h->max_tasks = dl.max_tasks;
     h->radius = sv->s.radius;
-    h->error = dl->d_error;
-    h->queue = dl->d_queue;
+    h->error = ln.d_error;
+    h->queue = ln.d_queue;
     h->iteration = 1;
-    LUMRAD_TRY(cudaMemcpyAsync(dl->d_loop, h.get(), sizeof(DevLoop), cudaMemcpyHostToDevice, dl->stream));
-    LUMRAD_TRY(cudaStreamSynchronize(dl->stream));
+    LUMRAD_TRY(cudaMemcpyAsync(ln.d_loop, h.get(), sizeof(DevLoop), cudaMemcpyHostToDevice, ln.stream));
+    LUMRAD_TRY(cudaStreamSynchronize(ln.stream));
 
     // the graph: one WHILE node whose body is one iteration of the loop
-    LUMRAD_TRY(cudaGraphCreate(&dl->graph, 0));
+    LUMRAD_TRY(cudaGraphCreate(&ln.graph, 0));
     cudaGraphConditionalHandle cond;
-    LUMRAD_TRY(cudaGraphConditionalHandleCreate(&cond, dl->graph, 1, cudaGraphCondAssignDefault));
+    LUMRAD_TRY(cudaGraphConditionalHandleCreate(&cond, ln.graph, 1, cudaGraphCondAssignDefault));
     cudaGraphNodeParams np = {};
     np.type = cudaGraphNodeTypeConditional;
     np.conditional.handle = cond;
     np.conditional.type = cudaGraphCondTypeWhile;
     np.conditional.size = 1;
     cudaGraphNode_t node;
-    LUMRAD_TRY(cudaGraphAddNode(&node, dl->graph, nullptr, nullptr, 0, &np));
+    LUMRAD_TRY(cudaGraphAddNode(&node, ln.graph, nullptr, nullptr, 0, &np));
     cudaGraph_t body = np.conditional.phGraph_out[0];
     DevLoopLaunch a;
     std::memset(static_cast<void*>(&a), 0, sizeof a);
-    char* base = reinterpret_cast<char*>(dl->d_loop);
+    char* base = reinterpret_cast<char*>(ln.d_loop);
     a.table = reinterpret_cast<const WorldPass*>(base + offsetof(DevLoop, table));
     a.n_table = reinterpret_cast<const int*>(base + offsetof(DevLoop, n_table));
     a.precision = sv->s.precision;
@@ -619,53 +623,66 @@ int devloop_create(Server* sv) {
     la.n_worlds = kDevBatch;
     la.dev_n_worlds = a.n_table;
     la.dev_total = reinterpret_cast<const long long*>(base + offsetof(DevLoop, total_tasks));
-    la.n_tasks = dl->max_tasks;
-    la.queue = dl->d_queue;
-    la.error = dl->d_error;
-    la.ray_res = dl->d_ray_res;
+    la.n_tasks = dl.max_tasks;
+    la.queue = ln.d_queue;
+    la.error = ln.d_error;
+    la.ray_res = ln.d_ray_res;
     la.in_cta = 1;
-    LUMRAD_TRY(cudaStreamBeginCaptureToGraph(dl->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    const cudaError_t ce = capture_devloop_body(dl->d_loop, a, cond, dl->stream);
-    const cudaError_t ee = cudaStreamEndCapture(dl->stream, &body);
+    LUMRAD_TRY(cudaStreamBeginCaptureToGraph(ln.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t ce = capture_devloop_body(ln.d_loop, a, cond, ln.stream);
+    const cudaError_t ee = cudaStreamEndCapture(ln.stream, &body);
     LUMRAD_TRY(ce);
     LUMRAD_TRY(ee);
-    LUMRAD_TRY(cudaGraphInstantiate(&dl->exec, dl->graph, 0));
+    LUMRAD_TRY(cudaGraphInstantiate(&ln.exec, ln.graph, 0));
+    sv->fixed += (size_t)dl.max_tasks * kTaskRays * sizeof(uint2) + sizeof(DevLoop);
+    return LUMRAD_OK;
+}
 
+int devloop_create(Server* sv) {
+    DevLoopHost* dl = new DevLoopHost();
+    sv->dl = dl;
+    int rc;
+    LUMRAD_TRY(cudaMalloc(&dl->d_worlds, kDevMaxWorlds * sizeof(DevWorld)));
+    sv->fixed += kDevMaxWorlds * sizeof(DevWorld);
+    for (DevLane& ln : dl->lanes)
+        if ((rc = devloop_lane_create(sv, *dl, ln))) return rc;
     // the device clock against the host's: the read with the shortest round trip
+    unsigned long long* d_timer = nullptr;
+    if ((rc = host_mapped(&dl->h_timer, &d_timer, 1))) return rc;
     double best = 1e9;
     for (int i = 0; i < 20; i++) {
         const double t0 = clock_s();
-        LUMRAD_TRY(launch_read_globaltimer(d_timer, dl->stream));
-        LUMRAD_TRY(cudaStreamSynchronize(dl->stream));
+        LUMRAD_TRY(launch_read_globaltimer(d_timer, dl->lanes[0].stream));
+        LUMRAD_TRY(cudaStreamSynchronize(dl->lanes[0].stream));
         const double t1 = clock_s();
         if (t1 - t0 < best) {
             best = t1 - t0;
             dl->offset_s = (double)*reinterpret_cast<volatile unsigned long long*>(dl->h_timer) * 1e-9 - 0.5 * (t0 + t1);
         }
     }
-    sv->fixed += (size_t)dl->max_tasks * kTaskRays * sizeof(uint2) + sizeof(DevLoop) + kDevMaxWorlds * sizeof(DevWorld);
     return LUMRAD_OK;
 }
 
-// Ends the loop (it stops at its next admit) and waits for it; the flag is cleared again.
-int devloop_halt(DevLoopHost* dl) {
-    if (!dl->running) return LUMRAD_OK;
-    ctl_word(*dl, 3) = 1;
-    const cudaError_t e = cudaStreamSynchronize(dl->stream);
-    ctl_word(*dl, 3) = 0;
-    dl->running = false;
+// Ends a lane's loop (it stops at its next admit) and waits for it; the flag is cleared again.
+int devloop_halt(DevLane& ln) {
+    if (!ln.running) return LUMRAD_OK;
+    ctl_word(ln, 3) = 1;
+    const cudaError_t e = cudaStreamSynchronize(ln.stream);
+    ctl_word(ln, 3) = 0;
+    ln.running = false;
     LUMRAD_TRY(e);
     return LUMRAD_OK;
 }
 
 int devloop_add_world(Server* sv, Context* c, int id, size_t* bytes) {
     DevLoopHost& dl = *sv->dl;
+    DevLane& ln = dl.lanes[id % kDevLanes];
     DeviceWorld& dw = c->world;
     if (id >= kDevMaxWorlds) return fail(LUMRAD_EINVAL, "the device loop holds at most 1024 worlds");
     if (dw.n_slots > 192) return fail(LUMRAD_EINVAL, "the device loop needs max_block_types <= 192");
     if ((long long)dw.W > dl.max_tasks) return fail(LUMRAD_EINVAL, "world too large for the device loop (2^20 blocks)");
     if (dw.cgrid_wide) return fail(LUMRAD_EINVAL, "the device loop needs at most 256 distinct block ids");
-    int rc = devloop_halt(&dl);
+    int rc = devloop_halt(ln);
     if (rc) return rc;
     // every id with a palette slot, and the shared empty id, gets its compact id now: the loop's
     // edits then only look ids up
@@ -715,20 +732,20 @@ int devloop_add_world(Server* sv, Context* c, int id, size_t* bytes) {
     w.cur = dw.cur;
     LUMRAD_TRY(cudaMemcpyAsync(dl.d_worlds + id, &w, sizeof w, cudaMemcpyHostToDevice, c->stream));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));
-    // chunk arrays for every world's chunks (a batch holds each world at most once)
-    dl.chunks_total += ((long long)dw.W + kDevChunk - 1) / kDevChunk;
-    if (dl.chunks_total > dl.chunk_cap) {
-        const long long cap = std::max(dl.chunks_total, 2 * dl.chunk_cap);
-        cudaFree(dl.d_chunk_count);
-        cudaFree(dl.d_chunk_off);
-        dl.d_chunk_count = dl.d_chunk_off = nullptr;
-        LUMRAD_TRY(cudaMalloc(&dl.d_chunk_count, cap * sizeof(int)));
-        LUMRAD_TRY(cudaMalloc(&dl.d_chunk_off, cap * sizeof(int)));
-        dl.chunk_cap = cap;
-        int* ptrs[2] = {dl.d_chunk_count, dl.d_chunk_off};
-        LUMRAD_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(dl.d_loop) + offsetof(DevLoop, chunk_count), ptrs,
-                                   sizeof ptrs, cudaMemcpyHostToDevice, dl.stream));
-        LUMRAD_TRY(cudaStreamSynchronize(dl.stream));
+    // the lane's chunk arrays: room for its worlds' chunks (a batch holds each world at most once)
+    ln.chunks_total += ((long long)dw.W + kDevChunk - 1) / kDevChunk;
+    if (ln.chunks_total > ln.chunk_cap) {
+        const long long cap = std::max(ln.chunks_total, 2 * ln.chunk_cap);
+        cudaFree(ln.d_chunk_count);
+        cudaFree(ln.d_chunk_off);
+        ln.d_chunk_count = ln.d_chunk_off = nullptr;
+        LUMRAD_TRY(cudaMalloc(&ln.d_chunk_count, cap * sizeof(int)));
+        LUMRAD_TRY(cudaMalloc(&ln.d_chunk_off, cap * sizeof(int)));
+        ln.chunk_cap = cap;
+        int* ptrs[2] = {ln.d_chunk_count, ln.d_chunk_off};
+        LUMRAD_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ln.d_loop) + offsetof(DevLoop, chunk_count), ptrs,
+                                   sizeof ptrs, cudaMemcpyHostToDevice, ln.stream));
+        LUMRAD_TRY(cudaStreamSynchronize(ln.stream));
     }
     dl.outstanding.resize((size_t)id + 1, 0);
     *bytes = dw.W * (1 + sizeof(unsigned long long) + sizeof(short4)) + cmap.size() * sizeof(int16_t);
@@ -738,71 +755,77 @@ int devloop_add_world(Server* sv, Context* c, int id, size_t* bytes) {
 int devloop_progress(Server* sv) {
     DevLoopHost& dl = *sv->dl;
     // completions the GPU wrote
-    const long long dh = ctl_word(dl, 2);
-    std::atomic_thread_fence(std::memory_order_acquire);
-    for (; dl.done_read < dh; dl.done_read++) {
-        const DevCompletion& c = dl.done[dl.done_read % dl.ring_cap];
-        const DevLoopHost::Published pr = dl.published.front();
-        dl.published.pop_front();
-        LumRadCompletion o{};
-        o.request = pr.id;
-        o.world = pr.world;
-        o.status = c.id == pr.id ? c.status : LUMRAD_EDEVICE;
-        o.probes = c.probes;
-        o.rays_per_probe = pr.rays;
-        o.arrival_s = pr.arrival;
-        o.start_s = pr.start;
-        o.done_s = (double)c.t_done_ns * 1e-9 - dl.offset_s - sv->t0;
-        sv->done.push_back(o);
-        sv->pending--;
-        dl.outstanding[pr.world]--;
-        sv->st.requests++;
-        sv->st.probes += (unsigned long long)c.probes;
-        sv->st.rays += (unsigned long long)c.probes * (unsigned long long)pr.rays;
-        dl.edit_tail = dl.edit_ends.front();
-        dl.edit_ends.pop_front();
+    for (DevLane& ln : dl.lanes) {
+        const long long dh = ctl_word(ln, 2);
+        std::atomic_thread_fence(std::memory_order_acquire);
+        for (; ln.done_read < dh; ln.done_read++) {
+            const DevCompletion& c = ln.done[ln.done_read % dl.ring_cap];
+            const DevLane::Published pr = ln.published.front();
+            ln.published.pop_front();
+            LumRadCompletion o{};
+            o.request = pr.id;
+            o.world = pr.world;
+            o.status = c.id == pr.id ? c.status : LUMRAD_EDEVICE;
+            o.probes = c.probes;
+            o.rays_per_probe = pr.rays;
+            o.arrival_s = pr.arrival;
+            o.start_s = pr.start;
+            o.done_s = (double)c.t_done_ns * 1e-9 - dl.offset_s - sv->t0;
+            sv->done.push_back(o);
+            sv->pending--;
+            dl.outstanding[pr.world]--;
+            sv->st.requests++;
+            sv->st.probes += (unsigned long long)c.probes;
+            sv->st.rays += (unsigned long long)c.probes * (unsigned long long)pr.rays;
+            ln.edit_tail = ln.edit_ends.front();
+            ln.edit_ends.pop_front();
+        }
     }
-    // due requests into the ring, in submission order
+    // due requests into their lanes' rings, in submission order
     const double now = sv->now();
-    bool published = false;
+    bool published[kDevLanes] = {};
     while (!dl.queue.empty()) {
         SRequest& r = dl.queue.front();
         if (r.arrival > now) break;
+        DevLane& ln = dl.lanes[r.world % kDevLanes];
         const long long ne = (long long)r.edits.size();
-        if (dl.head - dl.done_read >= dl.ring_cap || ne > dl.edit_cap - (dl.edit_head - dl.edit_tail)) break;
-        for (long long k = 0; k < ne; k++) dl.edits[(dl.edit_head + k) % dl.edit_cap] = r.edits[(size_t)k];
-        DevRequest& q = dl.ring[dl.head % dl.ring_cap];
+        if (ln.head - ln.done_read >= dl.ring_cap || ne > dl.edit_cap - (ln.edit_head - ln.edit_tail)) break;
+        for (long long k = 0; k < ne; k++) ln.edits[(ln.edit_head + k) % dl.edit_cap] = r.edits[(size_t)k];
+        DevRequest& q = ln.ring[ln.head % dl.ring_cap];
         q.id = r.id;
-        q.edit_off = dl.edit_head % dl.edit_cap;
+        q.edit_off = ln.edit_head % dl.edit_cap;
         q.world = r.world;
         q.n_edits = (int)ne;
         q.rays = r.p.rays_per_probe;
         q.time_seed = r.p.time_seed;
         q.max_dist = r.p.max_dist;
         q.blend = r.p.blend;
-        dl.edit_head += ne;
-        dl.edit_ends.push_back(dl.edit_head);
-        dl.published.push_back(DevLoopHost::Published{r.id, r.world, r.p.rays_per_probe, r.arrival, now});
+        ln.edit_head += ne;
+        ln.edit_ends.push_back(ln.edit_head);
+        ln.published.push_back(DevLane::Published{r.id, r.world, r.p.rays_per_probe, r.arrival, now});
         dl.outstanding[r.world]++;
-        dl.head++;
+        ln.head++;
+        published[r.world % kDevLanes] = true;
         dl.queue.pop_front();
-        published = true;
     }
-    if (published) {
-        std::atomic_thread_fence(std::memory_order_release);   // the entries before the head
-        ctl_word(dl, 0) = dl.head;
-    }
-    // the loop ended (no request within poll_ms): start it again if a published request waits
-    if (dl.running) {
-        const cudaError_t q = cudaEventQuery(dl.ev_end);
-        if (q == cudaSuccess) dl.running = false;
-        else if (q != cudaErrorNotReady) LUMRAD_TRY(q);
-    }
-    if (!dl.running && dl.head > dl.done_read) {
-        LUMRAD_TRY(cudaGraphLaunch(dl.exec, dl.stream));
-        LUMRAD_TRY(cudaEventRecord(dl.ev_end, dl.stream));
-        dl.running = true;
-        sv->st.launches++;
+    for (int l = 0; l < kDevLanes; l++) {
+        DevLane& ln = dl.lanes[l];
+        if (published[l]) {
+            std::atomic_thread_fence(std::memory_order_release);   // the entries before the head
+            ctl_word(ln, 0) = ln.head;
+        }
+        // the loop ended (no request within poll_ms): start it again if a published request waits
+        if (ln.running) {
+            const cudaError_t q = cudaEventQuery(ln.ev_end);
+            if (q == cudaSuccess) ln.running = false;
+            else if (q != cudaErrorNotReady) LUMRAD_TRY(q);
+        }
+        if (!ln.running && ln.head > ln.done_read) {
+            LUMRAD_TRY(cudaGraphLaunch(ln.exec, ln.stream));
+            LUMRAD_TRY(cudaEventRecord(ln.ev_end, ln.stream));
+            ln.running = true;
+            sv->st.launches++;
+        }
     }
     return LUMRAD_OK;
 }
@@ -810,10 +833,11 @@ int devloop_progress(Server* sv) {
 void devloop_destroy(Server* sv) {
     DevLoopHost* dl = sv->dl;
     if (!dl) return;
-    if (dl->ctl) {
-        ctl_word(*dl, 3) = 1;
-        if (dl->stream) cudaStreamSynchronize(dl->stream);
-    }
+    for (DevLane& ln : dl->lanes)
+        if (ln.ctl) {
+            ctl_word(ln, 3) = 1;
+            if (ln.stream) cudaStreamSynchronize(ln.stream);
+        }
     // the worlds go back to their contexts as the loop left them: volume side and grid
     for (size_t w = 0; w < sv->worlds.size() && dl->d_worlds && w < dl->outstanding.size(); w++) {
         DeviceWorld& dw = sv->worlds[w].ctx->world;
@@ -822,23 +846,25 @@ void devloop_destroy(Server* sv) {
         if (cudaMemcpy(dw.h_grid.data(), dw.d_grid, dw.W * sizeof(int16_t), cudaMemcpyDeviceToHost) == cudaSuccess)
             dw.grid_dirty = true;
     }
-    if (dl->exec) cudaGraphExecDestroy(dl->exec);
-    if (dl->graph) cudaGraphDestroy(dl->graph);
+    for (DevLane& ln : dl->lanes) {
+        if (ln.exec) cudaGraphExecDestroy(ln.exec);
+        if (ln.graph) cudaGraphDestroy(ln.graph);
+        cudaFree(ln.d_chunk_count);
+        cudaFree(ln.d_chunk_off);
+        cudaFree(ln.d_ray_res);
+        cudaFree(ln.d_queue);
+        cudaFree(ln.d_error);
+        cudaFree(ln.d_loop);
+        if (ln.ring) cudaFreeHost(ln.ring);
+        if (ln.edits) cudaFreeHost(ln.edits);
+        if (ln.done) cudaFreeHost(ln.done);
+        if (ln.ctl) cudaFreeHost(ln.ctl);
+        if (ln.ev_end) cudaEventDestroy(ln.ev_end);
+        if (ln.stream) cudaStreamDestroy(ln.stream);
+    }
     for (void* p : dl->bufs) cudaFree(p);
-    cudaFree(dl->d_chunk_count);
-    cudaFree(dl->d_chunk_off);
-    cudaFree(dl->d_ray_res);
-    cudaFree(dl->d_queue);
-    cudaFree(dl->d_error);
     cudaFree(dl->d_worlds);
-    cudaFree(dl->d_loop);
-    if (dl->ring) cudaFreeHost(dl->ring);
-    if (dl->edits) cudaFreeHost(dl->edits);
-    if (dl->done) cudaFreeHost(dl->done);
-    if (dl->ctl) cudaFreeHost(dl->ctl);
     if (dl->h_timer) cudaFreeHost(dl->h_timer);
-    if (dl->ev_end) cudaEventDestroy(dl->ev_end);
-    if (dl->stream) cudaStreamDestroy(dl->stream);
     delete dl;
     sv->dl = nullptr;
 }
