@@ -280,14 +280,17 @@ int DeviceWorld::ensure_hits(size_t n) {
 }
 
 // Fills the kernel's view of one pass over `d_req` (n requests) with parameters `p`
-// (size >= 1) reading rad[cur] and writing rad[1-cur].
+// (size >= 1) reading rad[cur] and writing rad[1-cur], and the pass's start: next starts as a copy
+// of prev (probes not in the list keep their value) and the counters are cleared, both by the
+// first march launch.
 int DeviceWorld::prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream,
-                              WorldPass* out) {
-    int rc = fill_pass(d_req, n, p, stream, out);
+                              LaunchArgs* la) {
+    int rc = fill_pass(d_req, n, p, stream, &la->single);
     if (rc) return rc;
-    // probes not in the list keep their value: next starts as a copy of prev
-    LUMRAD_TRY(cudaMemcpyAsync(d_rad[1 - cur], d_rad[cur], W * rad_stride, cudaMemcpyDeviceToDevice, stream));
-    LUMRAD_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(unsigned long long), stream));
+    la->copy_src = d_rad[cur];
+    la->copy_dst = d_rad[1 - cur];
+    la->copy_bytes = (long long)(W * rad_stride);
+    la->clear_stats = d_stats;
     return LUMRAD_OK;
 }
 
@@ -404,6 +407,7 @@ int Context::check_error() {
 int Context::handle_error(int e) {
     if (e != 0) {
         cudaMemsetAsync(d_error, 0, sizeof(int), stream);
+        if (d_pass_mask) cudaMemsetAsync(d_pass_mask, 0, (size_t)world.W * sizeof(uint32_t), stream);
         cudaMemsetAsync(d_queue, 0, kQueueWords * sizeof(unsigned long long), stream);
         cudaMemsetAsync(world.d_probe_count, 0, world.count_cap * sizeof(int), stream);
         cudaStreamSynchronize(stream);
@@ -430,7 +434,7 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
     frame++;
     LaunchArgs la;
     std::memset(&la, 0, sizeof la);
-    int rc = world.prepare_pass(d_reqs, n, p, stream, &la.single);
+    int rc = world.prepare_pass(d_reqs, n, p, stream, &la);
     if (rc) return rc;
     la.worlds = nullptr;
     la.n_worlds = 1;
@@ -445,7 +449,8 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
     last_count_on_device = dev_count != nullptr;
     if (dev_count) {
         if (!d_last_count) LUMRAD_TRY(cudaMalloc(&d_last_count, sizeof(int)));
-        LUMRAD_TRY(cudaMemcpyAsync(d_last_count, dev_count, sizeof(int), cudaMemcpyDeviceToDevice, stream));
+        la.count_src = dev_count;   // copied by the march launch
+        la.count_dst = d_last_count;
         last_size = p.size;
         last_R = p.rays_per_probe;
     }
@@ -491,9 +496,13 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     if (n <= 0) return LUMRAD_OK;
     int rc = world.sync_inputs(stream);
     if (rc) return rc;
+    if (!d_pass_mask) {   // zero between calls (the last finalize of each group clears it)
+        LUMRAD_TRY(cudaMalloc(&d_pass_mask, (size_t)world.W * sizeof(uint32_t)));
+        LUMRAD_TRY(cudaMemsetAsync(d_pass_mask, 0, (size_t)world.W * sizeof(uint32_t), stream));
+    }
     const int slot = (int)(n_passes % kRing);
     LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
-    LUMRAD_TRY(cudaMemsetAsync(world.d_stats, 0, 2 * sizeof(unsigned long long), stream));
+    bool first = true;   // the first launch clears the counters
     const size_t vol_bytes = (size_t)world.W * world.rad_stride;
     uint64_t probes = 0, rays = 0;
     auto aligned_tasks = [&](int i) -> long long {
@@ -507,7 +516,11 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
             LaunchArgs la;
             std::memset(&la, 0, sizeof la);
             if ((rc = world.fill_pass(reqs[i], ns[i], ps[i], stream, &la.single))) return rc;
-            LUMRAD_TRY(cudaMemcpyAsync(la.single.next, la.single.prev, vol_bytes, cudaMemcpyDeviceToDevice, stream));
+            la.copy_src = la.single.prev;   // next starts as a copy of prev: by the march launch
+            la.copy_dst = la.single.next;
+            la.copy_bytes = (long long)vol_bytes;
+            if (first) la.clear_stats = world.d_stats;
+            first = false;
             la.n_worlds = 1;
             la.n_tasks = la.single.n_tasks;
             la.queue = d_queue;
@@ -525,7 +538,7 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
         // the longest run of passes from i whose tasks fit one march launch
         int j = i;
         long long total = 0;
-        while (j < n && aligned_tasks(j) <= kMultiTasks - total) total += aligned_tasks(j++);
+        while (j < n && j - i < kMultiPasses && aligned_tasks(j) <= kMultiTasks - total) total += aligned_tasks(j++);
         const int k = j - i;
         if ((rc = ensure_pass_table(k))) return rc;
         WorldPass* tab = h_ptab[ptab_half];
@@ -565,6 +578,9 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
         la.error = d_error;
         la.ray_res = d_ray_res;
         la.ray_blk = d_ray_blk;
+        la.pass_mask = d_pass_mask;
+        if (first) la.clear_stats = world.d_stats;
+        first = false;
         LUMRAD_TRY(launch_passes(la, tab, k, vol_bytes, world.precision, num_sms, stream));
         i = j;
     }
@@ -668,6 +684,7 @@ void Context::release() {
     cudaFree(d_map_owner);
     if (h_blk) cudaFreeHost(h_blk);
     cudaFree(d_last_count);
+    cudaFree(d_pass_mask);
     cudaFree(d_blk_copies);
     if (h_err) cudaFreeHost(h_err);
     if (ev_req) cudaEventDestroy(ev_req);

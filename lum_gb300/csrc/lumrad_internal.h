@@ -24,6 +24,8 @@ constexpr int kQueueWords = 2;
 // Round size of batches: their task spaces are large, and two rounds of 2^20 tasks (402 MB of ray
 // results, past the L2) beat seven of 2^18 by 2% on 256 mixed worlds (fewer queue drains)
 constexpr int kBatchRoundTasks = 1 << 20;
+// Passes of one march launch over several passes of a context (bits of a pass-mask word)
+constexpr int kMultiPasses = 32;
 // Tasks of one march launch over several passes of a context (their rays, 8 B each, are kept
 // until the passes' finalize launches: 2^19 tasks = 134 MB, about the L2)
 constexpr int kMultiTasks = 1 << 19;
@@ -90,7 +92,24 @@ struct LaunchArgs {
     // and the number of worlds in the table, read by the kernels; null otherwise
     const long long* dev_total;
     const int* dev_n_worlds;
-    // scheduling (0 = the kernel's defaults, 1 and 32): a warp claims remaining / (guided_div *
+    // single-world passes: before marching, the march kernel copies copy_bytes (a multiple of 4) from
+    // copy_src to copy_dst (next starts as a copy of prev: probes not in the list keep their value),
+    // clears the two counters at clear_stats and copies *count_src to *count_dst; null: nothing.
+    // (One launch instead of three copies and a memset before it.)
+    const void* copy_src;
+    void* copy_dst;
+    long long copy_bytes;
+    unsigned long long* clear_stats;
+    const int* count_src;
+    int* count_dst;
+    // several passes of one context (launch_passes): one word per probe, bit i set while pass i of
+    // the launch lists the probe.  The march kernel sets the bits; the finalize kernel of pass
+    // mask_bit copies every probe whose bit is clear from copy_src (prev) to copy_dst (next) in
+    // fin_copy extra CTAs after its fin_ctas task CTAs (no copy launch between the passes), and
+    // with mask_clear (the last pass) zeroes the words for the next launch.  Null: not used.
+    uint32_t* pass_mask;
+    int mask_bit, mask_clear, fin_ctas, fin_copy;
+    // scheduling (0 = the kernel's defaults, 2 and 32): a warp claims remaining / (guided_div *
     // warps) tasks at a time, clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM
     // (capped by occupancy)
     int guided_div, max_chunk, march_ctas;
@@ -121,9 +140,11 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
                             cudaStream_t stream);
 
 // Several passes of one context (table `args.worlds`, pass i's tasks from worlds[i].task_begin,
-// n_tasks <= kMultiTasks in all): one march launch over every pass's tasks; then, pass by pass,
-// its next volume becomes a copy of its prev volume (`vol_bytes`) and the finalize kernel runs
-// over its tasks.  `h_tab` is the host copy of the table.  No hit records.
+// n_tasks <= kMultiTasks in all, n_passes <= kMultiPasses): one march launch over every pass's
+// tasks that also marks each pass's probes in `args.pass_mask` (one zeroed word per probe); then,
+// pass by pass, the finalize kernel over its tasks, whose extra CTAs copy the probes the pass does
+// not list from its prev volume to its next (`vol_bytes` each).  `h_tab` is the host copy of the
+// table.  No hit records.
 cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_passes, size_t vol_bytes,
                           int precision, int num_sms, cudaStream_t stream);
 

@@ -122,7 +122,7 @@ struct DeviceWorld {
     int ensure_dirs(int R, cudaStream_t stream, const float4** out);
     int ensure_scratch(size_t groups, int R);
     int ensure_hits(size_t n);
-    int prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, WorldPass* out);
+    int prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, LaunchArgs* la);
     int fill_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, WorldPass* out);
 };
 
@@ -163,6 +163,9 @@ struct Context {
     bool last_count_on_device = false;
     int* d_last_count = nullptr;
     int last_size = 1, last_R = 0;
+    // several-pass calls: one word per probe, bit i set while pass i of a march launch lists it
+    // (zero between calls)
+    uint32_t* d_pass_mask = nullptr;
 
     // adaptive time slicing state (internal_render.cpp:1190-1203)
     int frame = 0;

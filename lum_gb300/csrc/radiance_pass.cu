@@ -63,12 +63,112 @@ __device__ __forceinline__ bool regular_ray(float ivx, float ivy, float ivz) {
 // rings (227 KB per CTA: a 64x64x16 world of 34 block types fits); other launches (batches,
 // servers, larger worlds, hit records) read the world from global memory through L1.
 constexpr int kStageWarps = 32;
+// Queue defaults (LaunchArgs guided_div / max_chunk = 0): the CTA queue's divisor and the chunk
+// cap; the per-warp queue divides by kWarpQueueDiv
+constexpr int kQueueDiv = 2;
+constexpr int kQueueCap = 32;
+constexpr int kWarpQueueDiv = 1;
+// launches with fewer tasks than this per warp claim through the CTA queue (march_kernel's CTAQ)
+constexpr int kCtaQueueTasksPerWarp = 32;
 constexpr int kRingRays = 2 * kTaskRays;
 constexpr size_t kStageRingBytes = (size_t)kStageWarps * 3 * (kRingRays + kTaskRays) * sizeof(float4);
 
-template <bool RECORD, bool STAGE = false>
+// Tasks are claimed in two levels.  A CTA takes guided blocks from the launch's queue word
+// (remaining / (div * CTAs), clamped to [1, cap * warps per CTA]) into a shared-memory block word
+// (start << 32 | length << 20 | next); its warps take guided chunks of that block (its remainder /
+// (2 * warps per CTA), clamped to [1, cap]) with a shared-memory atomic, and the warp that finds it
+// empty fetches the next block under a shared lock.  The global word sees one claim per CTA block
+// instead of one per warp chunk (same-address atomics serialise), and warps balance at single
+// tasks at the end of a launch.
+struct CtaQueue {
+    unsigned long long blk;
+    int lock, done;
+};
+
+// One claim from the CTA's block: start << 12 | count of a guided chunk (its remainder /
+// (2 * warps per CTA), clamped to [1, cap]), or -2 when the block looked empty or ran out.
+__device__ __forceinline__ long long claim_from_block(int cap, int wpc, CtaQueue* q) {
+    const unsigned long long b = *reinterpret_cast<volatile unsigned long long*>(&q->blk);
+    const int next = (int)(b & 0xFFFFFull), len = (int)((b >> 20) & 0xFFFull);
+    if (next >= len) return -2;
+    const int k = max(1, min(cap, (len - next) / (2 * wpc)));
+    const unsigned long long o = atomicAdd(&q->blk, (unsigned long long)k);
+    const int n2 = (int)(o & 0xFFFFFull), l2 = (int)((o >> 20) & 0xFFFull);
+    return n2 < l2 ? ((long long)(o >> 32) + n2) << 12 | min(k, l2 - n2) : -2;
+}
+
+// The slow path (lane 0 of a warp that found the block empty): fetch the next block under the
+// CTA's lock, or claim from a block another warp fetched meanwhile.  Returns as claim_chunk.  Not
+// inlined: the march loop keeps its registers (a call per block, not per chunk).
+__device__ __noinline__ long long refill_block(unsigned long long* queue, int* error, int n_round, int div, int cap,
+                                               int wpc, int ctas, CtaQueue* q) {
+    for (int it = 0; it < (1 << 22); it++) {
+        const long long c = claim_from_block(cap, wpc, q);
+        if (c != -2) return c;
+        if (*reinterpret_cast<volatile int*>(&q->done)) return -1;
+        if (atomicCAS(&q->lock, 0, 1) == 0) {
+            const unsigned long long b = *reinterpret_cast<volatile unsigned long long*>(&q->blk);
+            if ((b & 0xFFFFFull) < ((b >> 20) & 0xFFFull)) {   // another warp filled it since
+                atomicExch(&q->lock, 0);
+                continue;
+            }
+            const long long rem = (long long)n_round - (long long)*reinterpret_cast<volatile unsigned long long*>(queue);
+            const long long cta_cap = min(4095LL, (long long)cap * wpc);
+            const long long kk = rem / ((long long)div * ctas);
+            const long long k = kk < 1 ? 1 : (kk > cta_cap ? cta_cap : kk);
+            const unsigned long long start = atomicAdd(queue, (unsigned long long)k);
+            if ((long long)start >= (long long)n_round) {
+                *reinterpret_cast<volatile int*>(&q->done) = 1;
+                __threadfence_block();
+                atomicExch(&q->lock, 0);
+                return -1;
+            }
+            const long long len = min(k, (long long)n_round - (long long)start);
+            const long long own = max(1LL, min((long long)cap, len / (2LL * wpc)));
+            atomicExch(&q->blk, (start << 32) | ((unsigned long long)len << 20) | (unsigned long long)own);
+            atomicExch(&q->lock, 0);
+            return ((long long)start << 12) | own;
+        }
+        __nanosleep(64);
+    }
+    atomicOr(error, 1);   // the lock holder never finished (it waits for nothing: cannot happen)
+    return -1;
+}
+
+// Lane 0: the warp's next chunk as start << 12 | count (round-relative), or -1 when none is left.
+__device__ __forceinline__ long long claim_chunk(unsigned long long* queue, int* error, int n_round, int div, int cap,
+                                                 int wpc, int ctas, CtaQueue* q) {
+    const long long c = claim_from_block(cap, wpc, q);
+    return c != -2 ? c : refill_block(queue, error, n_round, div, cap, wpc, ctas, q);
+}
+
+template <bool RECORD, bool STAGE = false, bool CTAQ = false>
 __global__ void __launch_bounds__(STAGE ? kStageWarps * 32 : kWarps * 32, STAGE ? 1 : 4)
 march_kernel(const __grid_constant__ LaunchArgs la) {
+    if (la.copy_dst) {   // the pass's start (see LaunchArgs): the march does not read the volumes
+        const long long stride = (long long)gridDim.x * blockDim.x;
+        const long long n16 = la.copy_bytes >> 4;
+        const uint4* s16 = reinterpret_cast<const uint4*>(la.copy_src);
+        uint4* d16 = reinterpret_cast<uint4*>(la.copy_dst);
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) d16[i] = __ldcs(s16 + i);
+        const long long n4 = la.copy_bytes >> 2;
+        for (long long i = n16 * 4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
+            reinterpret_cast<unsigned*>(la.copy_dst)[i] = reinterpret_cast<const unsigned*>(la.copy_src)[i];
+        if (blockIdx.x == 0 && threadIdx.x < 2 && la.clear_stats) la.clear_stats[threadIdx.x] = 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0 && la.count_dst) *la.count_dst = __ldcg(la.count_src);
+    }
+    if (la.pass_mask) {   // several passes: mark each pass's probes (see LaunchArgs)
+        if (blockIdx.x == 0 && threadIdx.x < 2 && la.clear_stats) la.clear_stats[threadIdx.x] = 0;
+        const long long stride = (long long)gridDim.x * blockDim.x;
+        for (int i = 0; i < la.n_worlds; i++) {
+            const WorldPass& w = la.worlds[i];
+            for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < w.n_groups; g += stride) {
+                const short4 q = __ldg(w.req + (g * w.size + w.shift));
+                if (q.x < 0 || q.y < 0 || q.z < 0 || q.x >= w.X || q.y >= w.Y || q.z >= w.Z) continue;
+                atomicOr(la.pass_mask + (q.x + (long long)w.X * (q.y + (long long)w.Y * q.z)), 1u << i);
+            }
+        }
+    }
     float4 (*s_ray)[3][kRingRays];    // set-up rays: origin, direction, (1/direction, regular)
     float4 (*s_park)[3][kTaskRays];   // in-flight ray state while the warp sets up
     const uint8_t* s_cg = nullptr;
@@ -98,6 +198,13 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         s_park = a_park;
     }
 
+    __shared__ CtaQueue s_q;
+    if (threadIdx.x == 0) {
+        s_q.blk = 0;
+        s_q.lock = 0;
+        s_q.done = 0;
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     float4* so = s_ray[wib][0];
@@ -131,33 +238,43 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
     int steps = 0;
     bool reg = true;             // the lane's ray is regular (see regular_ray)
 
-    // Tasks are claimed in guided chunks: remaining / (div * warps), clamped to [1, cap].  (Claiming
-    // the next chunk ahead of time hides the atomic's latency but holds work back from idle
-    // warps at the end; measured slower.)
+    // Tasks are claimed in two levels.  A CTA takes guided blocks from the launch's queue word
+    // (remaining / (div * CTAs), clamped to [1, cap * warps per CTA]) into a shared-memory block;
+    // its warps take single tasks from that block with a shared-memory atomic, and the warp that
+    // finds it empty fetches the next block under a shared lock.  The global word sees one claim
+    // per CTA block instead of one per warp chunk, and warps balance at single tasks.
+    // Claims: CTAQ, through the CTA's block (claim_chunk; launches with few tasks per warp, such as
+    // a single pass: the warps balance at single tasks); else straight from the launch's queue
+    // word in guided chunks of remaining / (div * warps), clamped to [1, cap] (several passes,
+    // batches: large chunks, few claims).  Two instantiations: the CTA queue's code costs the
+    // other form's march loop registers (2.5% on an 8-pass launch when only branched around).
     auto next_task = [&]() -> int {
         if (pending >= 0) return pending;
         if (tb >= te) {
             if (exhausted) return -1;
-            unsigned long long start = 0, k = 1;
+            long long c = 0;
             if (lane == 0) {
-                const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(la.queue);
-                const long long rem = (long long)n_round - (long long)cur;
-                                // defaults 1 and 32 (against 2 and 16: -0.6% on an 8-pass launch; a divisor of 4
-                // doubles the claims and costs a single pass 20%: the claims contend on one word)
-                const long long div = la.guided_div > 0 ? la.guided_div : 1;
-                const long long cap = la.max_chunk > 0 ? la.max_chunk : 32;
-                const long long kk = rem / (div * la.total_warps);
-                k = (unsigned long long)(kk < 1 ? 1 : (kk > cap ? cap : kk));
-                start = atomicAdd(la.queue, k);
+                const int div = la.guided_div > 0 ? la.guided_div : kQueueDiv;
+                const int cap = la.max_chunk > 0 ? la.max_chunk : kQueueCap;
+                if (CTAQ) {
+                    const int wpc = (int)(blockDim.x >> 5);
+                    c = claim_chunk(la.queue, la.error, n_round, div, cap, wpc, max(1, la.total_warps / wpc), &s_q);
+                } else {
+                    const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(la.queue);
+                    const long long kk = ((long long)n_round - (long long)cur) /
+                                         ((long long)(la.guided_div > 0 ? la.guided_div : kWarpQueueDiv) * la.total_warps);
+                    const long long k = kk < 1 ? 1 : (kk > cap ? cap : kk);
+                    const unsigned long long start = atomicAdd(la.queue, (unsigned long long)k);
+                    c = (long long)start >= (long long)n_round ? -1 : (long long)(start << 12) | min(k, (long long)n_round - (long long)start);
+                }
             }
-            start = __shfl_sync(kFull, start, 0);
-            k = __shfl_sync(kFull, k, 0);
-            if ((long long)start >= (long long)n_round) {
+            c = __shfl_sync(kFull, c, 0);
+            if (c < 0) {
                 exhausted = true;
                 return -1;
             }
-            tb = la.chunk_begin + (int)start;
-            te = la.chunk_begin + (int)min((long long)(start + k), (long long)n_round);
+            tb = la.chunk_begin + (int)(c >> 12);
+            te = tb + (int)(c & 0xFFF);
         }
         return tb;
     };
@@ -444,6 +561,19 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
 template <class Store, bool RECORD, bool IN_CTA, bool PERSIST = false>
 __global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? 6 : 4)
 finalize_kernel(const __grid_constant__ LaunchArgs la) {
+    if (la.pass_mask && (int)blockIdx.x >= la.fin_ctas) {   // copy role (see LaunchArgs)
+        using T = typename Store::T;
+        const T* src = reinterpret_cast<const T*>(la.copy_src);
+        T* dst = reinterpret_cast<T*>(la.copy_dst);
+        const long long n = la.copy_bytes / (long long)sizeof(T);
+        const long long stride = (long long)(gridDim.x - la.fin_ctas) * blockDim.x;
+        for (long long p = (long long)(blockIdx.x - la.fin_ctas) * blockDim.x + threadIdx.x; p < n; p += stride) {
+            const uint32_t m = la.pass_mask[p];
+            if (!((m >> la.mask_bit) & 1u)) dst[p] = __ldcs(src + p);
+            if (la.mask_clear && m) la.pass_mask[p] = 0;
+        }
+        return;
+    }
     __shared__ float4 s_mean[kFinWarps];
     __shared__ int s_count[kFinWarps];
     __shared__ unsigned s_stat[kFinWarps][2];
@@ -483,8 +613,17 @@ size_t stage_bytes(const WorldPass& w) {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
     if (!ready[dev]) {
         int v = 0;
+        cudaFuncAttributes fa{}, fq{};
         if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-            cudaFuncSetAttribute(march_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v) != cudaSuccess)
+            cudaFuncGetAttributes(&fa, march_kernel<false, true>) != cudaSuccess ||
+            cudaFuncGetAttributes(&fq, march_kernel<false, true, true>) != cudaSuccess)
+            v = 0;
+        // the kernels' static shared words (the CTA queue's block in one form)
+        v = std::max(0, v - (int)std::max(fa.sharedSizeBytes, fq.sharedSizeBytes));
+        if (v > 0 && (cudaFuncSetAttribute(march_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v) !=
+                          cudaSuccess ||
+                      cudaFuncSetAttribute(march_kernel<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           v) != cudaSuccess))
             v = 0;
         max_optin[dev] = v;
         ready[dev] = true;
@@ -495,23 +634,30 @@ size_t stage_bytes(const WorldPass& w) {
     return bytes <= (size_t)max_optin[dev] ? bytes : 0;
 }
 
-// The march launch of a round (no hit records): staged when the world fits shared memory.
+// The march launch of a round (no hit records): staged when the world fits shared memory; the
+// CTA queue when the round has few tasks per warp.
 void launch_march(LaunchArgs args, const WorldPass& w, long long round_tasks, int num_sms, cudaStream_t stream) {
     const size_t smem = stage_bytes(w);
     if (smem > 0) {
         const int blocks = (int)std::min<long long>(num_sms, (std::max(round_tasks, 1LL) + kStageWarps - 1) / kStageWarps);
         args.total_warps = blocks * kStageWarps;
-        march_kernel<false, true><<<blocks, kStageWarps * 32, smem, stream>>>(args);
+        if (round_tasks < (long long)kCtaQueueTasksPerWarp * args.total_warps)
+            march_kernel<false, true, true><<<blocks, kStageWarps * 32, smem, stream>>>(args);
+        else
+            march_kernel<false, true><<<blocks, kStageWarps * 32, smem, stream>>>(args);
     } else {
         const int blocks = march_grid(false, num_sms, round_tasks, args.march_ctas);
         args.total_warps = blocks * kWarps;
-        march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(args);
+        if (round_tasks < (long long)kCtaQueueTasksPerWarp * args.total_warps)
+            march_kernel<false, false, true><<<blocks, kWarps * 32, 0, stream>>>(args);
+        else
+            march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(args);
     }
 }
 
 template <class Store, bool RECORD>
 void launch_finalize(const LaunchArgs& args, int n, bool in_cta, cudaStream_t stream) {
-    const int blocks = (n + kFinWarps - 1) / kFinWarps;
+    const int blocks = (n + kFinWarps - 1) / kFinWarps + (args.pass_mask ? args.fin_copy : 0);
     if (in_cta) finalize_kernel<Store, RECORD, true><<<blocks, kFinWarps * 32, 0, stream>>>(args);
     else finalize_kernel<Store, RECORD, false><<<blocks, kFinWarps * 32, 0, stream>>>(args);
 }
@@ -529,6 +675,9 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
         const int n = args.chunk_end - args.chunk_begin;
         if (RECORD) march_kernel<RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
         else launch_march(args, a.single, std::min(a.n_tasks, round), num_sms, stream);
+        args.copy_dst = nullptr;   // the pass's start: in the first round's march only
+        args.clear_stats = nullptr;
+        args.count_dst = nullptr;
         const bool lean = a.force_lean || (a.worlds ? a.in_cta != 0 : combines_in_cta(&a.single, 1));
         launch_finalize<Store, RECORD>(args, n, lean, stream);
     }
@@ -544,16 +693,32 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
     args.chunk_begin = 0;
     args.chunk_end = (int)a.n_tasks;
     args.ray_origin = 0;
-    if (a.n_tasks > 0) launch_march(args, h_tab[0], a.n_tasks, num_sms, stream);
+    if (a.n_tasks > 0) {
+        launch_march(args, h_tab[0], a.n_tasks, num_sms, stream);
+    } else {   // every pass empty: plain copies
+        for (int i = 0; i < n_passes; i++) {
+            cudaError_t e = cudaMemcpyAsync(h_tab[i].next, h_tab[i].prev, vol_bytes, cudaMemcpyDeviceToDevice, stream);
+            if (e != cudaSuccess) return e;
+        }
+        if (a.clear_stats) return cudaMemsetAsync(a.clear_stats, 0, 2 * sizeof(unsigned long long), stream);
+        return cudaSuccess;
+    }
+    args.clear_stats = nullptr;
     const bool in_cta = combines_in_cta(h_tab, n_passes);
+    const long long probes = (long long)(vol_bytes / sizeof(typename Store::T));
+    const int copy_ctas = (int)std::max<long long>(1, std::min<long long>((probes + 1023) / 1024, 2LL * num_sms));
     for (int i = 0; i < n_passes; i++) {
         const WorldPass& w = h_tab[i];
-        cudaError_t e = cudaMemcpyAsync(w.next, w.prev, vol_bytes, cudaMemcpyDeviceToDevice, stream);
-        if (e != cudaSuccess) return e;
-        if (w.n_tasks <= 0) continue;
         args.chunk_begin = (int)w.task_begin;
         args.chunk_end = (int)(w.task_begin + w.n_tasks);
         const int n = args.chunk_end - args.chunk_begin;
+        args.copy_src = w.prev;
+        args.copy_dst = w.next;
+        args.copy_bytes = (long long)vol_bytes;
+        args.mask_bit = i;
+        args.mask_clear = i == n_passes - 1;
+        args.fin_ctas = (n + kFinWarps - 1) / kFinWarps;
+        args.fin_copy = copy_ctas;
         launch_finalize<Store, false>(args, n, in_cta, stream);
     }
     return cudaGetLastError();
@@ -563,7 +728,7 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
 
 cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_passes, size_t vol_bytes,
                           int precision, int num_sms, cudaStream_t stream) {
-    if (args.n_tasks > kMultiTasks) return cudaErrorInvalidValue;
+    if (args.n_tasks > kMultiTasks || n_passes > kMultiPasses || !args.pass_mask) return cudaErrorInvalidValue;
     switch (precision) {
         case LUMRAD_PRECISION_FP16: return passes_t<StoreF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
         case LUMRAD_PRECISION_BF16: return passes_t<StoreBF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
@@ -594,7 +759,16 @@ cudaError_t launch_table_pass(const LaunchArgs& a, int precision, int num_sms, c
 }
 
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream) {
-    if (args.n_tasks <= 0) return cudaSuccess;
+    if (args.n_tasks <= 0) {   // no march launch: the pass's start as copies
+        cudaError_t e = cudaSuccess;
+        if (args.copy_dst && args.copy_bytes > 0)
+            e = cudaMemcpyAsync(args.copy_dst, args.copy_src, (size_t)args.copy_bytes, cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess && args.clear_stats)
+            e = cudaMemsetAsync(args.clear_stats, 0, 2 * sizeof(unsigned long long), stream);
+        if (e == cudaSuccess && args.count_dst)
+            e = cudaMemcpyAsync(args.count_dst, args.count_src, sizeof(int), cudaMemcpyDeviceToDevice, stream);
+        return e;
+    }
     switch (precision) {
         case LUMRAD_PRECISION_FP16:
             return record ? launch_t<StoreF16, true>(args, num_sms, stream) : launch_t<StoreF16, false>(args, num_sms, stream);
@@ -875,7 +1049,8 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
         la.chunk_end = (int)std::min(c0 + (long long)kNoAllocRoundTasks, n_tasks);
         la.ray_origin = la.chunk_begin;
         const int tasks = la.chunk_end - la.chunk_begin;
-        march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(la);
+        if (tasks < kCtaQueueTasksPerWarp * la.total_warps) march_kernel<false, false, true><<<blocks, kWarps * 32, 0, stream>>>(la);
+        else march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(la);
         finalize_kernel<StoreF32, false, true><<<(tasks + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, stream>>>(la);
     }
     LUMRAD_TRY(cudaGetLastError());

@@ -154,3 +154,38 @@ def test_page_locked_lists():
             out.append(rw.get_radiance())
     for o in out[1:]:
         assert o.tobytes() == out[0].tobytes()
+
+
+def test_more_passes_than_one_launch_marks():
+    """40 passes in one call: the marches share launches of at most 32 passes (one mark bit per
+    pass and probe), so the call spans two; lists hold entries outside the world (skipped, as the
+    single pass skips them) and repeat probes across passes.  Equal to single passes, bit for bit,
+    and a second call (the marks cleared by the first) equal again."""
+    w = worldgen.terrain_world((8, 7, 5), seed=52, n_types=10)
+    rng = np.random.default_rng(53)
+    lists = []
+    for i in range(40):
+        l = worldgen.probe_subset(w.dims, 0.05 + 0.02 * (i % 7), seed=54, stream=i)
+        bad = np.array([[-1, 0, 0, 0], [w.dims[0], 1, 1, 0], [2, w.dims[1], 0, 0], [0, 0, -3, 0]], np.int16)
+        l = np.concatenate([l, bad[rng.permutation(4)[: i % 3]]])
+        lists.append(np.ascontiguousarray(l[rng.permutation(l.shape[0])]))
+    spec = [dict(rays=(32, 64, 128)[i % 3], max_dist=64.0, blend=0.15, time_seed=100 + i) for i in range(40)]
+    prev = random_prev(w, seed=55)
+    single, st_single = _run(w, lists, spec, prev, "single")
+    got, st = _run(w, lists, spec, prev, "resident")
+    assert got.tobytes() == single.tobytes()
+    assert st == st_single
+    import lum_gb300
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        rw.set_radiance(prev)
+        params = [lum_gb300.pass_params(**s) for s in spec]
+        rw.radiance_passes(lists, params)
+        rw.radiance_passes(lists[:5], params[:5])
+        twice = rw.get_radiance()
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        rw.set_radiance(prev)
+        for l, s in zip(lists + lists[:5], spec + spec[:5]):
+            rw.radiance_pass(l, lum_gb300.pass_params(**s))
+        assert twice.tobytes() == rw.get_radiance().tobytes()
