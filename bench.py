@@ -57,15 +57,15 @@ SEED = 1234
 S_R = 12            # bytes of FP32 RGB radiance per probe
 BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
-# finalize launches) in an ncu capture of this workload; ncu replays with cold caches
-# (march 1.04 + 46.23 MB, finalizes 118.23 + 0.00 MB)
-NCU_DRAM_BYTES_PER_STEP = 165.50e6
-# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 493.6 MB: its world
-# lookups are shared-memory loads, finalizes 986.7 MB)
-NCU_L2_BYTES_PER_STEP = 1480.3e6
+# finalize launches, whose extra CTAs copy each pass's unlisted probes) in an ncu capture of this
+# workload; ncu replays with cold caches (march 1.79 + 46.73 MB, finalizes 120.36 + 0.00 MB)
+NCU_DRAM_BYTES_PER_STEP = 168.88e6
+# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 498.7 MB: its world
+# lookups are shared-memory loads, finalizes 1,013.3 MB)
+NCU_L2_BYTES_PER_STEP = 1512.0e6
 # Warp instructions (smsp__inst_executed.sum) of the same 9 launches: the march over the 8 passes
-# (463.0 M) and the 8 finalize launches (406.7 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 463.0e6 + 406.7e6
+# (461.7 M) and the 8 finalize launches (409.9 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 461.7e6 + 409.9e6
 SCHEDULERS_PER_SM = 4
 
 
