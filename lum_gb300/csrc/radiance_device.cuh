@@ -26,6 +26,12 @@ __device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; 
 __device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
 // float -> int toward zero; PTX cvt.rzi saturates and maps NaN to 0.
 __device__ __forceinline__ int f2i(float f) { return __float2int_rz(f); }
+
+// Programmatic dependent launch: a kernel launched as a dependent of the stream's previous one
+// starts once every CTA of that one has called grid_launch_dependents, and grid_dependency_wait
+// returns when that kernel has finished and its writes are visible (at once for a plain launch).
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 // SPIR-V OpSMod for a positive divisor.
 __device__ __forceinline__ int smod(int a, int b) {
     int r = a % b;
@@ -275,14 +281,19 @@ __device__ __forceinline__ float3 sample_trilinear(const WorldPass& w, float ux,
 
 // info word of a marched ray: bits 0-15 coarse steps, 16-23 coarse voxel (records only),
 // 24 hit, 25 stopped by the step bound.
-template <class Store, bool RECORD>
-__device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchView& mv, float3 o, float3 d,
-                                               float coarse_frac, uint32_t info, int block, long long gr,
-                                               uint32_t& lookups) {
+//
+// A marched ray's shading in two parts: finalize_ray (refine, material, hit point; the sky for a
+// miss) reads no radiance volume; shade_hit (the trilinear taps of the previous volume) does.  A
+// pass's finalize launch may run the first part while the previous pass still writes the volume.
+// Returns whether the ray hit; a miss's light is in `light`, a hit's tap coordinates in u and its
+// material in m.
+template <bool RECORD>
+__device__ __forceinline__ bool finalize_ray(const WorldPass& w, const MarchView& mv, float3 o, float3 d,
+                                             float coarse_frac, uint32_t info, int block, long long gr,
+                                             uint32_t& lookups, float3& light, float3& u, float4& m) {
     const bool hit = (info >> 24) & 1u;
     const int coarse_steps = info & 0xffff;
     lookups = coarse_steps;
-    float3 light;
     LumRadHit rec;
     if (RECORD) {
         rec.voxel[0] = rec.voxel[1] = rec.voxel[2] = 0;
@@ -342,19 +353,15 @@ __device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchVi
         const float nx = -fmul((float)stx, fsx), ny = -fmul((float)sty, fsy), nz = -fmul((float)stz, fsz);
         const float fr = fadd(fadd(fmul(fsub(tmx, tdx), fsx), fmul(fsub(tmy, tdy), fsy)), fmul(fsub(tmz, tdz), fsz));
         // material (GetMat :145-157) and sample_radiance (:161-166); /16 == *0.0625 exactly
-        const float4 m = __ldg(w.mats + cur);
+        m = __ldg(w.mats + cur);
         const float hx = fadd(o.x, fmul(fr, d.x));
         const float hy = fadd(o.y, fmul(fr, d.y));
         const float hz = fadd(o.z, fmul(fr, d.z));
         const float bpx = fmul(fadd(hx, fmul(nx, 16.0f)), 0.0625f);
         const float bpy = fmul(fadd(hy, fmul(ny, 16.0f)), 0.0625f);
         const float bpz = fmul(fadd(hz, fmul(nz, 16.0f)), 0.0625f);
-        const float3 L = sample_trilinear<Store>(w, fdiv_by(fadd(bpx, 0.5f), (float)w.X, w.inv_dim[0]),
-                                                 fdiv_by(fadd(bpy, 0.5f), (float)w.Y, w.inv_dim[1]),
-                                                 fdiv_by(fadd(bpz, 0.5f), (float)w.Z, w.inv_dim[2]));
-        light = make_float3(fadd(0.0f, fadd(fmul(L.x, m.x), fmul(m.x, m.w))),
-                            fadd(0.0f, fadd(fmul(L.y, m.y), fmul(m.y, m.w))),
-                            fadd(0.0f, fadd(fmul(L.z, m.z), fmul(m.z, m.w))));
+        u = make_float3(fdiv_by(fadd(bpx, 0.5f), (float)w.X, w.inv_dim[0]), fdiv_by(fadd(bpy, 0.5f), (float)w.Y, w.inv_dim[1]),
+                        fdiv_by(fadd(bpz, 0.5f), (float)w.Z, w.inv_dim[2]));
         if (RECORD) {
             rec.voxel[0] = vx; rec.voxel[1] = vy; rec.voxel[2] = vz;
             rec.voxel_id = (uint8_t)cur;
@@ -382,7 +389,16 @@ __device__ __forceinline__ float3 finalize_ray(const WorldPass& w, const MarchVi
         light.z = fadd(light.z, __uint_as_float(kSkyB));
     }
     if (RECORD) w.hits[gr] = rec;
-    return light;
+    return hit;
+}
+
+// The hit's light (radiance.comp:331-333): the previous volume's trilinear sample at u
+// (sample_radiance :161-166) times the material colour, plus colour times emission.
+template <class Store>
+__device__ __forceinline__ float3 shade_hit(const WorldPass& w, float3 u, float4 m) {
+    const float3 L = sample_trilinear<Store>(w, u.x, u.y, u.z);
+    return make_float3(fadd(0.0f, fadd(fmul(L.x, m.x), fmul(m.x, m.w))), fadd(0.0f, fadd(fmul(L.y, m.y), fmul(m.y, m.w))),
+                       fadd(0.0f, fadd(fmul(L.z, m.z), fmul(m.z, m.w))));
 }
 
 __device__ __forceinline__ float3 butterfly_sum(float3 v) {

@@ -504,8 +504,12 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
         float3 o, d;
         setup_ray(*wp, g, k * kTaskRays + lane, o, d);   // bit-identical to the march's set-up
         uint32_t lookups;
-        float3 L = finalize_ray<Store, RECORD>(*wp, march_view(*wp), o, d, __uint_as_float(res.x), res.y, blk,
-                                               (long long)t_local * kTaskRays + lane, lookups);
+        float3 L, u;
+        float4 m;
+        const bool hit = finalize_ray<RECORD>(*wp, march_view(*wp), o, d, __uint_as_float(res.x), res.y, blk,
+                                              (long long)t_local * kTaskRays + lane, lookups, L, u, m);
+        grid_dependency_wait();   // from here on the volumes: the previous pass's launch has finished
+        if (hit) L = shade_hit<Store>(*wp, u, m);
         L = butterfly_sum(L);
         v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
         // counters: lookups and hits of this task, summed per CTA below
@@ -561,7 +565,9 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
 template <class Store, bool RECORD, bool IN_CTA, bool PERSIST = false>
 __global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? 6 : 4)
 finalize_kernel(const __grid_constant__ LaunchArgs la) {
+    grid_launch_dependents();   // the next pass's launch may start its volume-free part
     if (la.pass_mask && (int)blockIdx.x >= la.fin_ctas) {   // copy role (see LaunchArgs)
+        grid_dependency_wait();
         using T = typename Store::T;
         const T* src = reinterpret_cast<const T*>(la.copy_src);
         T* dst = reinterpret_cast<T*>(la.copy_dst);
@@ -655,11 +661,29 @@ void launch_march(LaunchArgs args, const WorldPass& w, long long round_tasks, in
     }
 }
 
+// overlap: launched as a programmatic dependent of the stream's previous kernel (a finalize launch
+// of the previous pass), whose CTAs let it start early (griddepcontrol.launch_dependents); its
+// volume reads and writes wait for that kernel's end (griddepcontrol.wait).
 template <class Store, bool RECORD>
-void launch_finalize(const LaunchArgs& args, int n, bool in_cta, cudaStream_t stream) {
+void launch_finalize(const LaunchArgs& args, int n, bool in_cta, cudaStream_t stream, bool overlap = false) {
     const int blocks = (n + kFinWarps - 1) / kFinWarps + (args.pass_mask ? args.fin_copy : 0);
-    if (in_cta) finalize_kernel<Store, RECORD, true><<<blocks, kFinWarps * 32, 0, stream>>>(args);
-    else finalize_kernel<Store, RECORD, false><<<blocks, kFinWarps * 32, 0, stream>>>(args);
+    if (blocks <= 0) return;
+    auto kern = in_cta ? finalize_kernel<Store, RECORD, true> : finalize_kernel<Store, RECORD, false>;
+    if (!overlap) {
+        kern<<<blocks, kFinWarps * 32, 0, stream>>>(args);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kFinWarps * 32);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args);
 }
 
 template <class Store, bool RECORD>
@@ -719,7 +743,9 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
         args.mask_clear = i == n_passes - 1;
         args.fin_ctas = (n + kFinWarps - 1) / kFinWarps;
         args.fin_copy = copy_ctas;
-        launch_finalize<Store, false>(args, n, in_cta, stream);
+        // from the second pass on, the launch overlaps the previous pass's tail: its refine and
+        // materials read no volume (the first pass's rays come from the march launch before it)
+        launch_finalize<Store, false>(args, n, in_cta, stream, i > 0);
     }
     return cudaGetLastError();
 }
