@@ -119,7 +119,7 @@ typedef struct {
     uint64_t rays;          /* rays traced */
     uint64_t steps;         /* grid+palette lookups: coarse steps + refine lookups */
     uint64_t hits;          /* rays that hit a voxel */
-    float    gpu_ms;        /* device time of the pass kernel (CUDA events) */
+    float    gpu_ms;        /* device time of the pass's kernels (timestamps they write) */
 } LumRadPassStats;
 
 /* ---- context lifetime (lum_create_instance / lum_init / lum_destroy_instance) ------------- */
@@ -223,8 +223,11 @@ int  lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out);
 /* The CUDA stream (cudaStream_t) every call of this context enqueues on, for callers that
  * order their own work or time passes with their own events on it. */
 int  lumrad_get_stream(LumRadContext ctx, void** stream);
-/* Device times (ms, CUDA events around the pass kernel) of the last min(cap, 64) passes,
- * oldest first; *n = number written.  Synchronises. */
+/* Device times (ms) of the last min(cap, 64) passes, oldest first; *n = number written.  Each is
+ * the span from the start of the pass's first kernel to the end of its last, from %globaltimer
+ * timestamps those kernels write (0 for a pass without kernels).  A pass call that follows another
+ * pass call on the context (no other call between them, no upload) starts its march while the
+ * previous pass's last kernel finishes, so consecutive spans may overlap.  Synchronises. */
 int  lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n);
 
 /* ---- producers: voxel models blockified into the world (blockify + map) ---------------------

@@ -198,6 +198,7 @@ int DeviceWorld::sync_inputs(cudaStream_t stream) {
         h_cur.clear();
         grid_dirty = true;
     }
+    if (grid_dirty || compact_dirty) uploads++;
     if (grid_dirty) {
         LUMRAD_TRY(cudaMemcpyAsync(d_grid, h_grid.data(), W * sizeof(int16_t), cudaMemcpyHostToDevice, stream));
         grid_dirty = false;
@@ -239,6 +240,7 @@ int DeviceWorld::ensure_dirs(int R, cudaStream_t stream, const float4** out) {
     std::vector<float4> t(R);
     for (int i = 0; i < R; i++) t[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
     float4* d = nullptr;
+    uploads++;
     LUMRAD_TRY(cudaMalloc(&d, sizeof(float4) * R));
     LUMRAD_TRY(cudaMemcpyAsync(d, t.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, stream));
     LUMRAD_TRY(cudaStreamSynchronize(stream));
@@ -254,6 +256,7 @@ int DeviceWorld::ensure_scratch(size_t groups, int R) {
         d_scratch = nullptr;
         scratch_cap = 0;
         const size_t cap = std::max<size_t>(groups * nsub, 1024);
+        uploads++;
         LUMRAD_TRY(cudaMalloc(&d_scratch, cap * sizeof(float4)));
         scratch_cap = cap;
     }
@@ -262,6 +265,7 @@ int DeviceWorld::ensure_scratch(size_t groups, int R) {
         d_probe_count = nullptr;
         count_cap = 0;
         const size_t cap = std::max<size_t>(groups, 1024);
+        uploads++;
         LUMRAD_TRY(cudaMalloc(&d_probe_count, cap * sizeof(int)));
         LUMRAD_TRY(cudaMemset(d_probe_count, 0, cap * sizeof(int)));
         count_cap = cap;
@@ -364,11 +368,14 @@ int Context::ensure_rays(long long n_tasks, long long cap_tasks) {
     if (need <= ray_cap) return LUMRAD_OK;
     LUMRAD_TRY(cudaStreamSynchronize(stream));
     cudaFree(d_ray_res);
+    cudaFree(d_ray_res2);
     cudaFree(d_ray_blk);
-    d_ray_res = nullptr;
+    d_ray_res = d_ray_res2 = nullptr;
     d_ray_blk = nullptr;
     ray_cap = 0;
+    pass_mark = -1;   // the buffers are new: no launch overlaps the synchronised one
     LUMRAD_TRY(cudaMalloc(&d_ray_res, need * sizeof(uint2)));
+    LUMRAD_TRY(cudaMalloc(&d_ray_res2, need * sizeof(uint2)));
     LUMRAD_TRY(cudaMalloc(&d_ray_blk, need * sizeof(int)));
     ray_cap = need;
     return LUMRAD_OK;
@@ -391,6 +398,7 @@ int Context::stage_requests(const int16_t* req, size_t n) {
         h_req_cap = cap;
     }
     std::memcpy(h_req_pinned, req, n * 4 * sizeof(int16_t));
+    world.uploads++;
     LUMRAD_TRY(cudaMemcpyAsync(d_req, h_req_pinned, n * sizeof(short4), cudaMemcpyHostToDevice, stream));
     LUMRAD_TRY(cudaEventRecord(ev_req, stream));
     req_copy_pending = true;
@@ -408,6 +416,7 @@ int Context::handle_error(int e) {
     if (e != 0) {
         cudaMemsetAsync(d_error, 0, sizeof(int), stream);
         if (d_pass_mask) cudaMemsetAsync(d_pass_mask, 0, (size_t)world.W * sizeof(uint32_t), stream);
+        if (d_pass_mask2) cudaMemsetAsync(d_pass_mask2, 0, (size_t)world.W * sizeof(uint32_t), stream);
         cudaMemsetAsync(d_queue, 0, kQueueWords * sizeof(unsigned long long), stream);
         cudaMemsetAsync(world.d_probe_count, 0, world.count_cap * sizeof(int), stream);
         cudaStreamSynchronize(stream);
@@ -442,7 +451,11 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
     la.queue = d_queue;
     la.error = d_error;
     if ((rc = ensure_rays(la.n_tasks))) return rc;
-    la.ray_res = d_ray_res;
+    // the march may start in the previous pass's finalize tail: see pass_mark (the list must not
+    // come from a kernel, the hits use the one record buffer)
+    const bool dependent = !p.record_hits && !dev_count && pass_mark == api_calls - 1 && uploads_mark == world.uploads;
+    la.ray_res = ray_side ? d_ray_res2 : d_ray_res;
+    ray_side ^= 1;
     la.ray_blk = d_ray_blk;
     la.dev_count = dev_count;
     la.force_lean = test_lean_finalize ? 1 : 0;
@@ -455,9 +468,11 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
         last_R = p.rays_per_probe;
     }
     const int slot = (int)(n_passes % kRing);
-    LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
-    LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream));
-    LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
+    la.time_start = la.time_end = d_ptime + 2 * slot;
+    timed[slot] = la.n_tasks > 0;
+    LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream, dependent));
+    pass_mark = p.record_hits ? -1 : api_calls;
+    uploads_mark = world.uploads;
     last_slot = slot;
     last_slot_passes = 1;
     n_passes++;
@@ -466,6 +481,17 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
     last.probes = (uint64_t)la.single.n_groups;
     last.rays = (uint64_t)la.single.n_groups * la.single.R;
     return LUMRAD_OK;
+}
+
+int Context::read_times() {
+    LUMRAD_TRY(cudaMemcpyAsync(h_ptime, d_ptime, 2 * kRing * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+    LUMRAD_TRY(cudaStreamSynchronize(stream));
+    return LUMRAD_OK;
+}
+
+float Context::slot_ms(int slot) const {
+    const unsigned long long t0 = h_ptime[2 * slot], t1 = h_ptime[2 * slot + 1];
+    return timed[slot] && t1 > t0 ? (float)((double)(t1 - t0) * 1e-6) : 0.0f;
 }
 
 int Context::ensure_pass_table(int n) {
@@ -496,13 +522,19 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     if (n <= 0) return LUMRAD_OK;
     int rc = world.sync_inputs(stream);
     if (rc) return rc;
-    if (!d_pass_mask) {   // zero between calls (the last finalize of each group clears it)
+    if (!d_pass_mask) {   // zero between calls (the last finalize of each group clears its mask)
         LUMRAD_TRY(cudaMalloc(&d_pass_mask, (size_t)world.W * sizeof(uint32_t)));
+        LUMRAD_TRY(cudaMalloc(&d_pass_mask2, (size_t)world.W * sizeof(uint32_t)));
         LUMRAD_TRY(cudaMemsetAsync(d_pass_mask, 0, (size_t)world.W * sizeof(uint32_t), stream));
+        LUMRAD_TRY(cudaMemsetAsync(d_pass_mask2, 0, (size_t)world.W * sizeof(uint32_t), stream));
     }
     const int slot = (int)(n_passes % kRing);
-    LUMRAD_TRY(cudaEventRecord(ring0[slot], stream));
-    bool first = true;   // the first launch clears the counters
+    timed[slot] = false;
+    bool first = true;   // the first launch clears the counters and starts the kernel time
+    // the first march may start in the previous pass's finalize tail: see pass_mark
+    bool dependent = pass_mark == api_calls - 1 && uploads_mark == world.uploads;
+    const int side = ray_side;   // this call's ray buffer (the previous pass's finalize reads the other)
+    ray_side ^= 1;
     const size_t vol_bytes = (size_t)world.W * world.rad_stride;
     uint64_t probes = 0, rays = 0;
     auto aligned_tasks = [&](int i) -> long long {
@@ -520,15 +552,19 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
             la.copy_dst = la.single.next;
             la.copy_bytes = (long long)vol_bytes;
             if (first) la.clear_stats = world.d_stats;
+            if (first) la.time_start = d_ptime + 2 * slot;
+            la.time_end = d_ptime + 2 * slot;
+            timed[slot] = timed[slot] || la.n_tasks > 0;
             first = false;
             la.n_worlds = 1;
             la.n_tasks = la.single.n_tasks;
             la.queue = d_queue;
             la.error = d_error;
             if ((rc = ensure_rays(la.n_tasks))) return rc;
-            la.ray_res = d_ray_res;
+            la.ray_res = side ? d_ray_res2 : d_ray_res;
             la.ray_blk = d_ray_blk;
-            LUMRAD_TRY(launch_radiance(la, world.precision, false, num_sms, stream));
+            LUMRAD_TRY(launch_radiance(la, world.precision, false, num_sms, stream, dependent));
+            dependent = false;
             probes += (uint64_t)la.single.n_groups;
             rays += (uint64_t)la.single.n_groups * la.single.R;
             world.cur = 1 - world.cur;
@@ -576,15 +612,20 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
         la.n_tasks = total;
         la.queue = d_queue;
         la.error = d_error;
-        la.ray_res = d_ray_res;
+        la.ray_res = side ? d_ray_res2 : d_ray_res;
         la.ray_blk = d_ray_blk;
-        la.pass_mask = d_pass_mask;
+        la.pass_mask = side ? d_pass_mask2 : d_pass_mask;
         if (first) la.clear_stats = world.d_stats;
+        if (first) la.time_start = d_ptime + 2 * slot;
+        la.time_end = d_ptime + 2 * slot;
+        timed[slot] = timed[slot] || total > 0;
         first = false;
-        LUMRAD_TRY(launch_passes(la, tab, k, vol_bytes, world.precision, num_sms, stream));
+        LUMRAD_TRY(launch_passes(la, tab, k, vol_bytes, world.precision, num_sms, stream, dependent));
+        dependent = false;
         i = j;
     }
-    LUMRAD_TRY(cudaEventRecord(ring1[slot], stream));
+    pass_mark = api_calls;
+    uploads_mark = world.uploads;
     last_slot = slot;
     last_slot_passes = n;
     n_passes++;
@@ -659,6 +700,7 @@ void Context::release() {
     cudaFree(d_queue);
     cudaFree(d_error);
     cudaFree(d_ray_res);
+    cudaFree(d_ray_res2);
     cudaFree(d_ray_blk);
     for (int h = 0; h < 2; h++) {
         if (h_ptab[h]) cudaFreeHost(h_ptab[h]);
@@ -685,17 +727,20 @@ void Context::release() {
     if (h_blk) cudaFreeHost(h_blk);
     cudaFree(d_last_count);
     cudaFree(d_pass_mask);
+    cudaFree(d_pass_mask2);
     cudaFree(d_blk_copies);
     if (h_err) cudaFreeHost(h_err);
     if (ev_req) cudaEventDestroy(ev_req);
-    for (int i = 0; i < kRing; i++) {
-        if (ring0[i]) cudaEventDestroy(ring0[i]);
-        if (ring1[i]) cudaEventDestroy(ring1[i]);
-    }
+    cudaFree(d_ptime);
+    if (h_ptime) cudaFreeHost(h_ptime);
     if (stream) cudaStreamDestroy(stream);
 }
 
-Context* as_ctx(LumRadContext c) { return reinterpret_cast<Context*>(c); }
+Context* as_ctx(LumRadContext c) {
+    Context* x = reinterpret_cast<Context*>(c);
+    if (x) x->api_calls++;
+    return x;
+}
 
 int check_unowned(const Context* c) {
     return c->owner ? fail(LUMRAD_ESTATE, "the context belongs to a server; use the server's calls") : LUMRAD_OK;
@@ -745,10 +790,9 @@ int lumrad_create(const LumRadSettings* s, LumRadContext* out) {
         LUMRAD_TRY(cudaMallocHost(&c->h_err, sizeof(int)));
         *c->h_err = 0;
         LUMRAD_TRY(cudaEventCreateWithFlags(&c->ev_req, cudaEventDisableTiming));
-        for (int i = 0; i < Context::kRing; i++) {
-            LUMRAD_TRY(cudaEventCreate(&c->ring0[i]));
-            LUMRAD_TRY(cudaEventCreate(&c->ring1[i]));
-        }
+        LUMRAD_TRY(cudaMalloc(&c->d_ptime, 2 * Context::kRing * sizeof(unsigned long long)));
+        LUMRAD_TRY(cudaMallocHost(&c->h_ptime, 2 * Context::kRing * sizeof(unsigned long long)));
+        LUMRAD_TRY(cudaMemsetAsync(c->d_ptime, 0, 2 * Context::kRing * sizeof(unsigned long long), c->stream));
         LUMRAD_TRY(cudaMalloc(&c->d_queue, kQueueWords * sizeof(unsigned long long)));
         LUMRAD_TRY(cudaMalloc(&c->d_error, sizeof(int)));
         LUMRAD_TRY(cudaMemsetAsync(c->d_queue, 0, kQueueWords * sizeof(unsigned long long), c->stream));
@@ -1003,8 +1047,8 @@ int lumrad_update_radiance(LumRadContext ctx, const LumRadPassParams* params) {
         if (c->test_pass_ms >= 0.0f) {
             c->last_ms = c->test_pass_ms;
         } else {
-            LUMRAD_TRY(cudaEventSynchronize(c->ring1[c->last_slot]));
-            LUMRAD_TRY(cudaEventElapsedTime(&c->last_ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
+            if ((rc = c->read_times())) return rc;
+            c->last_ms = c->slot_ms(c->last_slot);
             c->last_ms /= (float)c->last_slot_passes;   // a frame's pass time after a several-pass call
         }
     }
@@ -1269,8 +1313,8 @@ int lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out) {
     if (c->last_count_on_device)
         LUMRAD_TRY(cudaMemcpyAsync(&count, c->d_last_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     LUMRAD_TRY(cudaStreamSynchronize(c->stream));
-    float ms = 0.0f;
-    LUMRAD_TRY(cudaEventElapsedTime(&ms, c->ring0[c->last_slot], c->ring1[c->last_slot]));
+    if (int rc = c->read_times()) return rc;
+    const float ms = c->slot_ms(c->last_slot);
     *out = c->last;
     if (c->last_count_on_device) {
         out->probes = (uint64_t)(count / c->last_size);
@@ -1303,13 +1347,12 @@ int lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n) {
     Context* c = as_ctx(ctx);
     if (!c || !n || (cap > 0 && !ms)) return fail(LUMRAD_EINVAL, "null argument");
     LUMRAD_TRY(cudaSetDevice(c->device));
-    LUMRAD_TRY(cudaStreamSynchronize(c->stream));
+    if (int rc = c->read_times()) return rc;
     const long long avail = std::min<long long>(c->n_passes, Context::kRing);
     const int k = (int)std::min<long long>(avail, std::max(cap, 0));
     for (int i = 0; i < k; i++) {
         const long long pass = c->n_passes - k + i;
-        const int slot = (int)(pass % Context::kRing);
-        LUMRAD_TRY(cudaEventElapsedTime(&ms[i], c->ring0[slot], c->ring1[slot]));
+        ms[i] = c->slot_ms((int)(pass % Context::kRing));
     }
     *n = k;
     return c->check_error();

@@ -92,10 +92,11 @@ struct LaunchArgs {
     // and the number of worlds in the table, read by the kernels; null otherwise
     const long long* dev_total;
     const int* dev_n_worlds;
-    // single-world passes: before marching, the march kernel copies copy_bytes (a multiple of 4) from
+    // single-world passes: after marching, the march kernel copies copy_bytes (a multiple of 4) from
     // copy_src to copy_dst (next starts as a copy of prev: probes not in the list keep their value),
     // clears the two counters at clear_stats and copies *count_src to *count_dst; null: nothing.
-    // (One launch instead of three copies and a memset before it.)
+    // (One launch instead of three copies and a memset before it; after the marching, so that a
+    // march launched in the previous pass's finalize tail touches them only once that has ended.)
     const void* copy_src;
     void* copy_dst;
     long long copy_bytes;
@@ -103,12 +104,18 @@ struct LaunchArgs {
     const int* count_src;
     int* count_dst;
     // several passes of one context (launch_passes): one word per probe, bit i set while pass i of
-    // the launch lists the probe.  The march kernel sets the bits; the finalize kernel of pass
+    // the launch lists the probe.  The march kernel sets the bits (after marching); the finalize kernel of pass
     // mask_bit copies every probe whose bit is clear from copy_src (prev) to copy_dst (next) in
     // fin_copy extra CTAs after its fin_ctas task CTAs (no copy launch between the passes), and
     // with mask_clear (the last pass) zeroes the words for the next launch.  Null: not used.
     uint32_t* pass_mask;
     int mask_bit, mask_clear, fin_ctas, fin_copy;
+    // the kernel time of a pass (or several-pass call) as two %globaltimer words: the march launch
+    // that starts it writes [0] = its start and [1] = 0, each finalize CTA raises [1] to its end;
+    // null: not timed.  (Timestamps written by the kernels, not events between the launches, which
+    // would keep the next pass's march from starting in the previous finalize's tail.)
+    unsigned long long* time_start;
+    unsigned long long* time_end;
     // scheduling (0 = the kernel's defaults, 2 and 32): a warp claims remaining / (guided_div *
     // warps) tasks at a time, clamped to [1, max_chunk]; the march grid has march_ctas CTAs per SM
     // (capped by occupancy)
@@ -136,8 +143,11 @@ struct Tuning {
 // Runs one pass over the worlds of `args` (descriptors already on the device when n_worlds > 1)
 // on `stream`: for each round of up to kChunkTasks tasks, the march kernel then the finalize
 // kernel.  Returns a CUDA error code.
+// dependent: the stream's previous kernel is the previous pass's finalize launch and this pass's
+// rays go to the other ray buffer; the first march launch then starts in that launch's tail (its
+// pass-start work waits for it to end).  No hit records.
 cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms,
-                            cudaStream_t stream);
+                            cudaStream_t stream, bool dependent = false);
 
 // Several passes of one context (table `args.worlds`, pass i's tasks from worlds[i].task_begin,
 // n_tasks <= kMultiTasks in all, n_passes <= kMultiPasses): one march launch over every pass's
@@ -146,7 +156,7 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
 // not list from its prev volume to its next (`vol_bytes` each).  `h_tab` is the host copy of the
 // table.  No hit records.
 cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_passes, size_t vol_bytes,
-                          int precision, int num_sms, cudaStream_t stream);
+                          int precision, int num_sms, cudaStream_t stream, bool dependent = false);
 
 // Start of a multi-world pass: copies every world's prev volume into its next volume and clears
 // its counters (descriptors already on the device).

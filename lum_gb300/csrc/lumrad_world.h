@@ -77,6 +77,7 @@ struct DeviceWorld {
 
     int16_t* d_grid = nullptr;
     void* d_cgrid = nullptr;
+    long long uploads = 0;                // stream operations that changed inputs of a pass (copies)
     uint32_t* d_cbits = nullptr;
     int* d_cslot = nullptr;               // cbits_cap entries
     size_t cbits_cap = 0;
@@ -145,12 +146,28 @@ struct Context {
     // rays of one march/finalize round (up to kChunkTasks * 32 rays), or of one march launch over
     // several passes (up to kMultiTasks * 32)
     uint2* d_ray_res = nullptr;
+    uint2* d_ray_res2 = nullptr;           // the other ray buffer (consecutive passes alternate)
     int* d_ray_blk = nullptr;
     size_t ray_cap = 0;
+    int ray_side = 0;
+    // a pass call's first march may start in the previous pass's finalize tail (a programmatic
+    // dependent launch) when the call right before it on this context was a pass call whose last
+    // launch is that finalize: api_calls counts entry points, pass_mark is api_calls after a pass
+    // call's launches (-1 after one with hit records), and no upload happened since (world.uploads)
+    long long api_calls = 0;
+    long long pass_mark = -1;
+    long long uploads_mark = -1;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_req = nullptr;
-    cudaEvent_t ring0[kRing] = {}, ring1[kRing] = {};   // around each pass's kernels
+    // each pass's (or several-pass call's) kernel time: start and end %globaltimer words written by
+    // its kernels (LaunchArgs::time_start / time_end), kRing entries; timed[slot]: kernels ran
+    unsigned long long* d_ptime = nullptr;
+    unsigned long long* h_ptime = nullptr;   // page-locked copy
+    bool timed[kRing] = {};
+    // the kernel times of the ring's entries, read back once the stream is idle (waits for it)
+    int read_times();
+    float slot_ms(int slot) const;
     int last_slot = 0;                    // ring entry of the last pass (or several-pass call)
     int last_slot_passes = 1;             // passes that entry covers
     int* h_err = nullptr;                 // pinned copy of the error word
@@ -166,6 +183,7 @@ struct Context {
     // several-pass calls: one word per probe, bit i set while pass i of a march launch lists it
     // (zero between calls)
     uint32_t* d_pass_mask = nullptr;
+    uint32_t* d_pass_mask2 = nullptr;       // the other call's (consecutive calls alternate, as the rays)
 
     // adaptive time slicing state (internal_render.cpp:1190-1203)
     int frame = 0;

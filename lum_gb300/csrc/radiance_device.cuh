@@ -27,6 +27,13 @@ __device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; 
 // float -> int toward zero; PTX cvt.rzi saturates and maps NaN to 0.
 __device__ __forceinline__ int f2i(float f) { return __float2int_rz(f); }
 
+// The GPU's nanosecond clock (%globaltimer), the same on every SM.
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Programmatic dependent launch: a kernel launched as a dependent of the stream's previous one
 // starts once every CTA of that one has called grid_launch_dependents, and grid_dependency_wait
 // returns when that kernel has finished and its writes are visible (at once for a plain launch).

@@ -145,20 +145,12 @@ __device__ __forceinline__ long long claim_chunk(unsigned long long* queue, int*
 template <bool RECORD, bool STAGE = false, bool CTAQ = false>
 __global__ void __launch_bounds__(STAGE ? kStageWarps * 32 : kWarps * 32, STAGE ? 1 : 4)
 march_kernel(const __grid_constant__ LaunchArgs la) {
-    if (la.copy_dst) {   // the pass's start (see LaunchArgs): the march does not read the volumes
-        const long long stride = (long long)gridDim.x * blockDim.x;
-        const long long n16 = la.copy_bytes >> 4;
-        const uint4* s16 = reinterpret_cast<const uint4*>(la.copy_src);
-        uint4* d16 = reinterpret_cast<uint4*>(la.copy_dst);
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) d16[i] = __ldcs(s16 + i);
-        const long long n4 = la.copy_bytes >> 2;
-        for (long long i = n16 * 4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
-            reinterpret_cast<unsigned*>(la.copy_dst)[i] = reinterpret_cast<const unsigned*>(la.copy_src)[i];
-        if (blockIdx.x == 0 && threadIdx.x < 2 && la.clear_stats) la.clear_stats[threadIdx.x] = 0;
-        if (blockIdx.x == 0 && threadIdx.x == 0 && la.count_dst) *la.count_dst = __ldcg(la.count_src);
+    if (la.time_start && blockIdx.x == 0 && threadIdx.x == 0) {   // the pass's kernel-time start
+        la.time_start[0] = globaltimer_ns();
+        la.time_start[1] = 0;
     }
-    if (la.pass_mask) {   // several passes: mark each pass's probes (see LaunchArgs)
-        if (blockIdx.x == 0 && threadIdx.x < 2 && la.clear_stats) la.clear_stats[threadIdx.x] = 0;
+    if (la.pass_mask) {   // several passes: mark each pass's probes (this call's mask: the previous
+                          // call's last finalize clears the other)
         const long long stride = (long long)gridDim.x * blockDim.x;
         for (int i = 0; i < la.n_worlds; i++) {
             const WorldPass& w = la.worlds[i];
@@ -457,6 +449,27 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         }
     }
 
+
+    // The pass's start (see LaunchArgs), after the marching: a launch dependent on the previous
+    // pass's finalize marches in that launch's tail and waits here for it to end before touching
+    // what that launch reads or writes (the volumes, the counters)
+    if (la.copy_dst || la.clear_stats || la.count_dst) {
+        grid_dependency_wait();
+        const long long stride = (long long)gridDim.x * blockDim.x;
+        const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (la.copy_dst) {   // next starts as a copy of prev
+            const long long n16 = la.copy_bytes >> 4;
+            const uint4* s16 = reinterpret_cast<const uint4*>(la.copy_src);
+            uint4* d16 = reinterpret_cast<uint4*>(la.copy_dst);
+            for (long long i = tid; i < n16; i += stride) d16[i] = __ldcs(s16 + i);
+            const long long n4 = la.copy_bytes >> 2;
+            for (long long i = n16 * 4 + tid; i < n4; i += stride)
+                reinterpret_cast<unsigned*>(la.copy_dst)[i] = reinterpret_cast<const unsigned*>(la.copy_src)[i];
+        }
+        if (tid < 2 && la.clear_stats) la.clear_stats[tid] = 0;
+        if (tid == 0 && la.count_dst) *la.count_dst = __ldcg(la.count_src);
+    }
+
     // the last warp to finish resets the queue for the next launch
     if (lane == 0) {
         const unsigned long long e = atomicAdd(la.queue + 1, 1ull);
@@ -557,6 +570,7 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
         }
         if (a) atomicAdd(wp->stats, a);
         if (h) atomicAdd(wp->stats + 1, h);
+        if (la.time_end) atomicMax(la.time_end + 1, globaltimer_ns());
     }
 }
 
@@ -578,6 +592,8 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
             if (!((m >> la.mask_bit) & 1u)) dst[p] = __ldcs(src + p);
             if (la.mask_clear && m) la.pass_mask[p] = 0;
         }
+        __syncthreads();
+        if (threadIdx.x == 0 && la.time_end) atomicMax(la.time_end + 1, globaltimer_ns());
         return;
     }
     __shared__ float4 s_mean[kFinWarps];
@@ -640,24 +656,46 @@ size_t stage_bytes(const WorldPass& w) {
     return bytes <= (size_t)max_optin[dev] ? bytes : 0;
 }
 
+// A launch of `kern`; dependent: as a programmatic dependent of the stream's previous kernel (it
+// may start once every CTA of that kernel has called grid_launch_dependents; its reads and writes of
+// that kernel's data wait in grid_dependency_wait).
+cudaError_t launch_k(void (*kern)(LaunchArgs), int blocks, int threads, size_t smem, cudaStream_t stream, bool dependent,
+                     const LaunchArgs& args) {
+    if (!dependent) {
+        kern<<<blocks, threads, smem, stream>>>(args);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args);
+}
+
 // The march launch of a round (no hit records): staged when the world fits shared memory; the
-// CTA queue when the round has few tasks per warp.
-void launch_march(LaunchArgs args, const WorldPass& w, long long round_tasks, int num_sms, cudaStream_t stream) {
+// CTA queue when the round has few tasks per warp.  dependent: see launch_k (the previous kernel
+// is the previous pass's finalize; the march writes the other ray buffer).
+void launch_march(LaunchArgs args, const WorldPass& w, long long round_tasks, int num_sms, cudaStream_t stream,
+                  bool dependent = false) {
     const size_t smem = stage_bytes(w);
     if (smem > 0) {
         const int blocks = (int)std::min<long long>(num_sms, (std::max(round_tasks, 1LL) + kStageWarps - 1) / kStageWarps);
         args.total_warps = blocks * kStageWarps;
-        if (round_tasks < (long long)kCtaQueueTasksPerWarp * args.total_warps)
-            march_kernel<false, true, true><<<blocks, kStageWarps * 32, smem, stream>>>(args);
-        else
-            march_kernel<false, true><<<blocks, kStageWarps * 32, smem, stream>>>(args);
+        const bool q = round_tasks < (long long)kCtaQueueTasksPerWarp * args.total_warps;
+        launch_k(q ? march_kernel<false, true, true> : march_kernel<false, true>, blocks, kStageWarps * 32, smem, stream,
+                 dependent, args);
     } else {
         const int blocks = march_grid(false, num_sms, round_tasks, args.march_ctas);
         args.total_warps = blocks * kWarps;
-        if (round_tasks < (long long)kCtaQueueTasksPerWarp * args.total_warps)
-            march_kernel<false, false, true><<<blocks, kWarps * 32, 0, stream>>>(args);
-        else
-            march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(args);
+        const bool q = round_tasks < (long long)kCtaQueueTasksPerWarp * args.total_warps;
+        launch_k(q ? march_kernel<false, false, true> : march_kernel<false>, blocks, kWarps * 32, 0, stream, dependent,
+                 args);
     }
 }
 
@@ -668,26 +706,12 @@ template <class Store, bool RECORD>
 void launch_finalize(const LaunchArgs& args, int n, bool in_cta, cudaStream_t stream, bool overlap = false) {
     const int blocks = (n + kFinWarps - 1) / kFinWarps + (args.pass_mask ? args.fin_copy : 0);
     if (blocks <= 0) return;
-    auto kern = in_cta ? finalize_kernel<Store, RECORD, true> : finalize_kernel<Store, RECORD, false>;
-    if (!overlap) {
-        kern<<<blocks, kFinWarps * 32, 0, stream>>>(args);
-        return;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(kFinWarps * 32);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, args);
+    launch_k(in_cta ? finalize_kernel<Store, RECORD, true> : finalize_kernel<Store, RECORD, false>, blocks,
+             kFinWarps * 32, 0, stream, overlap, args);
 }
 
 template <class Store, bool RECORD>
-cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
+cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream, bool dependent) {
     const long long round = a.round_tasks > 0 ? a.round_tasks : kChunkTasks;
     const int blocks = march_grid(RECORD, num_sms, std::min(a.n_tasks, round), a.march_ctas);
     LaunchArgs args = a;
@@ -698,10 +722,11 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
         args.ray_origin = args.chunk_begin;
         const int n = args.chunk_end - args.chunk_begin;
         if (RECORD) march_kernel<RECORD><<<blocks, kWarps * 32, 0, stream>>>(args);
-        else launch_march(args, a.single, std::min(a.n_tasks, round), num_sms, stream);
+        else launch_march(args, a.single, std::min(a.n_tasks, round), num_sms, stream, dependent && c0 == 0);
         args.copy_dst = nullptr;   // the pass's start: in the first round's march only
         args.clear_stats = nullptr;
         args.count_dst = nullptr;
+        args.time_start = nullptr;
         const bool lean = a.force_lean || (a.worlds ? a.in_cta != 0 : combines_in_cta(&a.single, 1));
         launch_finalize<Store, RECORD>(args, n, lean, stream);
     }
@@ -710,7 +735,7 @@ cudaError_t launch_t(const LaunchArgs& a, int num_sms, cudaStream_t stream) {
 
 template <class Store>
 cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, size_t vol_bytes, int num_sms,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, bool dependent) {
     const int blocks = march_grid(false, num_sms, a.n_tasks, a.march_ctas);
     LaunchArgs args = a;
     args.total_warps = blocks * kWarps;
@@ -718,7 +743,7 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
     args.chunk_end = (int)a.n_tasks;
     args.ray_origin = 0;
     if (a.n_tasks > 0) {
-        launch_march(args, h_tab[0], a.n_tasks, num_sms, stream);
+        launch_march(args, h_tab[0], a.n_tasks, num_sms, stream, dependent);
     } else {   // every pass empty: plain copies
         for (int i = 0; i < n_passes; i++) {
             cudaError_t e = cudaMemcpyAsync(h_tab[i].next, h_tab[i].prev, vol_bytes, cudaMemcpyDeviceToDevice, stream);
@@ -728,6 +753,7 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
         return cudaSuccess;
     }
     args.clear_stats = nullptr;
+    args.time_start = nullptr;
     const bool in_cta = combines_in_cta(h_tab, n_passes);
     const long long probes = (long long)(vol_bytes / sizeof(typename Store::T));
     const int copy_ctas = (int)std::max<long long>(1, std::min<long long>((probes + 1023) / 1024, 2LL * num_sms));
@@ -753,14 +779,15 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
 }  // namespace
 
 cudaError_t launch_passes(const LaunchArgs& args, const WorldPass* h_tab, int n_passes, size_t vol_bytes,
-                          int precision, int num_sms, cudaStream_t stream) {
+                          int precision, int num_sms, cudaStream_t stream, bool dependent) {
     if (args.n_tasks > kMultiTasks || n_passes > kMultiPasses || !args.pass_mask) return cudaErrorInvalidValue;
     switch (precision) {
-        case LUMRAD_PRECISION_FP16: return passes_t<StoreF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
-        case LUMRAD_PRECISION_BF16: return passes_t<StoreBF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
+        case LUMRAD_PRECISION_FP16: return passes_t<StoreF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream, dependent);
+        case LUMRAD_PRECISION_BF16:
+            return passes_t<StoreBF16>(args, h_tab, n_passes, vol_bytes, num_sms, stream, dependent);
         case LUMRAD_PRECISION_RGB10A2:
-            return passes_t<StoreRGB10A2>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
-        default: return passes_t<StoreF32>(args, h_tab, n_passes, vol_bytes, num_sms, stream);
+            return passes_t<StoreRGB10A2>(args, h_tab, n_passes, vol_bytes, num_sms, stream, dependent);
+        default: return passes_t<StoreF32>(args, h_tab, n_passes, vol_bytes, num_sms, stream, dependent);
     }
 }
 
@@ -784,7 +811,8 @@ cudaError_t launch_table_pass(const LaunchArgs& a, int precision, int num_sms, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream) {
+cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, int num_sms, cudaStream_t stream,
+                            bool dependent) {
     if (args.n_tasks <= 0) {   // no march launch: the pass's start as copies
         cudaError_t e = cudaSuccess;
         if (args.copy_dst && args.copy_bytes > 0)
@@ -797,14 +825,14 @@ cudaError_t launch_radiance(const LaunchArgs& args, int precision, bool record, 
     }
     switch (precision) {
         case LUMRAD_PRECISION_FP16:
-            return record ? launch_t<StoreF16, true>(args, num_sms, stream) : launch_t<StoreF16, false>(args, num_sms, stream);
+            return record ? launch_t<StoreF16, true>(args, num_sms, stream, false) : launch_t<StoreF16, false>(args, num_sms, stream, dependent);
         case LUMRAD_PRECISION_BF16:
-            return record ? launch_t<StoreBF16, true>(args, num_sms, stream) : launch_t<StoreBF16, false>(args, num_sms, stream);
+            return record ? launch_t<StoreBF16, true>(args, num_sms, stream, false) : launch_t<StoreBF16, false>(args, num_sms, stream, dependent);
         case LUMRAD_PRECISION_RGB10A2:
-            return record ? launch_t<StoreRGB10A2, true>(args, num_sms, stream)
-                          : launch_t<StoreRGB10A2, false>(args, num_sms, stream);
+            return record ? launch_t<StoreRGB10A2, true>(args, num_sms, stream, false)
+                          : launch_t<StoreRGB10A2, false>(args, num_sms, stream, dependent);
         default:
-            return record ? launch_t<StoreF32, true>(args, num_sms, stream) : launch_t<StoreF32, false>(args, num_sms, stream);
+            return record ? launch_t<StoreF32, true>(args, num_sms, stream, false) : launch_t<StoreF32, false>(args, num_sms, stream, dependent);
     }
 }
 

@@ -31,11 +31,6 @@ namespace {
 
 constexpr int kLoopCta = 256;
 
-__device__ __forceinline__ unsigned long long globaltimer_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 __device__ __forceinline__ long long load_acquire_sys(const long long* p) {
     long long v;

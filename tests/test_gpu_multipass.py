@@ -189,3 +189,78 @@ def test_more_passes_than_one_launch_marks():
         for l, s in zip(lists + lists[:5], spec + spec[:5]):
             rw.radiance_pass(l, lum_gb300.pass_params(**s))
         assert twice.tobytes() == rw.get_radiance().tobytes()
+
+
+def test_back_to_back_calls_equal_synchronised_calls():
+    """Pass calls right after one another start their march in the previous pass's finalize tail
+    (the rays in the other buffer, the pass start after a wait): one-pass and several-pass calls
+    back to back, with an edit, an upload and a read-back between some of them, equal the same
+    calls each followed by a synchronisation, bit for bit, and the oracle's chain within 1e-5."""
+    import dataclasses
+
+    import lum_gb300
+    import oracle
+    w = worldgen.terrain_world((12, 10, 6), seed=56, n_types=12)
+    lists = [worldgen.probe_subset(w.dims, f, seed=57, stream=i) for i, f in enumerate((0.3, 0.6, 0.2, 0.5, 0.4, 0.7))]
+    spec = [dict(rays=(64, 128, 256, 32, 64, 128)[i], max_dist=80.0, blend=0.1 + 0.02 * i, time_seed=30 + i)
+            for i in range(6)]
+    edit = (3, 4, 2, 7)
+    prev = random_prev(w, seed=58)
+
+    def run(sync):
+        with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+            rw.load(w)
+            rw.set_radiance(prev)
+            for i, l in enumerate(lists):
+                rw.upload_requests(i, l)
+            params = [lum_gb300.pass_params(**s) for s in spec]
+            steps = [lambda: rw.radiance_pass_resident(0, params[0]),
+                     lambda: rw.radiance_pass_resident(1, params[1]),
+                     lambda: rw.radiance_passes_resident([2, 3], params[2:4]),
+                     lambda: rw.radiance_pass_resident(4, params[4]),
+                     lambda: rw.set_world_block(*edit),
+                     lambda: rw.radiance_pass_resident(5, params[5]),
+                     lambda: rw.radiance_passes_resident([0, 1], params[:2]),
+                     lambda: rw.get_radiance(),
+                     lambda: rw.radiance_pass_resident(2, params[2]),
+                     lambda: rw.radiance_passes_resident([3, 4, 5], params[3:6])]
+            for f in steps:
+                f()
+                if sync:
+                    rw.synchronize()
+            return rw.get_radiance()
+
+    fast, slow = run(False), run(True)
+    assert fast.tobytes() == slow.tobytes()
+    cur = prev
+    grid = w.grid
+    order = [0, 1, 2, 3, 4, "edit", 5, 0, 1, 2, 3, 4, 5]
+    for k in order:
+        if k == "edit":
+            grid = grid.copy()
+            grid[edit[2], edit[1], edit[0]] = edit[3]
+            continue
+        cur, _, _ = oracle.radiance_pass(dataclasses.replace(w, grid=grid), lists[k], prev=cur, **spec[k])
+    assert rel_err(fast, cur).max() <= RTOL
+
+
+def test_kernel_times_from_device_timestamps():
+    """Each pass's kernel time comes from timestamps its own kernels write (no events between the
+    launches): positive for passes with tasks, zero for an empty pass, one entry per call."""
+    import lum_gb300
+    w = worldgen.terrain_world((16, 16, 8), seed=59, n_types=12)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        allp = worldgen.all_probes(w.dims)
+        rw.upload_requests(0, allp)
+        rw.upload_requests(1, allp[:0])
+        p = lum_gb300.pass_params(rays=128, max_dist=64.0, blend=0.1)
+        for _ in range(3):
+            rw.radiance_pass_resident(0, p)
+        rw.radiance_pass_resident(1, p)
+        rw.radiance_passes_resident([0, 0], [p, p])
+        kt = rw.kernel_times(64)
+        assert kt.shape[0] == 5
+        assert (kt[:3] > 0.0).all() and kt[3] == 0.0 and kt[4] > 0.0
+        assert (kt < 1000.0).all()
+        assert rw.pass_stats()["gpu_ms"] > 0.0
