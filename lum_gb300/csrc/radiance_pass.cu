@@ -86,24 +86,29 @@ struct CtaQueue {
 };
 
 // One claim from the CTA's block: start << 12 | count of a guided chunk (its remainder /
-// (2 * warps per CTA), clamped to [1, cap]), or -2 when the block looked empty or ran out.
-__device__ __forceinline__ long long claim_from_block(int cap, int wpc, CtaQueue* q) {
+// (2 * WPC), clamped to [1, cap]), or -2 when the block looked empty or ran out.
+template <int WPC>
+__device__ __forceinline__ long long claim_from_block(int cap, CtaQueue* q) {
     const unsigned long long b = *reinterpret_cast<volatile unsigned long long*>(&q->blk);
     const int next = (int)(b & 0xFFFFFull), len = (int)((b >> 20) & 0xFFFull);
     if (next >= len) return -2;
-    const int k = max(1, min(cap, (len - next) / (2 * wpc)));
+    const int k = max(1, min(cap, (len - next) / (2 * WPC)));
     const unsigned long long o = atomicAdd(&q->blk, (unsigned long long)k);
     const int n2 = (int)(o & 0xFFFFFull), l2 = (int)((o >> 20) & 0xFFFull);
     return n2 < l2 ? ((long long)(o >> 32) + n2) << 12 | min(k, l2 - n2) : -2;
 }
 
 // The slow path (lane 0 of a warp that found the block empty): fetch the next block under the
-// CTA's lock, or claim from a block another warp fetched meanwhile.  Returns as claim_chunk.  Not
-// inlined: the march loop keeps its registers (a call per block, not per chunk).
-__device__ __noinline__ long long refill_block(unsigned long long* queue, int* error, int n_round, int div, int cap,
-                                               int wpc, int ctas, CtaQueue* q) {
+// CTA's lock, or claim from a block another warp fetched meanwhile.  Returns a chunk as
+// claim_from_block does, or -1 when the launch's tasks are exhausted.  Not inlined: the march loop
+// keeps its registers (a call per block, not per chunk).
+template <int WPC>
+__device__ __noinline__ long long refill_block(const LaunchArgs& la, int n_round, CtaQueue* q) {
+    const int div = la.guided_div > 0 ? la.guided_div : kQueueDiv;
+    const int cap = la.max_chunk > 0 ? la.max_chunk : kQueueCap;
+    const long long ctas = max(1, la.total_warps / WPC);
     for (int it = 0; it < (1 << 22); it++) {
-        const long long c = claim_from_block(cap, wpc, q);
+        const long long c = claim_from_block<WPC>(cap, q);
         if (c != -2) return c;
         if (*reinterpret_cast<volatile int*>(&q->done)) return -1;
         if (atomicCAS(&q->lock, 0, 1) == 0) {
@@ -112,11 +117,11 @@ __device__ __noinline__ long long refill_block(unsigned long long* queue, int* e
                 atomicExch(&q->lock, 0);
                 continue;
             }
-            const long long rem = (long long)n_round - (long long)*reinterpret_cast<volatile unsigned long long*>(queue);
-            const long long cta_cap = min(4095LL, (long long)cap * wpc);
+            const long long rem = (long long)n_round - (long long)*reinterpret_cast<volatile unsigned long long*>(la.queue);
+            const long long cta_cap = min(4095LL, (long long)cap * WPC);
             const long long kk = rem / ((long long)div * ctas);
             const long long k = kk < 1 ? 1 : (kk > cta_cap ? cta_cap : kk);
-            const unsigned long long start = atomicAdd(queue, (unsigned long long)k);
+            const unsigned long long start = atomicAdd(la.queue, (unsigned long long)k);
             if ((long long)start >= (long long)n_round) {
                 *reinterpret_cast<volatile int*>(&q->done) = 1;
                 __threadfence_block();
@@ -124,22 +129,15 @@ __device__ __noinline__ long long refill_block(unsigned long long* queue, int* e
                 return -1;
             }
             const long long len = min(k, (long long)n_round - (long long)start);
-            const long long own = max(1LL, min((long long)cap, len / (2LL * wpc)));
+            const long long own = max(1LL, min((long long)cap, len / (2LL * WPC)));
             atomicExch(&q->blk, (start << 32) | ((unsigned long long)len << 20) | (unsigned long long)own);
             atomicExch(&q->lock, 0);
             return ((long long)start << 12) | own;
         }
         __nanosleep(64);
     }
-    atomicOr(error, 1);   // the lock holder never finished (it waits for nothing: cannot happen)
+    atomicOr(la.error, 1);   // the lock holder never finished (it waits for nothing: cannot happen)
     return -1;
-}
-
-// Lane 0: the warp's next chunk as start << 12 | count (round-relative), or -1 when none is left.
-__device__ __forceinline__ long long claim_chunk(unsigned long long* queue, int* error, int n_round, int div, int cap,
-                                                 int wpc, int ctas, CtaQueue* q) {
-    const long long c = claim_from_block(cap, wpc, q);
-    return c != -2 ? c : refill_block(queue, error, n_round, div, cap, wpc, ctas, q);
 }
 
 template <bool RECORD, bool STAGE = false, bool CTAQ = false>
@@ -235,10 +233,10 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
     // its warps take single tasks from that block with a shared-memory atomic, and the warp that
     // finds it empty fetches the next block under a shared lock.  The global word sees one claim
     // per CTA block instead of one per warp chunk, and warps balance at single tasks.
-    // Claims: CTAQ, through the CTA's block (claim_chunk; launches with few tasks per warp, such as
-    // a single pass: the warps balance at single tasks); else straight from the launch's queue
-    // word in guided chunks of remaining / (div * warps), clamped to [1, cap] (several passes,
-    // batches: large chunks, few claims).  Two instantiations: the CTA queue's code costs the
+    // Claims: CTAQ, through the CTA's block (claim_from_block, refill_block; launches with few tasks
+    // per warp, such as a single pass: the warps balance at single tasks); else straight from the
+    // launch's queue word in guided chunks of remaining / (div * warps), clamped to [1, cap]
+    // (several passes, batches: large chunks, few claims).  Two instantiations: the CTA queue's code costs the
     // other form's march loop registers (2.5% on an 8-pass launch when only branched around).
     auto next_task = [&]() -> int {
         if (pending >= 0) return pending;
@@ -246,11 +244,11 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
             if (exhausted) return -1;
             long long c = 0;
             if (lane == 0) {
-                const int div = la.guided_div > 0 ? la.guided_div : kQueueDiv;
                 const int cap = la.max_chunk > 0 ? la.max_chunk : kQueueCap;
                 if (CTAQ) {
-                    const int wpc = (int)(blockDim.x >> 5);
-                    c = claim_chunk(la.queue, la.error, n_round, div, cap, wpc, max(1, la.total_warps / wpc), &s_q);
+                    constexpr int kWpc = STAGE ? kStageWarps : kWarps;
+                    c = claim_from_block<kWpc>(cap, &s_q);
+                    if (c == -2) c = refill_block<kWpc>(la, n_round, &s_q);
                 } else {
                     const unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(la.queue);
                     const long long kk = ((long long)n_round - (long long)cur) /
