@@ -14,7 +14,8 @@ Workload (one "step"): the 64x64x16-block terrain world plus 2000 random blocks 
              lists host->device (lumrad_radiance_passes) and reads the radiance volume back.
   roofline   the bound that limits the step's kernels (march + 8 finalize launches): instruction
              issue.  achieved = warp instructions per step (ncu's smsp__inst_executed.sum over the
-             same 9 launches, NCU_WARP_INST_PER_STEP) / the kernels' own event-timed duration;
+             same 9 launches, NCU_WARP_INST_PER_STEP) / the kernels' own duration (the span of
+             the %globaltimer stamps they write, lumrad_get_kernel_times);
              peak = one warp instruction per cycle on each of the 4 schedulers of every SM at the SM
              clock sampled during the timed region.  Beside it, the memory rooflines: algorithmic
              bytes of one step (3 B per grid+palette lookup, 16+8*12 B per hit, 8+2*12 B per probe;
@@ -58,14 +59,14 @@ S_R = 12            # bytes of FP32 RGB radiance per probe
 BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches, whose extra CTAs copy each pass's unlisted probes) in an ncu capture of this
-# workload; ncu replays with cold caches (march 1.79 + 46.73 MB, finalizes 120.36 + 0.00 MB)
-NCU_DRAM_BYTES_PER_STEP = 168.88e6
-# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 498.7 MB: its world
-# lookups are shared-memory loads, finalizes 1,013.3 MB)
-NCU_L2_BYTES_PER_STEP = 1512.0e6
+# workload; ncu replays with cold caches (march 1.87 + 46.74 MB, finalizes 120.36 + 0.00 MB)
+NCU_DRAM_BYTES_PER_STEP = 168.97e6
+# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 498.1 MB: its world
+# lookups are shared-memory loads, finalizes 1,015.7 MB)
+NCU_L2_BYTES_PER_STEP = 1513.9e6
 # Warp instructions (smsp__inst_executed.sum) of the same 9 launches: the march over the 8 passes
-# (461.7 M) and the 8 finalize launches (409.9 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 461.7e6 + 409.9e6
+# (466.4 M) and the 8 finalize launches (411.6 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 466.4e6 + 411.6e6
 SCHEDULERS_PER_SM = 4
 
 
