@@ -11,10 +11,7 @@ constexpr int kWarps = 8;
 // Warps (one task each) per finalize CTA; a divisor of kWarps, since worlds of a batch start at
 // multiples of kWarps tasks
 constexpr int kFinWarps = 8;
-static_assert(kWarps % kFinWarps == 0, "finalize runs must not straddle worlds");
-// Runs of kFinWarps tasks per finalize CTA (each warp takes one task of each run)
-constexpr int kFinReps = 1;
-constexpr int kFinTasks = kFinWarps * kFinReps;
+static_assert(kWarps % kFinWarps == 0, "finalize CTAs must not straddle worlds");
 // A task is one 32-ray subgroup of one probe (the unit radiance.comp sums with subgroupAdd).
 constexpr int kTaskRays = 32;
 // Tasks per march/finalize round: the per-ray buffer between the two kernels holds this many

@@ -304,8 +304,8 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
 
     // The coarse march (CastRay_fast, radiance.comp:198-244) of the lanes' rays, two coarse steps
     // per iteration (a lane whose ray ends in the first takes no second: the warp's vote and
-    // hand-out run once per two steps), until a task's room in the ring is free while tasks may remain, or no
-    // lane has a ray; a FAST loop also ends when a lane takes a ray that is not regular.
+    // hand-out run once per two steps), until the ring has room for a task while tasks may remain,
+    // or no lane has a ray; a FAST loop also ends when a lane takes a ray that is not regular.
     auto march = [&](auto fast_tag, auto wide_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
         constexpr bool WIDE = decltype(wide_tag)::value;
@@ -490,103 +490,91 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
 // then has no global-memory combine, which costs the general kernel 8 registers and spills, and
 // runs 6 CTAs per SM (40 registers): the kernel is latency-bound; against four CTAs, five measured
 // 4-6% faster and six 1% faster again (seven: slower on single passes).
-// One group (one CTA's work) of the finalize kernel: kFinReps runs of kFinWarps consecutive tasks,
-// warp w taking task w of each run (a run is 8-task aligned, so a probe's subgroups share a run
-// when R/32 divides 8); no barrier between the runs, so a warp whose task ended early goes on to
-// the next.
+// One 8-task group (one CTA's work) of the finalize kernel.
 template <class Store, bool RECORD, bool IN_CTA>
 __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, float4* s_mean, int* s_count,
                                                unsigned (*s_stat)[2]) {
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
-    if (threadIdx.x < kFinTasks) {
+    if (threadIdx.x < kFinWarps) {
         s_count[threadIdx.x] = 0;
         s_stat[threadIdx.x][0] = 0;
         s_stat[threadIdx.x][1] = 0;
     }
     __syncthreads();
-#pragma unroll 1
-    for (int rep = 0; rep < kFinReps; rep++) {
-        const int t0 = la.chunk_begin + group * kFinTasks + rep * kFinWarps;   // worlds start at multiples of 8
-        const int t = t0 + w;
-        const int slot = rep * kFinWarps + w;   // this task's shared-memory slot
-        const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
-        const int t_local = t - (int)wp->task_begin;
-        bool valid = t < la.chunk_end && t_local < wp->n_tasks;
-        if (la.dev_count)   // a list built on the device (single world): its own length bounds the tasks
-            valid = valid && t_local < (__ldcg(la.dev_count) / wp->size) * (wp->R >> 5);
-        const int nsub = wp->R >> 5;
-        const int g = div_nsub(max(t_local, 0), nsub);
-        const int k = t_local - g * nsub;
-        // a probe's subgroups share this CTA when R/32 divides 8 (task_begin is a multiple of 8)
-        const bool local = nsub > 1 && (kFinWarps % nsub) == 0 && (wp->task_begin % kFinWarps) == 0;
-        float3 v = make_float3(0.0f, 0.0f, 0.0f);
-        if (valid) {
-            const long long idx = (long long)(t - la.ray_origin) * kTaskRays + lane;
-            const uint2 res = __ldcg(la.ray_res + idx);
-            const int blk = RECORD ? __ldcg(la.ray_blk + idx) : 0;
-            float3 o, d;
-            setup_ray(*wp, g, k * kTaskRays + lane, o, d);   // bit-identical to the march's set-up
-            uint32_t lookups;
-            float3 L, u;
-            float4 m;
-            const bool hit = finalize_ray<RECORD>(*wp, march_view(*wp), o, d, __uint_as_float(res.x), res.y, blk,
-                                                  (long long)t_local * kTaskRays + lane, lookups, L, u, m);
-            grid_dependency_wait();   // from here on the volumes: the previous pass's launch has finished
-            if (hit) L = shade_hit<Store>(*wp, u, m);
-            L = butterfly_sum(L);
-            v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
-            // counters: lookups and hits of this task, summed per CTA below
-            const unsigned a = __reduce_add_sync(kFull, lookups);
-            const unsigned h = __popc(__ballot_sync(kFull, (res.y >> 24) & 1u));
-            if (lane == 0) {
-                s_stat[slot][0] = a;
-                s_stat[slot][1] = h;
-                if (nsub == 1) {
-                    store_probe<Store>(*wp, g, make_float3(fadd(0.0f, v.x), fadd(0.0f, v.y), fadd(0.0f, v.z)));
-                } else if (!local) {
-                    if (IN_CTA) atomicOr(la.error, 2);   // launched with the wrong kernel: reported, never stored
-                    else subgroup_done<Store>(*wp, g, k, v);
-                } else {
-                    // the last of the probe's subgroups in this CTA sums their means in subgroup
-                    // order (radiance.comp:401-407)
-                    volatile float* vm = reinterpret_cast<volatile float*>(s_mean);
-                    vm[4 * slot] = v.x;
-                    vm[4 * slot + 1] = v.y;
-                    vm[4 * slot + 2] = v.z;
+    const int t0 = la.chunk_begin + group * kFinWarps;   // worlds start at multiples of 8
+    const int t = t0 + w;
+    const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
+    const int t_local = t - (int)wp->task_begin;
+    bool valid = t < la.chunk_end && t_local < wp->n_tasks;
+    if (la.dev_count)   // a list built on the device (single world): its own length bounds the tasks
+        valid = valid && t_local < (__ldcg(la.dev_count) / wp->size) * (wp->R >> 5);
+    const int nsub = wp->R >> 5;
+    const int g = div_nsub(max(t_local, 0), nsub);
+    const int k = t_local - g * nsub;
+    // a probe's subgroups share this CTA when R/32 divides 8 (task_begin is a multiple of 8)
+    const bool local = nsub > 1 && (kFinWarps % nsub) == 0 && (wp->task_begin % kFinWarps) == 0;
+    float3 v = make_float3(0.0f, 0.0f, 0.0f);
+    if (valid) {
+        const long long idx = (long long)(t - la.ray_origin) * kTaskRays + lane;
+        const uint2 res = __ldcg(la.ray_res + idx);
+        const int blk = RECORD ? __ldcg(la.ray_blk + idx) : 0;
+        float3 o, d;
+        setup_ray(*wp, g, k * kTaskRays + lane, o, d);   // bit-identical to the march's set-up
+        uint32_t lookups;
+        float3 L, u;
+        float4 m;
+        const bool hit = finalize_ray<RECORD>(*wp, march_view(*wp), o, d, __uint_as_float(res.x), res.y, blk,
+                                              (long long)t_local * kTaskRays + lane, lookups, L, u, m);
+        grid_dependency_wait();   // from here on the volumes: the previous pass's launch has finished
+        if (hit) L = shade_hit<Store>(*wp, u, m);
+        L = butterfly_sum(L);
+        v = make_float3(fmul(L.x, 0.03125f), fmul(L.y, 0.03125f), fmul(L.z, 0.03125f));   // /32
+        // counters: lookups and hits of this task, summed per CTA below
+        const unsigned a = __reduce_add_sync(kFull, lookups);
+        const unsigned h = __popc(__ballot_sync(kFull, (res.y >> 24) & 1u));
+        if (lane == 0) {
+            s_stat[w][0] = a;
+            s_stat[w][1] = h;
+            if (nsub == 1) {
+                store_probe<Store>(*wp, g, make_float3(fadd(0.0f, v.x), fadd(0.0f, v.y), fadd(0.0f, v.z)));
+            } else if (!local) {
+                if (IN_CTA) atomicOr(la.error, 2);   // launched with the wrong kernel: reported, never stored
+                else subgroup_done<Store>(*wp, g, k, v);
+            } else {
+                // the last of the probe's subgroups in this CTA sums their means in subgroup
+                // order (radiance.comp:401-407)
+                volatile float* vm = reinterpret_cast<volatile float*>(s_mean);
+                vm[4 * w] = v.x;
+                vm[4 * w + 1] = v.y;
+                vm[4 * w + 2] = v.z;
+                __threadfence_block();
+                if (atomicAdd(&s_count[w - k], 1) == nsub - 1) {
                     __threadfence_block();
-                    if (atomicAdd(&s_count[slot - k], 1) == nsub - 1) {
-                        __threadfence_block();
-                        float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-                        for (int j = slot - k; j < slot - k + nsub; j++) {
-                            const float sx = vm[4 * j], sy = vm[4 * j + 1], sz = vm[4 * j + 2];
-                            acc = make_float3(fadd(acc.x, sx), fadd(acc.y, sy), fadd(acc.z, sz));
-                        }
-                        const float fn = (float)nsub;
-                        acc = make_float3(fdiv_by(acc.x, fn, wp->inv_nsub), fdiv_by(acc.y, fn, wp->inv_nsub),
-                                          fdiv_by(acc.z, fn, wp->inv_nsub));
-                        store_probe<Store>(*wp, g, acc);
+                    float3 acc = make_float3(0.0f, 0.0f, 0.0f);
+                    for (int j = w - k; j < w - k + nsub; j++) {
+                        const float sx = vm[4 * j], sy = vm[4 * j + 1], sz = vm[4 * j + 2];
+                        acc = make_float3(fadd(acc.x, sx), fadd(acc.y, sy), fadd(acc.z, sz));
                     }
+                    const float fn = (float)nsub;
+                    acc = make_float3(fdiv_by(acc.x, fn, wp->inv_nsub), fdiv_by(acc.y, fn, wp->inv_nsub),
+                                      fdiv_by(acc.z, fn, wp->inv_nsub));
+                    store_probe<Store>(*wp, g, acc);
                 }
             }
         }
     }
-    // the CTA's counters in one atomic each per run (a run is in one world); same-address atomics
-    // from every task serialise at one L2 slice and held warps at exit (measured 5% of the pass)
+    // the CTA's counters in one atomic each: one world per CTA; same-address atomics from every
+    // task serialise at one L2 slice and held warps at exit (measured 5% of the pass)
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int rep = 0; rep < kFinReps; rep++) {
-            unsigned long long a = 0, h = 0;
-            for (int j = rep * kFinWarps; j < (rep + 1) * kFinWarps; j++) {
-                a += s_stat[j][0];
-                h += s_stat[j][1];
-            }
-            if (!a && !h) continue;
-            const int t0 = la.chunk_begin + group * kFinTasks + rep * kFinWarps;
-            const WorldPass* wp = la.worlds ? la.worlds + world_of(la, t0) : &la.single;
-            if (a) atomicAdd(wp->stats, a);
-            if (h) atomicAdd(wp->stats + 1, h);
+        unsigned long long a = 0, h = 0;
+        for (int j = 0; j < kFinWarps; j++) {
+            a += s_stat[j][0];
+            h += s_stat[j][1];
         }
+        if (a) atomicAdd(wp->stats, a);
+        if (h) atomicAdd(wp->stats + 1, h);
         if (la.time_end) atomicMax(la.time_end + 1, globaltimer_ns());
     }
 }
@@ -613,15 +601,15 @@ finalize_kernel(const __grid_constant__ LaunchArgs la) {
         if (threadIdx.x == 0 && la.time_end) atomicMax(la.time_end + 1, globaltimer_ns());
         return;
     }
-    __shared__ float4 s_mean[kFinTasks];
-    __shared__ int s_count[kFinTasks];
-    __shared__ unsigned s_stat[kFinTasks][2];
+    __shared__ float4 s_mean[kFinWarps];
+    __shared__ int s_count[kFinWarps];
+    __shared__ unsigned s_stat[kFinWarps][2];
     if (!PERSIST) {
         finalize_group<Store, RECORD, IN_CTA>(la, (int)blockIdx.x, s_mean, s_count, s_stat);
         return;
     }
     const long long total = la.dev_total ? __ldcg(la.dev_total) : (long long)la.chunk_end;
-    const int groups = (int)((min(total, (long long)la.chunk_end) - la.chunk_begin + kFinTasks - 1) / kFinTasks);
+    const int groups = (int)((min(total, (long long)la.chunk_end) - la.chunk_begin + kFinWarps - 1) / kFinWarps);
     for (int g = (int)blockIdx.x; g < groups; g += (int)gridDim.x) {
         finalize_group<Store, RECORD, IN_CTA>(la, g, s_mean, s_count, s_stat);
         __syncthreads();   // thread 0 has read the counters before the next group clears them
@@ -721,7 +709,7 @@ void launch_march(LaunchArgs args, const WorldPass& w, long long round_tasks, in
 // volume reads and writes wait for that kernel's end (griddepcontrol.wait).
 template <class Store, bool RECORD>
 void launch_finalize(const LaunchArgs& args, int n, bool in_cta, cudaStream_t stream, bool overlap = false) {
-    const int blocks = (n + kFinTasks - 1) / kFinTasks + (args.pass_mask ? args.fin_copy : 0);
+    const int blocks = (n + kFinWarps - 1) / kFinWarps + (args.pass_mask ? args.fin_copy : 0);
     if (blocks <= 0) return;
     launch_k(in_cta ? finalize_kernel<Store, RECORD, true> : finalize_kernel<Store, RECORD, false>, blocks,
              kFinWarps * 32, 0, stream, overlap, args);
@@ -784,7 +772,7 @@ cudaError_t passes_t(const LaunchArgs& a, const WorldPass* h_tab, int n_passes, 
         args.copy_bytes = (long long)vol_bytes;
         args.mask_bit = i;
         args.mask_clear = i == n_passes - 1;
-        args.fin_ctas = (n + kFinTasks - 1) / kFinTasks;
+        args.fin_ctas = (n + kFinWarps - 1) / kFinWarps;
         args.fin_copy = copy_ctas;
         // from the second pass on, the launch overlaps the previous pass's tail: its refine and
         // materials read no volume (the first pass's rays come from the march launch before it)
@@ -1122,7 +1110,7 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
         const int tasks = la.chunk_end - la.chunk_begin;
         if (tasks < kCtaQueueTasksPerWarp * la.total_warps) march_kernel<false, false, true><<<blocks, kWarps * 32, 0, stream>>>(la);
         else march_kernel<false><<<blocks, kWarps * 32, 0, stream>>>(la);
-        finalize_kernel<StoreF32, false, true><<<(tasks + kFinTasks - 1) / kFinTasks, kFinWarps * 32, 0, stream>>>(la);
+        finalize_kernel<StoreF32, false, true><<<(tasks + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, stream>>>(la);
     }
     LUMRAD_TRY(cudaGetLastError());
     return LUMRAD_OK;
