@@ -471,7 +471,9 @@ int Context::run_pass(const short4* d_reqs, int n, const LumRadPassParams* p_in,
     la.time_start = la.time_end = d_ptime + 2 * slot;
     timed[slot] = la.n_tasks > 0;
     LUMRAD_TRY(launch_radiance(la, world.precision, p.record_hits != 0, num_sms, stream, dependent));
-    pass_mark = p.record_hits ? -1 : api_calls;
+    // the next pass call may start in this pass's finalize tail: only when its last operation is
+    // that finalize launch (not the copies of an empty pass) and it has no hit records
+    pass_mark = p.record_hits || la.n_tasks <= 0 ? -1 : api_calls;
     uploads_mark = world.uploads;
     last_slot = slot;
     last_slot_passes = 1;
@@ -531,6 +533,7 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     const int slot = (int)(n_passes % kRing);
     timed[slot] = false;
     bool first = true;   // the first launch clears the counters and starts the kernel time
+    bool ends_in_finalize = false;   // the call's last operation is a finalize launch
     // the first march may start in the previous pass's finalize tail: see pass_mark
     bool dependent = pass_mark == api_calls - 1 && uploads_mark == world.uploads;
     const int side = ray_side;   // this call's ray buffer (the previous pass's finalize reads the other)
@@ -565,6 +568,7 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
             la.ray_blk = d_ray_blk;
             LUMRAD_TRY(launch_radiance(la, world.precision, false, num_sms, stream, dependent));
             dependent = false;
+            ends_in_finalize = la.n_tasks > 0;
             probes += (uint64_t)la.single.n_groups;
             rays += (uint64_t)la.single.n_groups * la.single.R;
             world.cur = 1 - world.cur;
@@ -622,9 +626,10 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
         first = false;
         LUMRAD_TRY(launch_passes(la, tab, k, vol_bytes, world.precision, num_sms, stream, dependent));
         dependent = false;
+        ends_in_finalize = total > 0;
         i = j;
     }
-    pass_mark = api_calls;
+    pass_mark = ends_in_finalize ? api_calls : -1;
     uploads_mark = world.uploads;
     last_slot = slot;
     last_slot_passes = n;

@@ -194,8 +194,9 @@ def test_more_passes_than_one_launch_marks():
 def test_back_to_back_calls_equal_synchronised_calls():
     """Pass calls right after one another start their march in the previous pass's finalize tail
     (the rays in the other buffer, the pass start after a wait): one-pass and several-pass calls
-    back to back, with an edit, an upload and a read-back between some of them, equal the same
-    calls each followed by a synchronisation, bit for bit, and the oracle's chain within 1e-5."""
+    back to back, with an empty pass, an edit, an upload and a read-back between some of them,
+    equal the same calls each followed by a synchronisation, bit for bit, and the oracle's chain
+    within 1e-5."""
     import dataclasses
 
     import lum_gb300
@@ -213,8 +214,10 @@ def test_back_to_back_calls_equal_synchronised_calls():
             rw.set_radiance(prev)
             for i, l in enumerate(lists):
                 rw.upload_requests(i, l)
+            rw.upload_requests(6, lists[0][:0])   # an empty list: a pass of copies only
             params = [lum_gb300.pass_params(**s) for s in spec]
             steps = [lambda: rw.radiance_pass_resident(0, params[0]),
+                     lambda: rw.radiance_pass_resident(6, params[1]),
                      lambda: rw.radiance_pass_resident(1, params[1]),
                      lambda: rw.radiance_passes_resident([2, 3], params[2:4]),
                      lambda: rw.radiance_pass_resident(4, params[4]),
