@@ -284,16 +284,24 @@ SERVE_WORKLOAD = {
 }
 
 
-def _serve_trace(srv, reqs, arrivals, params_of):
+def _serve_trace(srv, reqs, arrivals, params_of, allow_shed=False):
     """Submits every request with its arrival time (offset into the future), serves them all and
-    returns (latencies s, rays, span s)."""
+    returns (latencies s, rays, span s) of the requests that ran (allow_shed: requests shed by a
+    queueing bound are left out)."""
+    import lum_gb300
     base = srv.now() + 0.5 + 2e-5 * len(reqs)
     for k, (w, e) in enumerate(reqs):
         srv.submit(w, e, params_of(k), base + float(arrivals[k]))
     late = srv.now() > base
     srv.run(timeout_s=600)
     d = srv.poll(len(reqs) + 16)
-    assert len(d) == len(reqs) and (d["status"] == 0).all(), "serving trace failed"
+    ok = d["status"] == 0
+    if allow_shed:
+        ok_or_shed = ok | (d["status"] == lum_gb300._native.LUMRAD_ETIMEOUT)
+        assert len(d) == len(reqs) and ok_or_shed.all(), "serving trace failed"
+        d = d[ok]
+    else:
+        assert len(d) == len(reqs) and ok.all(), "serving trace failed"
     lat = d["done_s"] - d["arrival_s"]
     rays = int((d["probes"].astype(np.int64) * d["rays_per_probe"]).sum())
     span = float(d["done_s"].max() - d["arrival_s"].min())
@@ -521,6 +529,24 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
     sat = summary(*_serve_trace(srv, reqs, np.zeros(n_requests), params_of))
     st = srv.stats()
     srv.close()
+    # overload with a queueing bound: requests that waited past max_queue_ms are shed, the rest
+    # keep a bounded latency
+    bounded = None
+    if rates:
+        bound_ms = 2.0
+        bsrv = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=inflight,
+                                        max_queue_ms=bound_ms)
+        for rw in rws:
+            bsrv.add_world(rw)
+        _serve_trace(bsrv, reqs[:200], np.zeros(200), params_of, allow_shed=True)
+        shed0 = bsrv.stats()["shed"]
+        rate = max(rates)
+        arr = worldgen.poisson_arrivals(n_requests, rate, seed=SEED + int(rate))
+        lat, rays, span, late = _serve_trace(bsrv, reqs, arr, params_of, allow_shed=True)
+        shed = bsrv.stats()["shed"] - shed0
+        bounded = dict(summary(lat, rays, span, late), rate_per_s=rate, max_queue_ms=bound_ms,
+                       shed=int(shed), shed_fraction=shed / n_requests)
+        bsrv.close()
     plain = lum_gb300.RadianceServer(device=local, hbm_budget_bytes=budget, max_inflight=1,
                                      max_requests_per_launch=1)
     for rw in rws:
@@ -546,7 +572,7 @@ def serving_leg(local: int, n_requests: int = 10000, rates=(2000.0, 5000.0, 1000
                 "plain_saturated": psat, "speedup_vs_plain": sat["probe_rays_per_s"] / psat["probe_rays_per_s"],
                 "launches": st["launches"], "max_requests_in_launch": st["max_requests_in_launch"],
                 "resident_gb": st["resident_bytes"] / 1e9, "peak_inflight_mb": st["peak_inflight_bytes"] / 1e6,
-                "max_inflight": inflight,
+                "max_inflight": inflight, "overload_bounded": bounded,
                 "device_loop": {"sweep": dsweep, "saturated": dsat, "graph_launches": dst["launches"],
                                 "how": "one CUDA graph (WHILE node) per busy period: admit -> edits -> dirty "
                                        "lists -> pass -> completions, polling a page-locked request ring"}})

@@ -339,6 +339,13 @@ typedef struct {
     int    device_loop;           /* 1 = the request loop runs on the device (see below) */
     float  poll_ms;               /* device loop: how long it waits for a request before it ends
                                      (the host starts it again on the next request); 0 = 2 ms */
+    float  max_queue_ms;          /* queueing bound (0 = none): a request that has waited longer
+                                     than this since its arrival when its turn comes is not run; it
+                                     completes with LUMRAD_ETIMEOUT and its edits are not applied.
+                                     Under overload this sheds load instead of letting every
+                                     request's latency grow.  Host loop: checked at admission.
+                                     Device loop: the host keeps at most two iterations' requests
+                                     published per lane and checks when it publishes. */
 } LumRadServerSettings;
 
 typedef struct { int16_t x, y, z, block; } LumRadEdit;
@@ -347,6 +354,7 @@ typedef struct {
     long long request;            /* id given by lumrad_server_submit */
     int    world;
     int    status;                /* LUMRAD_OK, LUMRAD_ENOMEM (never fits the budget), LUMRAD_ECANCELED,
+                                     LUMRAD_ETIMEOUT (waited past max_queue_ms; not run),
                                      LUMRAD_EDEVICE */
     int    probes;                /* probes relit */
     int    rays_per_probe;
@@ -366,6 +374,7 @@ typedef struct {
     long long evictions;          /* worlds evicted to make room */
     long long readmissions;       /* evicted worlds uploaded again */
     double peak_device_bytes;     /* largest resident + launch buffers + in flight, ever */
+    long long shed;               /* requests not run: waited past max_queue_ms */
 } LumRadServerStats;
 
 int  lumrad_server_create(const LumRadServerSettings* settings, LumRadServer* out);

@@ -333,11 +333,12 @@ class RadianceServer:
 
     def __init__(self, device: int = 0, precision: str = "fp32", hbm_budget_bytes: float = 0.0,
                  max_inflight: int = 4, max_requests_per_launch: int = 0, radius: int = 2,
-                 device_loop: bool = False, poll_ms: float = 0.0):
+                 device_loop: bool = False, poll_ms: float = 0.0, max_queue_ms: float = 0.0):
         from ._native import ServerSettings
         self.lib = load()
         s = ServerSettings(int(device), PRECISION[precision], float(hbm_budget_bytes), int(max_inflight),
-                           int(max_requests_per_launch), int(radius), 1 if device_loop else 0, float(poll_ms))
+                           int(max_requests_per_launch), int(radius), 1 if device_loop else 0, float(poll_ms),
+                           float(max_queue_ms))
         h = C.c_void_p()
         check(self.lib.lumrad_server_create(C.byref(s), C.byref(h)))
         self.h = h

@@ -57,14 +57,15 @@ class Tuning(C.Structure):
 class ServerSettings(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget_bytes", C.c_double),
                 ("max_inflight", C.c_int), ("max_requests_per_launch", C.c_int), ("radius", C.c_int),
-                ("device_loop", C.c_int), ("poll_ms", C.c_float)]
+                ("device_loop", C.c_int), ("poll_ms", C.c_float), ("max_queue_ms", C.c_float)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("launches", C.c_longlong), ("requests", C.c_longlong), ("probes", C.c_uint64),
                 ("rays", C.c_uint64), ("resident_bytes", C.c_double), ("launch_bytes", C.c_double),
                 ("peak_inflight_bytes", C.c_double), ("max_requests_in_launch", C.c_int),
-                ("evictions", C.c_longlong), ("readmissions", C.c_longlong), ("peak_device_bytes", C.c_double)]
+                ("evictions", C.c_longlong), ("readmissions", C.c_longlong), ("peak_device_bytes", C.c_double),
+                ("shed", C.c_longlong)]
 
 
 # LumRadEdit and LumRadCompletion as numpy records (same layout as the C structs)

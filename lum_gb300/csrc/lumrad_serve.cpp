@@ -313,11 +313,19 @@ int launch(Server* sv, int k, int free_slots, bool* started) {
     Slot& sl = *sv->slots[k];
     const double now = sv->now();
     const size_t budget = sv->budget();
-    // candidates: the front request of each idle world, oldest submission first
+    // candidates: the front request of each idle world, oldest submission first; a front request
+    // past the queueing bound is shed (not run) and the world's next one considered
     std::vector<int> cand;
+    const double bound = sv->s.max_queue_ms > 0.0f ? 1e-3 * sv->s.max_queue_ms : -1.0;
     for (size_t w = 0; w < sv->worlds.size(); w++) {
         SWorld& sw = sv->worlds[w];
-        if (!sw.busy && !sw.fifo.empty() && sw.fifo.front().arrival <= now) cand.push_back((int)w);
+        if (sw.busy) continue;
+        while (bound >= 0.0 && !sw.fifo.empty() && now - sw.fifo.front().arrival > bound) {
+            complete_now(sv, sw.fifo.front(), LUMRAD_ETIMEOUT);
+            sw.fifo.pop_front();
+            sv->st.shed++;
+        }
+        if (!sw.fifo.empty() && sw.fifo.front().arrival <= now) cand.push_back((int)w);
     }
     if (cand.empty()) return LUMRAD_OK;
     std::sort(cand.begin(), cand.end(),
@@ -781,15 +789,26 @@ int devloop_progress(Server* sv) {
             ln.edit_ends.pop_front();
         }
     }
-    // due requests into their lanes' rings, in submission order
+    // due requests into their lanes' rings, in submission order.  With a queueing bound a lane
+    // holds at most two iterations' requests published (the rest wait here, where a request past
+    // the bound is shed rather than published)
     const double now = sv->now();
+    const double bound = sv->s.max_queue_ms > 0.0f ? 1e-3 * sv->s.max_queue_ms : -1.0;
+    const long long window = bound >= 0.0 ? 2LL * kDevBatch : dl.ring_cap;
     bool published[kDevLanes] = {};
     while (!dl.queue.empty()) {
         SRequest& r = dl.queue.front();
         if (r.arrival > now) break;
+        if (bound >= 0.0 && now - r.arrival > bound) {
+            complete_now(sv, r, LUMRAD_ETIMEOUT);
+            dl.queue.pop_front();
+            sv->st.shed++;
+            continue;
+        }
         DevLane& ln = dl.lanes[r.world % kDevLanes];
         const long long ne = (long long)r.edits.size();
-        if (ln.head - ln.done_read >= dl.ring_cap || ne > dl.edit_cap - (ln.edit_head - ln.edit_tail)) break;
+        if (ln.head - ln.done_read >= std::min(window, dl.ring_cap) || ne > dl.edit_cap - (ln.edit_head - ln.edit_tail))
+            break;
         for (long long k = 0; k < ne; k++) ln.edits[(ln.edit_head + k) % dl.edit_cap] = r.edits[(size_t)k];
         DevRequest& q = ln.ring[ln.head % dl.ring_cap];
         q.id = r.id;
@@ -928,6 +947,7 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
     if (s->hbm_budget_bytes < 0 || s->max_requests_per_launch < 0) return fail(LUMRAD_EINVAL, "negative limit");
     if (s->device_loop != 0 && s->device_loop != 1) return fail(LUMRAD_EINVAL, "device_loop must be 0 or 1");
     if (!(s->poll_ms >= 0.0f && s->poll_ms <= 1000.0f)) return fail(LUMRAD_EINVAL, "poll_ms must be in [0, 1000]");
+    if (!(s->max_queue_ms >= 0.0f && s->max_queue_ms <= 3.6e6f)) return fail(LUMRAD_EINVAL, "max_queue_ms must be in [0, 3.6e6]");
     Server* sv = new Server();
     sv->s = *s;
     if (sv->s.max_inflight == 0) sv->s.max_inflight = 4;

@@ -65,3 +65,39 @@ def test_create_without_gpu_reports_device_error():
     with pytest.raises(lum_gb300.LumRadError) as e:
         lum_gb300.RadianceWorld((4, 4, 4))
     assert e.value.code == _native.LUMRAD_EDEVICE
+
+
+def test_ctypes_layouts_match_the_header(tmp_path):
+    """Every struct the binding mirrors has the header's size and field offsets: a C program built
+    against include/lumrad.h prints them (gcc), the ctypes classes must agree."""
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"LumRadSettings": _native.Settings, "LumRadMaterial": _native.Material,
+             "LumRadPassParams": _native.PassParams, "LumRadMeshTransform": _native.MeshTransform,
+             "LumRadPassStats": _native.PassStats, "LumRadTuning": _native.Tuning,
+             "LumRadServerSettings": _native.ServerSettings, "LumRadServerStats": _native.ServerStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lumrad.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        lines.append(f'  printf("{cname} .sizeof %zu\\n", sizeof({cname}));')
+        for f in cls._fields_:
+            lines.append(f'  printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            name, field, value = line.split()
+            got[(name, field)] = int(value)
+    for cname, cls in pairs.items():
+        assert got[(cname, ".sizeof")] == C.sizeof(cls), cname
+        for f in cls._fields_:
+            assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])

@@ -273,3 +273,48 @@ def test_server_with_probes_spanning_ctas():
     srv.close()
     for rw in rws:
         rw.close()
+
+
+@pytest.mark.parametrize("device_loop", [False, True])
+def test_queue_bound_sheds_late_requests(device_loop):
+    """max_queue_ms: requests that waited past the bound when their turn came complete with
+    LUMRAD_ETIMEOUT without running (their edits not applied); every request that ran started within
+    the bound, and the worlds equal a server without the bound that ran only those requests."""
+    import lum_gb300
+    from lum_gb300 import _native as N
+    worlds = _worlds()
+    which = list(range(len(DIMS)))
+    # all due at one moment (50 ms after submission): the queue builds up; the device loop needs
+    # more than its publish window (2 x 64 per lane) to hold requests back on the host
+    reqs = _requests(100 if device_loop else 12, seed=9)
+    bound_ms = 0.3
+    srv, rws = _server(worlds, which, device_loop=device_loop, max_queue_ms=bound_ms)
+    due = srv.now() + 0.05
+    for i, e, r, seed in reqs:
+        srv.submit(i, e, lum_gb300.pass_params(rays=r, max_dist=64.0, blend=0.1, time_seed=seed), due)
+    srv.run(timeout_s=300)
+    done = srv.poll(len(reqs) + 8)
+    assert len(done) == len(reqs)
+    ok = done[done["status"] == 0]
+    shed = done[done["status"] == N.LUMRAD_ETIMEOUT]
+    assert len(ok) + len(shed) == len(reqs)
+    assert len(ok) >= len(which) and len(shed) > 0
+    assert srv.stats()["shed"] == len(shed)
+    assert (ok["start_s"] - ok["arrival_s"] <= bound_ms * 1e-3 + 1e-4).all()
+    got = [srv.get_radiance(k) for k in which]
+    srv.close()
+    for rw in rws:
+        rw.close()
+    ran = set(ok["request"].tolist())
+    ref, rrws = _server(worlds, which)
+    # the same submission order, only the requests that ran (ids are 0, 1, ... in submission order)
+    kept = [q for rid, q in enumerate(reqs) if rid in ran]
+    _submit(ref, kept, which)
+    ref.run(timeout_s=300)
+    d2 = ref.poll(len(kept) + 8)
+    assert len(d2) == len(kept) and (d2["status"] == 0).all()
+    for k in which:
+        assert ref.get_radiance(k).tobytes() == got[k].tobytes(), k
+    ref.close()
+    for rw in rrws:
+        rw.close()
