@@ -8,6 +8,7 @@ namespace lumrad {
 constexpr int kDevBatch = 64;          // requests (of distinct worlds) per loop iteration
 constexpr int kDevMaxWorlds = 1024;    // worlds a device-loop server can hold
 constexpr int kDevChunk = 1024;        // cells per chunk of the dirty-list scan
+constexpr int kDevDefer = 256;         // requests taken from the ring and held for a later iteration
 
 // One request in the host-written ring (page-locked, read by the loop's admit kernel).
 struct DevRequest {
@@ -43,7 +44,7 @@ struct DevLoop {
     const DevRequest* ring;
     long long ring_cap;
     const long long* head;             // requests published by the host
-    volatile long long* tail_host;     // requests completed (the host may reuse their slots and edits)
+    volatile long long* tail_host;     // ring entries taken (run or held back; the slots may be reused)
     const LumRadEdit* edits;
     long long edit_cap;
     DevCompletion* done;               // completion ring (ring_cap entries)
@@ -58,6 +59,10 @@ struct DevLoop {
     unsigned long long* queue;         // the march kernel's task queue
     int* chunk_count;                  // per chunk of the batch's worlds (capacity: every world's chunks)
     int* chunk_off;
+    // requests taken from the ring whose world already had a request in that iteration's batch,
+    // oldest first; the next iteration's admit takes from them before the ring
+    DevRequest deferred[kDevDefer];
+    int n_deferred, pad2;
     // per iteration
     long long tail;                    // next ring entry to admit
     unsigned long long iteration;      // starts at 1

@@ -29,6 +29,7 @@
 #include <deque>
 #include <memory>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 namespace lumrad {
@@ -528,14 +529,18 @@ struct DevLane {
     DevRequest* ring = nullptr;          // page-locked, mapped (host pointers; the device's below)
     LumRadEdit* edits = nullptr;
     DevCompletion* done = nullptr;
-    long long* ctl = nullptr;            // [0] head, [1] tail (completed), [2] done head, [3] stop
+    long long* ctl = nullptr;            // [0] head, [1] tail (taken by the loop), [2] done head, [3] stop
     DevRequest* d_ring = nullptr;
     LumRadEdit* d_edits = nullptr;
     DevCompletion* d_done = nullptr;
     long long* d_ctl = nullptr;
     long long head = 0, done_read = 0, edit_head = 0, edit_tail = 0;
-    std::deque<long long> edit_ends;     // arena position after each published request's edits
-    std::deque<Published> published;     // published, not yet completed (ring order)
+    // published, not yet completed, by id (the loop completes a request in the iteration that runs
+    // it, and holds back a request whose world is already in that iteration's batch); and the ids
+    // in publish order with each one's arena position after its edits (the arena is freed up to
+    // the oldest request not completed)
+    std::unordered_map<long long, Published> published;
+    std::deque<std::pair<long long, long long>> pub_order;
     DevLoop* d_loop = nullptr;
     int* d_chunk_count = nullptr;
     int* d_chunk_off = nullptr;
@@ -768,12 +773,14 @@ int devloop_progress(Server* sv) {
         std::atomic_thread_fence(std::memory_order_acquire);
         for (; ln.done_read < dh; ln.done_read++) {
             const DevCompletion& c = ln.done[ln.done_read % dl.ring_cap];
-            const DevLane::Published pr = ln.published.front();
-            ln.published.pop_front();
+            const auto it = ln.published.find(c.id);
+            if (it == ln.published.end()) return fail(LUMRAD_EDEVICE, "the device loop completed an unknown request");
+            const DevLane::Published pr = it->second;
+            ln.published.erase(it);
             LumRadCompletion o{};
             o.request = pr.id;
             o.world = pr.world;
-            o.status = c.id == pr.id ? c.status : LUMRAD_EDEVICE;
+            o.status = c.status;
             o.probes = c.probes;
             o.rays_per_probe = pr.rays;
             o.arrival_s = pr.arrival;
@@ -785,8 +792,10 @@ int devloop_progress(Server* sv) {
             sv->st.requests++;
             sv->st.probes += (unsigned long long)c.probes;
             sv->st.rays += (unsigned long long)c.probes * (unsigned long long)pr.rays;
-            ln.edit_tail = ln.edit_ends.front();
-            ln.edit_ends.pop_front();
+        }
+        while (!ln.pub_order.empty() && !ln.published.count(ln.pub_order.front().first)) {
+            ln.edit_tail = ln.pub_order.front().second;
+            ln.pub_order.pop_front();
         }
     }
     // due requests into their lanes' rings, in submission order.  With a queueing bound a lane
@@ -820,8 +829,8 @@ int devloop_progress(Server* sv) {
         q.max_dist = r.p.max_dist;
         q.blend = r.p.blend;
         ln.edit_head += ne;
-        ln.edit_ends.push_back(ln.edit_head);
-        ln.published.push_back(DevLane::Published{r.id, r.world, r.p.rays_per_probe, r.arrival, now});
+        ln.pub_order.emplace_back(r.id, ln.edit_head);
+        ln.published.emplace(r.id, DevLane::Published{r.id, r.world, r.p.rays_per_probe, r.arrival, now});
         dl.outstanding[r.world]++;
         ln.head++;
         published[r.world % kDevLanes] = true;

@@ -54,34 +54,48 @@ __device__ __forceinline__ int batch_of(const long long* base, int n, long long 
     return lo;
 }
 
+// The iteration's batch: requests of distinct worlds, oldest first, from the held-back requests
+// and then the ring.  A request whose world already has one in the batch is held back (not a
+// reason to stop: the batch goes on with other worlds' requests, as the host loop's launches do),
+// and one past the ray buffer's task bound ends the batch.  One warp: ring entries (page-locked
+// host memory) are fetched 32 at a time into shared memory; lane 0 forms the batch.
 __global__ void admit_kernel(DevLoop* L, cudaGraphConditionalHandle cond) {
     __shared__ unsigned seen[kDevMaxWorlds / 32];
-    for (int i = threadIdx.x; i < kDevMaxWorlds / 32; i += blockDim.x) seen[i] = 0;
-    __syncwarp();
-    if (threadIdx.x != 0) return;
+    __shared__ DevRequest s_buf[32];
+    const int lane = threadIdx.x;
+    for (int i = lane; i < kDevMaxWorlds / 32; i += blockDim.x) seen[i] = 0;
     const long long tail = L->tail;
-    long long head = load_acquire_sys(L->head);
-    const unsigned long long t0 = globaltimer_ns();
-    int stop = load_relaxed_sys(L->stop);
-    // a bounded wait for the host's next request (the loop ends when it runs out)
-    while (head == tail && !stop && globaltimer_ns() - t0 < L->poll_ns) {
-        __nanosleep(256);
+    const int n_def = L->n_deferred;
+    long long head = 0;
+    int stop = 0;
+    if (lane == 0) {
         head = load_acquire_sys(L->head);
+        const unsigned long long t0 = globaltimer_ns();
         stop = load_relaxed_sys(L->stop);
+        // a bounded wait for the host's next request (the loop ends when it runs out)
+        while (n_def == 0 && head == tail && !stop && globaltimer_ns() - t0 < L->poll_ns) {
+            __nanosleep(256);
+            head = load_acquire_sys(L->head);
+            stop = load_relaxed_sys(L->stop);
+        }
     }
-    int n = 0;
+    head = __shfl_sync(kFull, head, 0);
+    stop = __shfl_sync(kFull, stop, 0);
+    if (lane != 0) (void)load_acquire_sys(L->head);   // each lane's ring reads ordered after the host's publish
+    __syncwarp();
+    int n = 0, m = 0;
     long long tasks = 0, edits = 0, chunks = 0;
-    L->edit_base[0] = 0;
-    L->chunk_base[0] = 0;
-    while (!stop && n < kDevBatch && tail + n < head) {
-        const DevRequest r = L->ring[(tail + n) % L->ring_cap];
+    bool full = stop != 0;
+    // lane 0: 0 = taken into the batch, 1 = held back (world already in the batch), 2 = batch full
+    auto take = [&](const DevRequest& r) -> int {
         const unsigned bit = 1u << (r.world & 31);
-        if (seen[r.world >> 5] & bit) break;   // the world's earlier request is in this batch
+        if (seen[r.world >> 5] & bit) return 1;
+        if (n == kDevBatch) return 2;
         const DevWorld& w = L->worlds[r.world];
         const long long W = (long long)w.pass.X * w.pass.Y * w.pass.Z;
         const long long side = 2LL * L->radius + 1;
         const long long bound = (min(W, (long long)r.n_edits * side * side * side) * (r.rays >> 5) + 7) / 8 * 8;
-        if (n > 0 && tasks + bound > L->max_tasks) break;
+        if (n > 0 && tasks + bound > L->max_tasks) return 2;
         seen[r.world >> 5] |= bit;
         L->batch[n] = r;
         tasks += bound;
@@ -90,12 +104,56 @@ __global__ void admit_kernel(DevLoop* L, cudaGraphConditionalHandle cond) {
         n++;
         L->edit_base[n] = edits;
         L->chunk_base[n] = chunks;
+        return 0;
+    };
+    if (lane == 0) {
+        L->edit_base[0] = 0;
+        L->chunk_base[0] = 0;
+        // held-back requests first (compacted in place, order kept)
+        for (int i = 0; i < n_def; i++) {
+            const DevRequest r = L->deferred[i];
+            const int v = full ? 2 : take(r);
+            if (v == 2) full = true;
+            if (v != 0) L->deferred[m++] = r;
+        }
     }
+    full = __shfl_sync(kFull, full ? 1 : 0, 0) != 0;
+    m = __shfl_sync(kFull, m, 0);
+    // then the ring, 32 entries at a time
+    long long k = 0;
+    while (!full && tail + k < head && m < kDevDefer) {
+        const int avail = (int)min(32LL, head - (tail + k));
+        if (lane < avail) s_buf[lane] = L->ring[(tail + k + lane) % L->ring_cap];
+        __syncwarp();
+        if (lane == 0) {
+            for (int j = 0; j < avail && m < kDevDefer; j++) {
+                const int v = take(s_buf[j]);
+                if (v == 2) {
+                    full = true;
+                    break;
+                }
+                if (v == 1) L->deferred[m++] = s_buf[j];
+                k++;
+            }
+        }
+        full = __shfl_sync(kFull, full ? 1 : 0, 0) != 0;
+        m = __shfl_sync(kFull, m, 0);
+        k = __shfl_sync(kFull, k, 0);
+        __syncwarp();
+    }
+    if (lane != 0) return;
+    L->n_deferred = m;
+    L->tail = tail + k;
     L->n_batch = n;
     L->n_table = n;
     L->total_tasks = 0;
     L->idle = (n == 0);
-    cudaGraphSetConditional(cond, n > 0 ? 1u : 0u);
+    // the taken ring slots may be reused by the host
+    __threadfence_system();
+    *L->tail_host = tail + k;
+    // go on while there is work; a stop ends the loop at once (held-back requests stay for the
+    // next launch)
+    cudaGraphSetConditional(cond, (n > 0 || m > 0) && !stop ? 1u : 0u);
 }
 
 // per edit: the winning-edit stamp and the dirty marks around it
@@ -285,11 +343,9 @@ __global__ void complete_kernel(DevLoop* L) {
         L->queue[0] = 0;
         L->queue[1] = 0;
     }
-    L->tail += n;
     L->iteration++;
     __threadfence_system();
     *L->done_head = d0 + n;
-    *L->tail_host = L->tail;
     __threadfence_system();
 }
 
