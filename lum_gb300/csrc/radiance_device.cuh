@@ -138,22 +138,11 @@ __device__ __forceinline__ MarchView march_view(const WorldPass& w) {
     return MarchView{w.X, w.Y, w.Z, w.cgrid_wide, reinterpret_cast<const uint8_t*>(w.cgrid), w.cbits};
 }
 
-// Compact lookup: compact id of the block (0 iff block id 0) and whether the voxel is solid.
-__device__ __forceinline__ bool solid_at(const MarchView& m, int ix, int iy, int iz, int& cid) {
-    int idx;
-    int c = 0;
-    if (grid_index(m.X, m.Y, m.Z, ix, iy, iz, idx))
-        c = m.wide ? (int)__ldg(reinterpret_cast<const uint16_t*>(m.cgrid) + idx) : (int)__ldg(m.cgrid + idx);
-    cid = c;
-    // the mask's bit x + 16y + 256z, read as the 16-bit row (y, z) of its little-endian words
-    // (fewer index operations than the 32-bit word holding two rows: 1-2% of the pass)
-    const unsigned row = __ldg(reinterpret_cast<const uint16_t*>(m.cbits) + ((c << 8) | ((iz & 15) << 4) | (iy & 15)));
-    return (row >> (ix & 15)) & 1u;
-}
-
-// The same with the compact id's width known at compile time (WIDE: uint16 ids, else uint8), on
-// the compact grid `cg` and the masks' 16-bit rows `rows`, in global memory (read through the
-// read-only path) or, SMEM, staged in shared memory.
+// Compact lookup: compact id of the block (0 iff block id 0) and whether the voxel is solid (the
+// mask's bit x + 16y + 256z, read as the 16-bit row (y, z) of its little-endian words: fewer index
+// operations than the 32-bit word holding two rows), with the compact id's width known at
+// compile time (WIDE: uint16 ids, else uint8), on the compact grid `cg` and the masks' 16-bit rows
+// `rows`, in global memory (read through the read-only path) or, SMEM, staged in shared memory.
 template <bool WIDE, bool SMEM>
 __device__ __forceinline__ bool solid_at_p(const uint8_t* cg, const uint16_t* rows, int X, int Y, int Z, int ix,
                                            int iy, int iz, int& cid) {
@@ -293,8 +282,9 @@ __device__ __forceinline__ float3 sample_trilinear(const WorldPass& w, float ux,
 // miss) reads no radiance volume; shade_hit (the trilinear taps of the previous volume) does.  A
 // pass's finalize launch may run the first part while the previous pass still writes the volume.
 // Returns whether the ray hit; a miss's light is in `light`, a hit's tap coordinates in u and its
-// material in m.
-template <bool RECORD>
+// material in m.  WIDE: the compact ids' width (the caller branches on it once per warp: 3% of the
+// finalize's instructions against testing it at every lookup).
+template <bool RECORD, bool WIDE>
 __device__ __forceinline__ bool finalize_ray(const WorldPass& w, const MarchView& mv, float3 o, float3 d,
                                              float coarse_frac, uint32_t info, int block, long long gr,
                                              uint32_t& lookups, float3& light, float3& u, float4& m) {
@@ -329,7 +319,7 @@ __device__ __forceinline__ bool finalize_ray(const WorldPass& w, const MarchView
         const float tdx = fabsf(ivx), tdy = fabsf(ivy), tdz = fabsf(ivz);   // 1/|d| == |1/d|
         int vx = f2i(bhx), vy = f2i(bhy), vz = f2i(bhz);
         int cid;
-        bool solid = solid_at(mv, vx, vy, vz, cid);
+        bool solid = solid_at_w<WIDE>(mv, vx, vy, vz, cid);
         float fsx = 0.0f, fsy = 0.0f, fsz = 0.0f;
         int it = 0;
         while (it < 5 && !solid) {
@@ -341,7 +331,7 @@ __device__ __forceinline__ bool finalize_ray(const WorldPass& w, const MarchView
             tmx = fadd(tmx, fmul(tdx, fsx));
             tmy = fadd(tmy, fmul(tdy, fsy));
             tmz = fadd(tmz, fmul(tdz, fsz));
-            solid = solid_at(mv, vx, vy, vz, cid);
+            solid = solid_at_w<WIDE>(mv, vx, vy, vz, cid);
             it++;
         }
         lookups += 1 + it;

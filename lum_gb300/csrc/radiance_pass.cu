@@ -524,8 +524,11 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
         uint32_t lookups;
         float3 L, u;
         float4 m;
-        const bool hit = finalize_ray<RECORD>(*wp, march_view(*wp), o, d, __uint_as_float(res.x), res.y, blk,
-                                              (long long)t_local * kTaskRays + lane, lookups, L, u, m);
+        const MarchView mv = march_view(*wp);
+        const float fc = __uint_as_float(res.x);
+        const long long gr = (long long)t_local * kTaskRays + lane;
+        const bool hit = mv.wide ? finalize_ray<RECORD, true>(*wp, mv, o, d, fc, res.y, blk, gr, lookups, L, u, m)
+                                 : finalize_ray<RECORD, false>(*wp, mv, o, d, fc, res.y, blk, gr, lookups, L, u, m);
         grid_dependency_wait();   // from here on the volumes: the previous pass's launch has finished
         if (hit) L = shade_hit<Store>(*wp, u, m);
         L = butterfly_sum(L);
