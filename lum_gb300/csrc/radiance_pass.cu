@@ -4,7 +4,8 @@
 // kernels per round of up to kChunkTasks tasks (a task = one 32-ray subgroup of one probe):
 //
 //   march_kernel     persistent warps take tasks from a queue in guided chunks (large early,
-//                    single tasks at the end).  A warp sets up a task's 32 rays in lock step
+//                    single tasks at the end; through a shared-memory block per CTA when the
+//                    launch has few tasks per warp).  A warp sets up a task's 32 rays in lock step
 //                    (hash seeds, direction, origin, 1/direction) into a 32-ray ring in shared
 //                    memory.  Its lanes march in a flat loop, two coarse steps per iteration; a
 //                    lane whose ray ends writes (fraction, info) and takes the next ray in ring
@@ -19,10 +20,14 @@
 //                    counter.  Lookup and hit counters are summed per CTA.
 //
 // Several passes of one context (launch_passes): one march launch over all their tasks (the
-// traversal does not read the radiance volume), then each pass's finalize in order.
+// traversal does not read the radiance volume), then each pass's finalize in order, each launched
+// as a programmatic dependent of the one before (its volume-free work runs in that one's tail).
+// The pass start (next = prev, counters cleared) runs inside the launches, not as copies between
+// them; a pass call right after another starts its march in the previous finalize's tail.
 //
 // Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
-// world (uint8 ids + occupancy bits, L1-resident); between the kernels each ray keeps 8 B
+// world (uint8 ids + occupancy bits, L1-resident; staged in shared memory by the march of a launch
+// over one world that fits); between the kernels each ray keeps 8 B
 // (coarse fraction, info word): 67 MB for a single pass's round of 2^18 tasks (L2-resident),
 // up to 134 MB for several passes, 268 MB for a batch's round of 2^20.
 
