@@ -11,7 +11,8 @@ Workload (one "step"): the 64x64x16-block terrain world plus 2000 random blocks 
              between steps, outside the timed region.
   single_pass  the same step as 8 lumrad_radiance_pass_resident calls (one frame's update each).
   e2e        the same metric through the C ABI with host buffers: each step copies its 8 request
-             lists host->device (lumrad_radiance_passes) and reads the radiance volume back.
+             lists host->device (lumrad_radiance_passes, the lists back to back in one page-locked
+             array) and reads the radiance volume back.
   roofline   the bound that limits the step's kernels (march + 8 finalize launches): instruction
              issue.  achieved = warp instructions per step (ncu's smsp__inst_executed.sum over the
              same 9 launches, NCU_WARP_INST_PER_STEP) / the kernels' own duration (the span of
@@ -772,19 +773,20 @@ def main():
     # the caller's request lists (back to back in one array) and result buffer in page-locked
     # host memory
     pinned = torch.from_numpy(np.concatenate(lists)).pin_memory()
-    cuts = np.cumsum([0] + [l.shape[0] for l in lists])
-    host_lists = [pinned.numpy()[cuts[i]:cuts[i + 1]] for i in range(PASSES)]
+    host_lists = pinned.numpy()                       # the 8 lists back to back
+    counts = [l.shape[0] for l in lists]
+    pparams = (lum_gb300.PassParams * PASSES)(*plist)
     out_t = torch.empty(world.grid.shape + (3,), dtype=torch.float32).pin_memory()
     host_out = out_t.numpy()
     for _ in range(max(1, args.warmup)):
-        rw2.radiance_passes(host_lists, plist)
+        rw2.radiance_passes_packed(host_lists, counts, pparams)
         rw2.get_radiance(out=host_out)
     e2e_s = 0.0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rw2.radiance_passes(host_lists, plist)
+        rw2.radiance_passes_packed(host_lists, counts, pparams)
         rw2.get_radiance(out=host_out)
         e2e_s += time.perf_counter() - t0
     e2e_value = job_value(args.steps * rays_per_step, world_size, max_over_ranks(e2e_s, pg, dev))

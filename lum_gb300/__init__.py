@@ -213,13 +213,44 @@ class RadianceWorld:
 
     def radiance_passes(self, lists, params) -> None:
         """Passes over int16 (n, 4) lists in order, as radiance_pass over each would run them;
-        their marches share launches."""
-        reqs = [np.ascontiguousarray(r, dtype=np.int16).reshape(-1, 4) for r in lists]
-        n = len(reqs)
-        ptrs = (C.c_void_p * max(n, 1))(*[r.ctypes.data for r in reqs])
-        counts = (C.c_int * max(n, 1))(*[r.shape[0] for r in reqs])
-        ps = (PassParams * max(n, 1))(*params)
+        their marches share launches.  Lists that already are C-contiguous int16 (n, 4) arrays are
+        passed as they are (the call's own cost sits before the GPU's first launch)."""
+        n = len(lists)
+        ptrs = (C.c_void_p * max(n, 1))()
+        counts = (C.c_int * max(n, 1))()
+        keep = []
+        for i, r in enumerate(lists):
+            if not (type(r) is np.ndarray and r.dtype == np.int16 and r.ndim == 2 and r.shape[1] == 4
+                    and r.flags.c_contiguous):
+                r = np.ascontiguousarray(r, dtype=np.int16).reshape(-1, 4)
+                keep.append(r)
+            ptrs[i] = r.__array_interface__["data"][0]
+            counts[i] = r.shape[0]
+        ps = params if isinstance(params, C.Array) else (PassParams * max(n, 1))(*params)
         check(self.lib.lumrad_radiance_passes(self.h, ptrs, counts, ps, n))
+
+    def radiance_passes_packed(self, requests: np.ndarray, counts, params) -> None:
+        """radiance_passes over lists stored back to back in one C-contiguous int16 (total, 4)
+        array: list i is the next counts[i] rows.  One pointer lookup instead of one per list
+        (a page-locked array is copied straight from, as one run)."""
+        if not (type(requests) is np.ndarray and requests.dtype == np.int16 and requests.ndim == 2
+                and requests.shape[1] == 4 and requests.flags.c_contiguous):
+            raise ValueError("requests must be a C-contiguous int16 (total, 4) array")
+        n = len(counts)
+        ptrs = (C.c_void_p * max(n, 1))()
+        cts = (C.c_int * max(n, 1))()
+        base, off = requests.ctypes.data, 0
+        for i, c in enumerate(counts):
+            c = int(c)
+            if c < 0:
+                raise ValueError("counts must be non-negative")
+            ptrs[i] = base + 8 * off
+            cts[i] = c
+            off += c
+        if off != requests.shape[0]:
+            raise ValueError("counts must add up to the rows of requests")
+        ps = params if isinstance(params, C.Array) else (PassParams * max(n, 1))(*params)
+        check(self.lib.lumrad_radiance_passes(self.h, ptrs, cts, ps, n))
 
     def radiance_passes_resident(self, slots, params) -> None:
         n = len(slots)

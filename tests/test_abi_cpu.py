@@ -4,6 +4,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 import lum_gb300
@@ -101,3 +102,26 @@ def test_ctypes_layouts_match_the_header(tmp_path):
         assert got[(cname, ".sizeof")] == C.sizeof(cls), cname
         for f in cls._fields_:
             assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])
+
+
+def test_packed_lists_are_checked_before_any_call():
+    """radiance_passes_packed rejects a non-int16 or non-(n, 4) array and counts that do not add up
+    to its rows, before it reaches the library (no GPU needed)."""
+    rw = lum_gb300.RadianceWorld.__new__(lum_gb300.RadianceWorld)
+
+    class NoCall:
+        def lumrad_radiance_passes(self, *a):
+            raise AssertionError("the library must not be called")
+
+    rw.lib = NoCall()
+    rw.h = None
+    p = [lum_gb300.pass_params(rays=64)] * 2
+    good = np.zeros((5, 4), np.int16)
+    with pytest.raises(ValueError):
+        rw.radiance_passes_packed(good.astype(np.int32), [2, 3], p)
+    with pytest.raises(ValueError):
+        rw.radiance_passes_packed(np.zeros((5, 3), np.int16), [2, 3], p)
+    with pytest.raises(ValueError):
+        rw.radiance_passes_packed(good, [2, 2], p)
+    with pytest.raises(ValueError):
+        rw.radiance_passes_packed(good, [6, -1], p)

@@ -267,3 +267,30 @@ def test_kernel_times_from_device_timestamps():
         assert (kt[:3] > 0.0).all() and kt[3] == 0.0 and kt[4] > 0.0
         assert (kt < 1000.0).all()
         assert rw.pass_stats()["gpu_ms"] > 0.0
+
+
+def test_packed_lists_equal_separate_lists():
+    """radiance_passes_packed (lists back to back in one array, a zero-length one among them, in
+    page-locked memory or not) equals radiance_passes over the separate lists, bit for bit."""
+    import torch
+    import lum_gb300
+    w = worldgen.terrain_world((9, 8, 6), seed=60, n_types=10)
+    lists = [worldgen.probe_subset(w.dims, f, seed=61, stream=i) for i, f in enumerate((0.4, 0.0, 0.7, 0.3))]
+    lists[1] = lists[1][:0]
+    params = [lum_gb300.pass_params(rays=(64, 32, 128, 64)[i], blend=0.1, time_seed=70 + i) for i in range(4)]
+    packed = np.ascontiguousarray(np.concatenate(lists))
+    counts = [l.shape[0] for l in lists]
+    out = []
+    for mode in ("lists", "packed", "packed-pinned"):
+        with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+            rw.load(w)
+            if mode == "lists":
+                rw.radiance_passes(lists, params)
+            elif mode == "packed":
+                rw.radiance_passes_packed(packed, counts, params)
+            else:
+                pinned = torch.from_numpy(packed.copy()).pin_memory()
+                rw.radiance_passes_packed(pinned.numpy(), counts, (lum_gb300.PassParams * 4)(*params))
+            out.append(rw.get_radiance())
+    assert out[1].tobytes() == out[0].tobytes()
+    assert out[2].tobytes() == out[0].tobytes()
