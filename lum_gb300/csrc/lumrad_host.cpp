@@ -249,7 +249,7 @@ int DeviceWorld::ensure_dirs(int R, cudaStream_t stream, const float4** out) {
     return LUMRAD_OK;
 }
 
-int DeviceWorld::ensure_scratch(size_t groups, int R) {
+int DeviceWorld::ensure_scratch(size_t groups, int R, cudaStream_t stream) {
     const size_t nsub = (size_t)(R / 32);
     if (groups * nsub > scratch_cap) {
         cudaFree(d_scratch);
@@ -267,7 +267,9 @@ int DeviceWorld::ensure_scratch(size_t groups, int R) {
         const size_t cap = std::max<size_t>(groups, 1024);
         uploads++;
         LUMRAD_TRY(cudaMalloc(&d_probe_count, cap * sizeof(int)));
-        LUMRAD_TRY(cudaMemset(d_probe_count, 0, cap * sizeof(int)));
+        // zeroed in order on the pass's stream (a plain memset runs on the default stream, which
+        // a non-blocking stream does not wait for)
+        LUMRAD_TRY(cudaMemsetAsync(d_probe_count, 0, cap * sizeof(int), stream));
         count_cap = cap;
     }
     return LUMRAD_OK;
@@ -308,7 +310,7 @@ int DeviceWorld::fill_pass(const short4* d_req, int n, const LumRadPassParams& p
     const int R = p.rays_per_probe;
     const int groups = n / p.size;
     if ((long long)groups * (R / 32) >= (1LL << 31)) return fail(LUMRAD_EINVAL, "pass has too many subgroups (>= 2^31)");
-    if ((rc = ensure_scratch((size_t)std::max(groups, 1), R))) return rc;
+    if ((rc = ensure_scratch((size_t)std::max(groups, 1), R, stream))) return rc;
     if (p.record_hits && (rc = ensure_hits((size_t)groups * R))) return rc;
     WorldPass& w = *out;
     std::memset(&w, 0, sizeof w);
@@ -525,6 +527,7 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     int rc = world.sync_inputs(stream);
     if (rc) return rc;
     if (!d_pass_mask) {   // zero between calls (the last finalize of each group clears its mask)
+        world.uploads++;   // the zeroing below precedes the march: no launch may overlap it
         LUMRAD_TRY(cudaMalloc(&d_pass_mask, (size_t)world.W * sizeof(uint32_t)));
         LUMRAD_TRY(cudaMalloc(&d_pass_mask2, (size_t)world.W * sizeof(uint32_t)));
         LUMRAD_TRY(cudaMemsetAsync(d_pass_mask, 0, (size_t)world.W * sizeof(uint32_t), stream));

@@ -257,7 +257,7 @@ void complete_now(Server* sv, const SRequest& r, int status) {
 
 // Per-pass buffers of a world at their size for 256 rays, so the serving loop never reallocates them.
 int prepare_world(DeviceWorld& dw, cudaStream_t stream) {
-    int rc = dw.ensure_scratch(dw.W, 256);
+    int rc = dw.ensure_scratch(dw.W, 256, stream);
     if (rc) return rc;
     for (int R : {32, 64, 128, 256}) {
         const float4* d = nullptr;

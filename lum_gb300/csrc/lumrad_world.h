@@ -121,7 +121,7 @@ struct DeviceWorld {
     size_t footprint() const;
     int sync_inputs(cudaStream_t stream);
     int ensure_dirs(int R, cudaStream_t stream, const float4** out);
-    int ensure_scratch(size_t groups, int R);
+    int ensure_scratch(size_t groups, int R, cudaStream_t stream);
     int ensure_hits(size_t n);
     int prepare_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, LaunchArgs* la);
     int fill_pass(const short4* d_req, int n, const LumRadPassParams& p, cudaStream_t stream, WorldPass* out);
