@@ -225,9 +225,10 @@ int  lumrad_get_pass_stats(LumRadContext ctx, LumRadPassStats* out);
 int  lumrad_get_stream(LumRadContext ctx, void** stream);
 /* Device times (ms) of the last min(cap, 64) passes, oldest first; *n = number written.  Each is
  * the span from the start of the pass's first kernel to the end of its last, from %globaltimer
- * timestamps those kernels write (0 for a pass without kernels).  A pass call that follows another
- * pass call on the context (no other call between them, no upload) starts its march while the
- * previous pass's last kernel finishes, so consecutive spans may overlap.  Synchronises. */
+ * timestamps those kernels write (0 for a pass without kernels).  A one-pass call over a resident
+ * list (lumrad_radiance_pass_resident) right after another pass call on the context (no other call
+ * between them, no upload) starts its march while the previous pass's last kernel finishes, so
+ * consecutive spans may overlap.  Synchronises. */
 int  lumrad_get_kernel_times(LumRadContext ctx, float* ms, int cap, int* n);
 
 /* ---- producers: voxel models blockified into the world (blockify + map) ---------------------

@@ -537,8 +537,9 @@ int Context::run_passes(const short4* const* reqs, const int* ns, const LumRadPa
     timed[slot] = false;
     bool first = true;   // the first launch clears the counters and starts the kernel time
     bool ends_in_finalize = false;   // the call's last operation is a finalize launch
-    // the first march may start in the previous pass's finalize tail: see pass_mark
-    bool dependent = pass_mark == api_calls - 1 && uploads_mark == world.uploads;
+    // (the march here follows the pass table's copy, so it never starts in the previous pass's
+    // finalize tail; the ray buffer and the pass mask still alternate, for the pass call after it)
+    bool dependent = false;
     const int side = ray_side;   // this call's ray buffer (the previous pass's finalize reads the other)
     ray_side ^= 1;
     const size_t vol_bytes = (size_t)world.W * world.rad_stride;

@@ -23,7 +23,8 @@
 // traversal does not read the radiance volume), then each pass's finalize in order, each launched
 // as a programmatic dependent of the one before (its volume-free work runs in that one's tail).
 // The pass start (next = prev, counters cleared) runs inside the launches, not as copies between
-// them; a pass call right after another starts its march in the previous finalize's tail.
+// them; a one-pass call right after another pass call starts its march in the previous
+// finalize's tail.
 //
 // Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
 // world (uint8 ids + occupancy bits, L1-resident; staged in shared memory by the march of a launch
