@@ -294,3 +294,33 @@ def test_packed_lists_equal_separate_lists():
             out.append(rw.get_radiance())
     assert out[1].tobytes() == out[0].tobytes()
     assert out[2].tobytes() == out[0].tobytes()
+
+
+def test_update_radiance_between_dependent_passes():
+    """Frames of lumrad_update_radiance (the list built on the device) between one-pass calls over
+    resident lists, back to back, equal the same calls each followed by a synchronisation."""
+    import lum_gb300
+    w = worldgen.terrain_world((14, 12, 6), seed=62, n_types=12)
+    lists = [worldgen.probe_subset(w.dims, f, seed=63, stream=i) for i, f in enumerate((0.3, 0.5, 0.2))]
+    prev = random_prev(w, seed=64)
+
+    def run(sync):
+        with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+            rw.load(w)
+            rw.set_radiance(prev)
+            for i, l in enumerate(lists):
+                rw.upload_requests(i, l)
+            steps = []
+            for k in range(3):
+                steps.append(lambda k=k: rw.radiance_pass_resident(k, lum_gb300.pass_params(rays=64, blend=0.2,
+                                                                                              time_seed=10 + k)))
+                steps.append(lambda k=k: rw.update_radiance(lum_gb300.pass_params(rays=32, blend=0.1,
+                                                                                  time_seed=20 + k)))
+            steps.append(lambda: rw.radiance_pass_resident(0, lum_gb300.pass_params(rays=128, time_seed=30)))
+            for f in steps:
+                f()
+                if sync:
+                    rw.synchronize()
+            return rw.get_radiance()
+
+    assert run(False).tobytes() == run(True).tobytes()
