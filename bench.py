@@ -59,15 +59,16 @@ SEED = 1234
 S_R = 12            # bytes of FP32 RGB radiance per probe
 BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
-# finalize launches, whose extra CTAs copy each pass's unlisted probes) in an ncu capture of this
-# workload; ncu replays with cold caches (march 1.87 + 46.95 MB, finalizes 120.37 + 0.00 MB)
-NCU_DRAM_BYTES_PER_STEP = 169.19e6
-# L2 bytes (lts__t_bytes.sum) of the same 9 launches in the same capture (march 453.7 MB: its world
-# lookups are shared-memory loads, finalizes 1,016.6 MB)
-NCU_L2_BYTES_PER_STEP = 1470.3e6
-# Warp instructions (smsp__inst_executed.sum) of the same 9 launches: the march over the 8 passes
-# (462.6 M) and the 8 finalize launches (411.6 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 462.6e6 + 411.6e6
+# finalize launches, whose extra CTAs copy each pass's unlisted probes) in ncu captures of this
+# workload (the march's launch, and 3 of the 8 finalize launches scaled to 8); ncu replays with cold
+# caches (march 1.83 + 47.05 MB, finalizes 120.42 + 0.00 MB)
+NCU_DRAM_BYTES_PER_STEP = 169.30e6
+# L2 bytes (lts__t_bytes.sum) of the same launches in the same captures (march 454.6 MB: its world
+# lookups are shared-memory loads, finalizes 845.9 MB)
+NCU_L2_BYTES_PER_STEP = 1300.5e6
+# Warp instructions (smsp__inst_executed.sum) of the same launches: the march over the 8 passes
+# (462.6 M) and the 8 finalize launches (404.1 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 462.6e6 + 404.1e6
 SCHEDULERS_PER_SM = 4
 
 
