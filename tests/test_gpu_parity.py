@@ -141,3 +141,54 @@ def test_rgb10a2_storage_matches_oracle(rays, odd):
             assert_hits_equal(rw.get_hits(), ref_hits)
             got = rw.get_radiance()
             assert got.tobytes() == ref.tobytes(), (s, np.abs(got - ref).max())
+
+
+def test_more_than_256_block_ids():
+    """A world with ~280 distinct block ids: compact ids are 16-bit (the march's and the refine's
+    wide forms; more than 256 masks never fit shared memory beside the rays' rings, so the world is
+    read through L1).  Hit records bit-exact and radiance within 1e-5 against the oracle, over two
+    chained passes."""
+    w = worldgen.terrain_world((16, 16, 8), seed=33, n_types=300)
+    assert len(np.unique(w.grid)) > 257
+    prev = random_prev(w)
+    req = worldgen.all_probes(w.dims)
+    got, hits, _ = gpu_pass(w, req, prev, passes=2, seeds=[3, 4], rays=64, max_dist=160.0, blend=0.2)
+    ref, ref_hits, _ = oracle_pass(w, req, prev, passes=2, seeds=[3, 4], rays=64, max_dist=160.0, blend=0.2)
+    assert_hits_equal(hits, ref_hits)
+    assert rel_err(got, ref).max() <= RTOL
+
+
+def test_more_than_256_block_ids_in_several_passes_and_a_batch():
+    """The same wide world through one several-pass call and inside a batch (the unstaged march):
+    equal to single passes, bit for bit."""
+    import lum_gb300
+    w = worldgen.terrain_world((16, 16, 8), seed=34, n_types=300)
+    other = worldgen.terrain_world((6, 5, 4), seed=35, n_types=8)
+    lists = [worldgen.probe_subset(w.dims, f, seed=36, stream=i) for i, f in enumerate((0.5, 0.3))]
+    params = [lum_gb300.pass_params(rays=64, max_dist=96.0, blend=0.1, time_seed=40 + i) for i in range(2)]
+    prev = random_prev(w)
+
+    def world(x):
+        rw = lum_gb300.RadianceWorld(x.dims, max_block_types=x.palette.shape[0])
+        rw.load(x)
+        return rw
+
+    with world(w) as a, world(w) as b:
+        a.set_radiance(prev)
+        b.set_radiance(prev)
+        for l, p in zip(lists, params):
+            a.radiance_pass(l, p)
+        b.radiance_passes(lists, params)
+        single = a.get_radiance()
+        assert b.get_radiance().tobytes() == single.tobytes()
+    with world(w) as c, world(other) as d:
+        c.set_radiance(prev)
+        with lum_gb300.RadianceBatch([c, d]) as bt:
+            bt.set_requests(0, lists[0], params[0])
+            bt.set_requests(1, worldgen.all_probes(other.dims), lum_gb300.pass_params(rays=32))
+            bt.run(params[0].time_seed)
+            bt.synchronize()
+        with world(w) as e:
+            e.set_radiance(prev)
+            e.radiance_pass(lists[0], params[0])
+            assert c.get_radiance().tobytes() == e.get_radiance().tobytes()
