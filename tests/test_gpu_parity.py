@@ -192,3 +192,27 @@ def test_more_than_256_block_ids_in_several_passes_and_a_batch():
             e.set_radiance(prev)
             e.radiance_pass(lists[0], params[0])
             assert c.get_radiance().tobytes() == e.get_radiance().tobytes()
+
+
+def test_more_than_256_block_ids_staged():
+    """A world small enough that 16-bit compact ids for 258 ids (257 block ids and air) still fit
+    shared memory beside the rays' rings (9x9x4 blocks): the staged wide march, without hit
+    records, against the oracle within 1e-5, and equal to the recording (unstaged) pass."""
+    import lum_gb300
+    base = worldgen.terrain_world((9, 9, 4), seed=37, n_types=257)
+    g = np.zeros(9 * 9 * 4, np.int16)
+    g[:257] = np.arange(1, 258, dtype=np.int16)
+    g = g[worldgen.randint(38, 1, g.size, 0, 1 << 30).argsort(kind="stable")]
+    w = worldgen.World(grid=g.reshape(4, 9, 9), palette=base.palette, materials=base.materials)
+    prev = random_prev(w)
+    req = worldgen.all_probes(w.dims)
+    params = dict(rays=64, max_dist=96.0, blend=0.2, time_seed=5)
+    with lum_gb300.RadianceWorld(w.dims, max_block_types=w.palette.shape[0]) as rw:
+        rw.load(w)
+        rw.set_radiance(prev)
+        rw.radiance_pass(req, lum_gb300.pass_params(**params))
+        got = rw.get_radiance()
+    ref, _, _ = oracle_pass(w, req, prev, **params)
+    assert rel_err(got, ref).max() <= RTOL
+    rec, _, _ = gpu_pass(w, req, prev, **params)
+    assert rec.tobytes() == got.tobytes()
