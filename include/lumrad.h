@@ -271,7 +271,9 @@ int  lumrad_get_block_palette(LumRadContext ctx, uint8_t* voxels);
 typedef void* LumRadBatch;
 
 /* Scheduling of the march queue: a warp claims remaining/(guided_div*warps) tasks at a time,
- * at most max_chunk; march_ctas CTAs per SM (0 = as many as fit).  pass_ms: autotune's timing. */
+ * at most max_chunk (0 = the default; at most LUMRAD_MAX_CHUNK, else LUMRAD_EINVAL); march_ctas
+ * CTAs per SM (0 = as many as fit).  pass_ms: autotune's timing. */
+#define LUMRAD_MAX_CHUNK 4095
 typedef struct {
     int   guided_div;
     int   max_chunk;

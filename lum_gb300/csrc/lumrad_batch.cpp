@@ -331,6 +331,8 @@ int lumrad_batch_set_tuning(LumRadBatch batch, const LumRadTuning* t) {
     Batch* b = as_batch(batch);
     if (!b || !t) return fail(LUMRAD_EINVAL, "null argument");
     if (t->guided_div < 0 || t->max_chunk < 0 || t->march_ctas < 0) return fail(LUMRAD_EINVAL, "negative tuning value");
+    // a claimed chunk carries its task count in 12 bits (the march kernel's queue words)
+    if (t->max_chunk > LUMRAD_MAX_CHUNK) return fail(LUMRAD_EINVAL, "max_chunk above LUMRAD_MAX_CHUNK");
     b->tuning.guided_div = t->guided_div;
     b->tuning.max_chunk = t->max_chunk;
     b->tuning.march_ctas = t->march_ctas;

@@ -74,6 +74,7 @@ constexpr int kStageWarps = 32;
 // cap; the per-warp queue divides by kWarpQueueDiv
 constexpr int kQueueDiv = 2;
 constexpr int kQueueCap = 32;
+static_assert(LUMRAD_MAX_CHUNK < (1 << 12) && kQueueCap <= LUMRAD_MAX_CHUNK, "a chunk's count fits 12 bits");
 constexpr int kWarpQueueDiv = 1;
 // launches with fewer tasks than this per warp claim through the CTA queue (march_kernel's CTAQ)
 constexpr int kCtaQueueTasksPerWarp = 32;

@@ -68,6 +68,10 @@ def test_batch_and_server_reject_bad_requests():
             assert _code(b.set_requests, 0, req, lum_gb300.pass_params(size=0)) == N.LUMRAD_EINVAL
             assert _code(b.set_requests, 0, req, lum_gb300.pass_params(record_hits=True)) == N.LUMRAD_EINVAL
             assert _code(b.run, 0) == N.LUMRAD_ESTATE   # no requests set yet
+            # a claimed chunk's task count has 12 bits in the march queue's words
+            assert _code(b.set_tuning, 2, 4096, 0) == N.LUMRAD_EINVAL
+            assert _code(b.set_tuning, 2, -1, 0) == N.LUMRAD_EINVAL
+            b.set_tuning(2, 4095, 0)
             assert _code(b.stats) == N.LUMRAD_ESTATE
         with lum_gb300.RadianceServer() as srv:
             i = srv.add_world(rw)
