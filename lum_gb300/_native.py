@@ -22,6 +22,7 @@ LUMRAD_ESTATE = -5
 LUMRAD_ECANCELED = -6
 LUMRAD_TEST_LEAN_FINALIZE = 1
 LUMRAD_TEST_PASS_MS = 2
+LUMRAD_MAX_CHUNK = 4095   # include/lumrad.h: the largest LumRadTuning.max_chunk
 
 PRECISION = {"fp32": 0, "fp16": 1, "bf16": 2, "rgb10a2": 3}
 

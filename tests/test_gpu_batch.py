@@ -69,6 +69,36 @@ def test_per_world_path_and_autotune_restore():
         rw.close()
 
 
+def test_batch_results_do_not_depend_on_tuning():
+    """The queue settings change only the schedule: single-task claims, the largest chunk the
+    queue words carry (LUMRAD_MAX_CHUNK), a divisor that forces one-task claims and one CTA per SM
+    all give the default's volumes bit for bit (small batches claim through the CTA queue, a
+    batch with more tasks than 32 per warp through the per-warp queue)."""
+    import lum_gb300
+    from lum_gb300 import _native as N
+    big = [(worldgen.terrain_world((56, 48, 8), seed=23, n_types=32), worldgen.all_probes((56, 48, 8)), 256),
+           (worldgen.terrain_world((24, 20, 8), seed=24, n_types=32),
+            worldgen.probe_subset((24, 20, 8), 0.5, seed=24, stream=0), 128)]   # 179,712 tasks
+    for mix in (worldgen.mixed_worlds(n=6, seed=21, max_dims=(10, 10, 6)), big):
+        results = {}
+        for tuning in (None, (1, 1, 0), (2, N.LUMRAD_MAX_CHUNK, 0), (1000, 32, 0), (2, 32, 1)):
+            rws = _make(mix)
+            with lum_gb300.RadianceBatch(rws) as b:
+                for i, (w, req, r) in enumerate(mix):
+                    b.set_requests(i, req, lum_gb300.pass_params(rays=r, max_dist=128.0, blend=0.1))
+                if tuning is not None:
+                    b.set_tuning(*tuning)
+                for seed in (5, 6):
+                    b.run(seed)
+                b.synchronize()
+                results[tuning] = [rw.get_radiance() for rw in rws]
+            for rw in rws:
+                rw.close()
+        for tuning, got in results.items():
+            for i in range(len(mix)):
+                assert np.array_equal(got[i], results[None][i]), (tuning, i)
+
+
 def test_batch_in_the_mix_equals_alone():
     """A world's result is identical whether it runs alone or in a batch with others."""
     import lum_gb300
