@@ -61,14 +61,14 @@ BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches, whose extra CTAs copy each pass's unlisted probes) in ncu captures of this
 # workload (the march's launch, and 3 of the 8 finalize launches scaled to 8); ncu replays with cold
-# caches (march 1.83 + 47.05 MB, finalizes 120.42 + 0.00 MB)
-NCU_DRAM_BYTES_PER_STEP = 169.30e6
+# caches (march 1.83 + 47.05 MB, finalizes 120.41 + 0.00 MB)
+NCU_DRAM_BYTES_PER_STEP = 169.29e6
 # L2 bytes (lts__t_bytes.sum) of the same launches in the same captures (march 454.6 MB: its world
-# lookups are shared-memory loads, finalizes 845.9 MB)
-NCU_L2_BYTES_PER_STEP = 1300.5e6
+# lookups are shared-memory loads, finalizes 934.9 MB, of which their register spills' share)
+NCU_L2_BYTES_PER_STEP = 1389.5e6
 # Warp instructions (smsp__inst_executed.sum) of the same launches: the march over the 8 passes
-# (462.6 M) and the 8 finalize launches (404.1 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 462.6e6 + 404.1e6
+# (462.6 M) and the 8 finalize launches (370.9 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 462.6e6 + 370.9e6
 SCHEDULERS_PER_SM = 4
 
 
