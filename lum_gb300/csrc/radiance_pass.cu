@@ -495,14 +495,16 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
 
 // ---------------------------------------------------------------- finalize kernel
 // IN_CTA: every probe of the launch combines inside one CTA (R/32 divides kFinWarps); the kernel
-// then has no global-memory combine, which costs the general kernel 8 registers and spills, and
-// runs 6 CTAs per SM (40 registers): the kernel is latency-bound; against four CTAs, five measured
-// 4-6% faster and six 1% faster again (seven: slower on single passes).
+// then has no global-memory combine, which costs the general kernel 8 registers and spills.  The
+// kernel is latency-bound, so occupancy pays: the table form (IN_CTA, a world per CTA) runs 6 CTAs
+// per SM at 40 registers (against four CTAs, five measured 4-6% faster and six 1% faster again).
 // One 8-task group (one CTA's work) of the finalize kernel.  SINGLE: the launch covers one world
 // (a single pass, or one pass of a several-pass call), read from the kernel's parameters, whose
 // fields are operands from the constant bank; else the world table's entry for the group through
-// a generic pointer, whose fields the compiler keeps in registers: the lean kernel's 24 B of spills
-// went with SINGLE (0 B at 37-40 registers), the 8-pass step 5.6% faster, a single pass 2.8%.
+// a generic pointer, whose fields the compiler keeps in registers.  SINGLE took the lean kernel
+// from 40 registers and 24 B of spills to 40 registers and none (the 8-pass step 5.6% faster, a
+// single pass 2.8%), and then fits 8 CTAs per SM at 32 registers with 32 B of spills: 1.9% faster
+// again on the 8-pass step, 0.9% on a single pass (launch 48.8 against 51.0 us).
 template <class Store, bool RECORD, bool IN_CTA, bool SINGLE>
 __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, float4* s_mean, int* s_count,
                                                unsigned (*s_stat)[2]) {
@@ -597,7 +599,7 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
 // PERSIST (launches sized on the device): a fixed grid walks the 8-task groups of the device's
 // task count; otherwise one CTA per group.
 template <class Store, bool RECORD, bool IN_CTA, bool PERSIST = false, bool SINGLE = false>
-__global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? 6 : 4)
+__global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? (SINGLE ? 8 : 6) : 4)
 finalize_kernel(const __grid_constant__ LaunchArgs la) {
     grid_launch_dependents();   // the next pass's launch may start its volume-free part
     if (la.pass_mask && (int)blockIdx.x >= la.fin_ctas) {   // copy role (see LaunchArgs)
