@@ -61,14 +61,15 @@ BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches, whose extra CTAs copy each pass's unlisted probes) in ncu captures of this
 # workload (the march's launch, and 3 of the 8 finalize launches scaled to 8); ncu replays with cold
-# caches (march 1.83 + 47.05 MB, finalizes 120.41 + 0.00 MB)
-NCU_DRAM_BYTES_PER_STEP = 169.29e6
-# L2 bytes (lts__t_bytes.sum) of the same launches in the same captures (march 454.6 MB: its world
-# lookups are shared-memory loads, finalizes 934.9 MB, of which their register spills' share)
-NCU_L2_BYTES_PER_STEP = 1389.5e6
+# caches (march 1.07 + 376.30 MB: most of the step's 430 MB of 32-byte ray results leave the L2
+# before their finalize launches; finalizes 442.51 + 0.66 MB)
+NCU_DRAM_BYTES_PER_STEP = 820.54e6
+# L2 bytes (lts__t_bytes.sum) of the same launches in the same captures (march 824.3 MB: its world
+# lookups are shared-memory loads, finalizes 1255.6 MB)
+NCU_L2_BYTES_PER_STEP = 2079.9e6
 # Warp instructions (smsp__inst_executed.sum) of the same launches: the march over the 8 passes
-# (462.6 M) and the 8 finalize launches (370.9 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 462.6e6 + 370.9e6
+# (480.7 M) and the 8 finalize launches (308.0 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 480.7e6 + 308.0e6
 SCHEDULERS_PER_SM = 4
 
 
