@@ -43,7 +43,7 @@ struct Batch {
     long long n_tasks = 0;
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
-    uint2* d_ray_res = nullptr;
+    RayResult* d_ray_res = nullptr;
     size_t ray_cap = 0;
     Tuning tuning;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
@@ -95,7 +95,7 @@ int build(Batch* b) {
         cudaFree(b->d_ray_res);
         b->d_ray_res = nullptr;
         b->ray_cap = 0;
-        LUMRAD_TRY(cudaMalloc(&b->d_ray_res, need * sizeof(uint2)));
+        LUMRAD_TRY(cudaMalloc(&b->d_ray_res, need * sizeof(RayResult)));
         b->ray_cap = need;
     }
     b->release_graphs();

@@ -376,8 +376,8 @@ int Context::ensure_rays(long long n_tasks, long long cap_tasks) {
     d_ray_blk = nullptr;
     ray_cap = 0;
     pass_mark = -1;   // the buffers are new: no launch overlaps the synchronised one
-    LUMRAD_TRY(cudaMalloc(&d_ray_res, need * sizeof(uint2)));
-    LUMRAD_TRY(cudaMalloc(&d_ray_res2, need * sizeof(uint2)));
+    LUMRAD_TRY(cudaMalloc(&d_ray_res, need * sizeof(RayResult)));
+    LUMRAD_TRY(cudaMalloc(&d_ray_res2, need * sizeof(RayResult)));
     LUMRAD_TRY(cudaMalloc(&d_ray_blk, need * sizeof(int)));
     ray_cap = need;
     return LUMRAD_OK;

@@ -15,20 +15,33 @@ static_assert(kWarps % kFinWarps == 0, "finalize CTAs must not straddle worlds")
 // A task is one 32-ray subgroup of one probe (the unit radiance.comp sums with subgroupAdd).
 constexpr int kTaskRays = 32;
 // Tasks per march/finalize round: the per-ray buffer between the two kernels holds this many
-// tasks' rays (8 B per ray: 67 MB, L2-resident on GB300).  Fewer, larger rounds shorten the
-// march kernel's tails (measured: 2^18 tasks 13% faster than 2^16 on many small worlds).
+// tasks' rays (32 B per ray: 268 MB).  Fewer, larger rounds shorten the march kernel's tails
+// (measured: 2^18 tasks 13% faster than 2^16 on many small worlds).
 constexpr int kChunkTasks = 1 << 18;
 // Words of a launch's task queue: [0] next march task, [1] march warps finished; zero between
 // launches (the march's last warp resets them)
 constexpr int kQueueWords = 2;
-// Round size of batches: their task spaces are large, and two rounds of 2^20 tasks (402 MB of ray
-// results, past the L2) beat seven of 2^18 by 2% on 256 mixed worlds (fewer queue drains)
+// Round size of batches: their task spaces are large, and two rounds of 2^20 tasks beat seven of
+// 2^18 by 2% on 256 mixed worlds (fewer queue drains; measured with 8-byte ray results)
 constexpr int kBatchRoundTasks = 1 << 20;
 // Passes of one march launch over several passes of a context (bits of a pass-mask word)
 constexpr int kMultiPasses = 32;
-// Tasks of one march launch over several passes of a context (their rays, 8 B each, are kept
-// until the passes' finalize launches: 2^19 tasks = 134 MB, about the L2)
+// Tasks of one march launch over several passes of a context (their rays, 32 B each, are kept
+// until the passes' finalize launches: 2^19 tasks = 537 MB)
 constexpr int kMultiTasks = 1 << 19;
+
+// A marched ray as the march leaves it for the finalize (32 B, two 16-byte words): the coarse
+// fraction's bits and the info word (bits 0-15 coarse steps, 16-23 coarse voxel (records only),
+// 24 hit, 25 stopped by the step bound), then the ray's origin and direction as the march set them
+// up.  The finalize reads the ray back instead of setting it up again: against 8-byte results and
+// a second set-up, the march +2.8% (four times the bytes stored) and each finalize -8.5%; the
+// 8-pass step -3.0%, a single pass -2.4%, a batch -1.9% (bit-identical).
+struct __align__(16) RayResult {
+    uint32_t frac, info;
+    float ox, oy;
+    float oz, dx, dy, dz;
+};
+static_assert(sizeof(RayResult) == 32, "two 16-byte words");
 
 // One world's pass as the kernels see it (all pointers are device pointers).
 //
@@ -77,7 +90,7 @@ struct LaunchArgs {
     long long n_tasks;           // tasks of all worlds
     unsigned long long* queue;   // kQueueWords words (see kQueueWords); zero between launches
     int* error;                  // set non-zero if a warp's scheduler stops making progress
-    uint2* ray_res;              // per ray of the round: coarse fraction bits, info word
+    RayResult* ray_res;          // per ray of the round
     int* ray_blk;                // per ray of the round: block id at the last coarse step (records)
     int ray_origin;              // task whose rays start ray_res (the march launch's chunk_begin)
     int round_tasks;             // tasks per march/finalize round (0: kChunkTasks); ray_res holds one round

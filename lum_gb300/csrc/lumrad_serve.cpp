@@ -143,7 +143,7 @@ struct Slot {
     unsigned long long* d_queue = nullptr;
     int* d_error = nullptr;
     int* h_error = nullptr;       // pinned
-    uint2* d_ray_res = nullptr;
+    RayResult* d_ray_res = nullptr;
     bool busy = false;
     std::vector<SRequest> reqs;
     std::vector<int> probes;
@@ -547,7 +547,7 @@ struct DevLane {
     long long chunk_cap = 0, chunks_total = 0;
     int* d_error = nullptr;
     unsigned long long* d_queue = nullptr;
-    uint2* d_ray_res = nullptr;
+    RayResult* d_ray_res = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_end = nullptr;
     cudaGraph_t graph = nullptr;
@@ -588,7 +588,7 @@ int devloop_lane_create(Server* sv, DevLoopHost& dl, DevLane& ln) {
     LUMRAD_TRY(cudaMalloc(&ln.d_loop, sizeof(DevLoop)));
     LUMRAD_TRY(cudaMalloc(&ln.d_error, sizeof(int)));
     LUMRAD_TRY(cudaMalloc(&ln.d_queue, kQueueWords * sizeof(unsigned long long)));
-    LUMRAD_TRY(cudaMalloc(&ln.d_ray_res, (size_t)dl.max_tasks * kTaskRays * sizeof(uint2)));
+    LUMRAD_TRY(cudaMalloc(&ln.d_ray_res, (size_t)dl.max_tasks * kTaskRays * sizeof(RayResult)));
     LUMRAD_TRY(cudaMemsetAsync(ln.d_error, 0, sizeof(int), ln.stream));
     LUMRAD_TRY(cudaMemsetAsync(ln.d_queue, 0, kQueueWords * sizeof(unsigned long long), ln.stream));
     std::unique_ptr<DevLoop> h(new DevLoop());
@@ -647,7 +647,7 @@ int devloop_lane_create(Server* sv, DevLoopHost& dl, DevLane& ln) {
     LUMRAD_TRY(ce);
     LUMRAD_TRY(ee);
     LUMRAD_TRY(cudaGraphInstantiate(&ln.exec, ln.graph, 0));
-    sv->fixed += (size_t)dl.max_tasks * kTaskRays * sizeof(uint2) + sizeof(DevLoop);
+    sv->fixed += (size_t)dl.max_tasks * kTaskRays * sizeof(RayResult) + sizeof(DevLoop);
     return LUMRAD_OK;
 }
 
@@ -982,7 +982,7 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
             *sl.h_error = 0;
             LUMRAD_TRY(cudaMemsetAsync(sl.d_queue, 0, kQueueWords * sizeof(unsigned long long), sl.stream));
             LUMRAD_TRY(cudaMemsetAsync(sl.d_error, 0, sizeof(int), sl.stream));
-            LUMRAD_TRY(cudaMalloc(&sl.d_ray_res, rays * sizeof(uint2)));
+            LUMRAD_TRY(cudaMalloc(&sl.d_ray_res, rays * sizeof(RayResult)));
             // request packs sized up front so the serving loop rarely grows them
             const size_t pack = (size_t)16 << 20;
             LUMRAD_TRY(cudaMallocHost(&sl.h_pack, pack));
@@ -990,7 +990,7 @@ int lumrad_server_create(const LumRadServerSettings* s, LumRadServer* out) {
             LUMRAD_TRY(cudaMallocAsync(reinterpret_cast<void**>(&sl.d_pack), pack, sl.stream));
             sl.d_cap = pack;
             LUMRAD_TRY(cudaStreamSynchronize(sl.stream));
-            sv->fixed += rays * sizeof(uint2) + pack + 2 * sizeof(unsigned long long) + sizeof(int);
+            sv->fixed += rays * sizeof(RayResult) + pack + 2 * sizeof(unsigned long long) + sizeof(int);
         }
         if (sv->fixed > sv->budget()) return fail(LUMRAD_ENOMEM, "the launch buffers alone exceed the HBM budget");
         return LUMRAD_OK;

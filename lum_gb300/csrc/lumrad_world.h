@@ -145,8 +145,8 @@ struct Context {
     int* d_error = nullptr;
     // rays of one march/finalize round (up to kChunkTasks * 32 rays), or of one march launch over
     // several passes (up to kMultiTasks * 32)
-    uint2* d_ray_res = nullptr;
-    uint2* d_ray_res2 = nullptr;           // the other ray buffer (consecutive passes alternate)
+    RayResult* d_ray_res = nullptr;
+    RayResult* d_ray_res2 = nullptr;           // the other ray buffer (consecutive passes alternate)
     int* d_ray_blk = nullptr;
     size_t ray_cap = 0;
     int ray_side = 0;

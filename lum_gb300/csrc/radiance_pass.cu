@@ -8,14 +8,14 @@
 //                    launch has few tasks per warp).  A warp sets up a task's 32 rays in lock step
 //                    (hash seeds, direction, origin, 1/direction) into a 32-ray ring in shared
 //                    memory.  Its lanes march in a flat loop, two coarse steps per iteration; a
-//                    lane whose ray ends writes (fraction, info) and takes the next ray in ring
-//                    order.  The ring is set up again as soon as its rays are handed out, so lanes
+//                    lane whose ray ends writes its RayResult (fraction, info, origin, direction)
+//                    and takes the next ray in ring order.  The ring is set up again as soon as its rays are handed out, so lanes
 //                    never wait for each other.
 //   finalize_kernel  one warp per task, eight consecutive tasks per CTA, in lock step: the ray
-//                    set up again (cheaper than a round trip through L2), refine DDA, material,
-//                    trilinear fetch of the previous radiance, shading, xor-butterfly sum.  When
-//                    R/32 divides 8 a probe's subgroups share a CTA and their means are summed in
-//                    order from shared memory (a lean instantiation, 6 CTAs per SM, when every
+//                    read back, refine DDA, material, trilinear fetch of the previous radiance,
+//                    shading, xor-butterfly sum.  When R/32 divides 8 a probe's subgroups share a
+//                    CTA and their means are summed in order from shared memory (a lean
+//                    instantiation, 8 CTAs per SM over one world, 6 over a world table, when every
 //                    probe of the launch does); otherwise through global scratch and a per-probe
 //                    counter.  Lookup and hit counters are summed per CTA.
 //
@@ -28,9 +28,9 @@
 //
 // Exactness: see radiance_device.cuh.  Memory: both kernels test voxels through the compact
 // world (uint8 ids + occupancy bits, L1-resident; staged in shared memory by the march of a launch
-// over one world that fits); between the kernels each ray keeps 8 B
-// (coarse fraction, info word): 67 MB for a single pass's round of 2^18 tasks (L2-resident),
-// up to 134 MB for several passes, 268 MB for a batch's round of 2^20.
+// over one world that fits); between the kernels each ray keeps its 32 B RayResult: 268 MB for a
+// single pass's round of 2^18 tasks, up to 537 MB for several passes, 1.07 GB for a batch's round
+// of 2^20.
 
 #include "radiance_device.cuh"
 #include "lumrad_devloop.h"
@@ -369,7 +369,10 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                         if (solid) info |= (uint32_t)v << 16;
                         la.ray_blk[my] = blk;
                     }
-                    __stcg(la.ray_res + my, make_uint2(__float_as_uint(f2), info));
+                    uint4* rr = reinterpret_cast<uint4*>(la.ray_res + my);   // RayResult
+                    __stcg(rr, make_uint4(__float_as_uint(f2), info, __float_as_uint(ox), __float_as_uint(oy)));
+                    __stcg(rr + 1, make_uint4(__float_as_uint(oz), __float_as_uint(dx), __float_as_uint(dy),
+                                              __float_as_uint(dz)));
                     my = -1;
                     fin = true;
                 }
@@ -531,10 +534,12 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
     float3 v = make_float3(0.0f, 0.0f, 0.0f);
     if (valid) {
         const long long idx = (long long)(t - la.ray_origin) * kTaskRays + lane;
-        const uint2 res = __ldcg(la.ray_res + idx);
+        const uint4* rr = reinterpret_cast<const uint4*>(la.ray_res + idx);   // RayResult
+        const uint4 r0 = __ldcg(rr), r1 = __ldcg(rr + 1);
+        const uint2 res = make_uint2(r0.x, r0.y);
         const int blk = RECORD ? __ldcg(la.ray_blk + idx) : 0;
-        float3 o, d;
-        setup_ray(*wp, g, k * kTaskRays + lane, o, d);   // bit-identical to the march's set-up
+        const float3 o = make_float3(__uint_as_float(r0.z), __uint_as_float(r0.w), __uint_as_float(r1.x));
+        const float3 d = make_float3(__uint_as_float(r1.y), __uint_as_float(r1.z), __uint_as_float(r1.w));
         uint32_t lookups;
         float3 L, u;
         float4 m;
@@ -945,13 +950,13 @@ constexpr size_t kNaCgrid = 0;                                                  
 constexpr size_t kNaCbits = align256(kNaCgrid + 2 * (size_t)kNoAllocMaxBlocks);      // 512 B per compact id
 constexpr size_t kNaRayRes = align256(kNaCbits + (size_t)(LUMRAD_MAX_BLOCK_SLOTS + 2) * 512);
 // the direction tables for R = 32, 64, 128, 256 back to back (480 entries), uploaded once per device
-constexpr size_t kNaDirs = align256(kNaRayRes + (size_t)kNoAllocRoundTasks * kTaskRays * sizeof(uint2));
+constexpr size_t kNaDirs = align256(kNaRayRes + (size_t)kNoAllocRoundTasks * kTaskRays * sizeof(RayResult));
 constexpr int kNaDirEntries = 32 + 64 + 128 + 256;
 constexpr size_t kNaQueue = align256(kNaDirs + kNaDirEntries * sizeof(float4));
 constexpr size_t kNaError = kNaQueue + kQueueWords * sizeof(unsigned long long);
 constexpr size_t kNaStats = align256(kNaError + sizeof(int));
 constexpr size_t kNaBytes = align256(kNaStats + 2 * sizeof(unsigned long long));
-static_assert(kNaBytes <= (5u << 20), "no-allocation scratch must stay under 5 MiB");
+static_assert(kNaBytes <= (8u << 20), "no-allocation scratch must stay under 8 MiB");
 
 }  // namespace
 }  // namespace lumrad
@@ -1123,7 +1128,7 @@ extern "C" int lumrad_radiance_pass_noalloc(const int* world_size, const int16_t
     la.n_tasks = n_tasks;
     la.queue = queue;
     la.error = error;
-    la.ray_res = reinterpret_cast<uint2*>(base + kNaRayRes);
+    la.ray_res = reinterpret_cast<RayResult*>(base + kNaRayRes);
     const int blocks = march_grid(false, nd->num_sms, std::min<long long>(n_tasks, kNoAllocRoundTasks));
     la.total_warps = blocks * kWarps;
     for (long long c0 = 0; c0 < n_tasks; c0 += kNoAllocRoundTasks) {
