@@ -418,7 +418,7 @@ int  lumrad_dirty_probes(const int* world_size, const LumRadEdit* edits, int n_e
  * they run: engines that reserve their whole device-memory budget up front and forbid later
  * allocations (an allocation can synchronise the device mid-frame), or hosts whose allocator
  * owns the device heap.  The call allocates nothing; the caller passes device pointers to the
- * inputs and the output, and every working buffer lives in one fixed array (about 4 MiB)
+ * inputs and the output, and every working buffer lives in one fixed array (about 7 MiB)
  * compiled into this library, which each GPU that loads the library keeps until exit.
  *   world_size  blocks per axis; X*Y*Z <= LUMRAD_NOALLOC_MAX_BLOCKS, else LUMRAD_EINVAL
  *   d_grid      X*Y*Z int16 block ids (x-fastest)
