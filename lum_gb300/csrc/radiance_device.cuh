@@ -19,6 +19,11 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+// c + a*b rounded once, for a product a*b that is exact in FP32 (a power-of-two scale of a value
+// that stays normal, or a product by 0 or 1): then fadd(c, fmul(a, b)) rounds only the sum, the
+// same value (a zero product takes the sign rules of the addition either way), in one instruction
+// instead of two.
+__device__ __forceinline__ float fadd_exact_mul(float c, float a, float b) { return __fmaf_rn(a, b, c); }
 // x / d where `inv` is 1/d if that is exact (d a power of two), else 0
 __device__ __forceinline__ float fdiv_by(float x, float d, float inv) { return inv != 0.0f ? fmul(x, inv) : fdiv(x, d); }
 // GLSL min/max definitions: identical NaN and signed-zero behaviour everywhere.
@@ -229,18 +234,20 @@ __device__ __forceinline__ void setup_ray(const WorldPass& w, int g, int r, floa
     const short4 q = __ldg(w.req + ((long long)g * w.size + w.shift));
     uint32_t sx = (uint32_t)g * (uint32_t)w.R + (uint32_t)r + w.seed;
     const uint32_t sy = w.seed, sz = w.seed;
-    const float3 c = make_float3(fadd(fmul((float)q.x, 16.0f), 8.0f), fadd(fmul((float)q.y, 16.0f), 8.0f),
-                                 fadd(fmul((float)q.z, 16.0f), 8.0f));
+    // block centre q*16 + 8 (q an int16: the product is exact)
+    const float3 c = make_float3(fadd_exact_mul(8.0f, (float)q.x, 16.0f), fadd_exact_mul(8.0f, (float)q.y, 16.0f),
+                                 fadd_exact_mul(8.0f, (float)q.z, 16.0f));
     const float4 f = __ldg(w.dirs + r);
     const float3 r1 = hash33(sx, sy, sz);
     sx++;
-    const float3 j = make_float3(fmul(0.1f, fmul(fsub(r1.x, 0.5f), 2.0f)), fmul(0.1f, fmul(fsub(r1.y, 0.5f), 2.0f)),
-                                 fmul(0.1f, fmul(fsub(r1.z, 0.5f), 2.0f)));
+    // 0.1*((r - 0.5)*2) as 0.2*(r - 0.5): the doubling is exact (|r - 0.5| >= 2^-32 or 0) and the
+    // float 0.2f is exactly twice the float 0.1f, so both round the same real product
+    const float3 j = make_float3(fmul(0.2f, fsub(r1.x, 0.5f)), fmul(0.2f, fsub(r1.y, 0.5f)), fmul(0.2f, fsub(r1.z, 0.5f)));
     d = normalize3(make_float3(fadd(f.x, j.x), fadd(f.y, j.y), fadd(f.z, j.z)));
     o = make_float3(fadd(c.x, fmul(d.x, 6.0f)), fadd(c.y, fmul(d.y, 6.0f)), fadd(c.z, fmul(d.z, 6.0f)));
     const float3 r2 = hash33(sx, sy, sz);
-    o = make_float3(fadd(o.x, fmul(fsub(r2.x, 0.5f), 2.0f)), fadd(o.y, fmul(fsub(r2.y, 0.5f), 2.0f)),
-                    fadd(o.z, fmul(fsub(r2.z, 0.5f), 2.0f)));
+    o = make_float3(fadd_exact_mul(o.x, fsub(r2.x, 0.5f), 2.0f), fadd_exact_mul(o.y, fsub(r2.y, 0.5f), 2.0f),
+                    fadd_exact_mul(o.z, fsub(r2.z, 0.5f), 2.0f));
     if (r & 1) d = make_float3(-d.x, -d.y, -d.z);
 }
 
@@ -328,9 +335,9 @@ __device__ __forceinline__ bool finalize_ray(const WorldPass& w, const MarchView
             const bool bz = (tmz <= tmx) && (tmz <= tmy);
             fsx = bx ? 1.0f : 0.0f; fsy = by ? 1.0f : 0.0f; fsz = bz ? 1.0f : 0.0f;
             vx += bx ? stx : 0; vy += by ? sty : 0; vz += bz ? stz : 0;
-            tmx = fadd(tmx, fmul(tdx, fsx));
-            tmy = fadd(tmy, fmul(tdy, fsy));
-            tmz = fadd(tmz, fmul(tdz, fsz));
+            tmx = fadd_exact_mul(tmx, tdx, fsx);   // fs is 0 or 1 (inf * 0 is NaN either way)
+            tmy = fadd_exact_mul(tmy, tdy, fsy);
+            tmz = fadd_exact_mul(tmz, tdz, fsz);
             solid = solid_at_w<WIDE>(mv, vx, vy, vz, cid);
             it++;
         }
@@ -348,15 +355,15 @@ __device__ __forceinline__ bool finalize_ray(const WorldPass& w, const MarchView
             }
         }
         const float nx = -fmul((float)stx, fsx), ny = -fmul((float)sty, fsy), nz = -fmul((float)stz, fsz);
-        const float fr = fadd(fadd(fmul(fsub(tmx, tdx), fsx), fmul(fsub(tmy, tdy), fsy)), fmul(fsub(tmz, tdz), fsz));
+        const float fr = fadd_exact_mul(fadd_exact_mul(fmul(fsub(tmx, tdx), fsx), fsub(tmy, tdy), fsy), fsub(tmz, tdz), fsz);
         // material (GetMat :145-157) and sample_radiance (:161-166); /16 == *0.0625 exactly
         m = __ldg(w.mats + cur);
         const float hx = fadd(o.x, fmul(fr, d.x));
         const float hy = fadd(o.y, fmul(fr, d.y));
         const float hz = fadd(o.z, fmul(fr, d.z));
-        const float bpx = fmul(fadd(hx, fmul(nx, 16.0f)), 0.0625f);
-        const float bpy = fmul(fadd(hy, fmul(ny, 16.0f)), 0.0625f);
-        const float bpz = fmul(fadd(hz, fmul(nz, 16.0f)), 0.0625f);
+        const float bpx = fmul(fadd_exact_mul(hx, nx, 16.0f), 0.0625f);   // n is 0 or +-1
+        const float bpy = fmul(fadd_exact_mul(hy, ny, 16.0f), 0.0625f);
+        const float bpz = fmul(fadd_exact_mul(hz, nz, 16.0f), 0.0625f);
         u = make_float3(fdiv_by(fadd(bpx, 0.5f), (float)w.X, w.inv_dim[0]), fdiv_by(fadd(bpy, 0.5f), (float)w.Y, w.inv_dim[1]),
                         fdiv_by(fadd(bpz, 0.5f), (float)w.Z, w.inv_dim[2]));
         if (RECORD) {

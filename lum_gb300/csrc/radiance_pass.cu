@@ -343,9 +343,10 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                 const bool solid =
                     FAST ? solid_at_tbp<WIDE, STAGE>(cgp, rowp, mv.X, mv.Y, mv.Z, tbx, tby, tbz, ix, iy, iz, cid)
                          : solid_at_p<WIDE, STAGE>(cgp, rowp, mv.X, mv.Y, mv.Z, ix, iy, iz, cid);
-                const float bx = fadd(fmul(tbx, 16.0f), cx);
-                const float by = fadd(fmul(tby, 16.0f), cy);
-                const float bz = fadd(fmul(tbz, 16.0f), cz);
+                // tb*16 is exact (tb = trunc(p/16), an integer of at most |p|/16)
+                const float bx = fadd_exact_mul(cx, tbx, 16.0f);
+                const float by = fadd_exact_mul(cy, tby, 16.0f);
+                const float bz = fadd_exact_mul(cz, tbz, 16.0f);
                 const float tx = fadd(fmul(bx, ivx), fmul(-px, ivx));
                 const float ty = fadd(fmul(by, ivy), fmul(-py, ivy));
                 const float tz = fadd(fmul(bz, ivz), fmul(-pz, ivz));
