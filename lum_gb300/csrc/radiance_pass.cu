@@ -500,8 +500,10 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
 // ---------------------------------------------------------------- finalize kernel
 // IN_CTA: every probe of the launch combines inside one CTA (R/32 divides kFinWarps); the kernel
 // then has no global-memory combine, which costs the general kernel 8 registers and spills.  The
-// kernel is latency-bound, so occupancy pays: the table form (IN_CTA, a world per CTA) runs 6 CTAs
-// per SM at 40 registers (against four CTAs, five measured 4-6% faster and six 1% faster again).
+// kernel waits on its lookup chain, so occupancy pays: the lean forms run 8 CTAs per SM at 32
+// registers (the world-table form: 52 B of spills, the 256-world batch 2.8% faster than at 6 CTAs
+// and 40 registers; at 4 CTAs it was slower again: five 4-6% faster, six 1% faster), the
+// device loop's persistent form 6 (its spills at 32 registers would be 208 B).
 // One 8-task group (one CTA's work) of the finalize kernel.  SINGLE: the launch covers one world
 // (a single pass, or one pass of a several-pass call), read from the kernel's parameters, whose
 // fields are operands from the constant bank; else the world table's entry for the group through
@@ -605,7 +607,7 @@ __device__ __forceinline__ void finalize_group(const LaunchArgs& la, int group, 
 // PERSIST (launches sized on the device): a fixed grid walks the 8-task groups of the device's
 // task count; otherwise one CTA per group.
 template <class Store, bool RECORD, bool IN_CTA, bool PERSIST = false, bool SINGLE = false>
-__global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? (SINGLE ? 8 : 6) : 4)
+__global__ void __launch_bounds__(kFinWarps * 32, IN_CTA ? (PERSIST ? 6 : 8) : 4)
 finalize_kernel(const __grid_constant__ LaunchArgs la) {
     grid_launch_dependents();   // the next pass's launch may start its volume-free part
     if (la.pass_mask && (int)blockIdx.x >= la.fin_ctas) {   // copy role (see LaunchArgs)
@@ -833,7 +835,7 @@ cudaError_t launch_table_pass(const LaunchArgs& a, int precision, int num_sms, c
     // mostly small (p50 5-8% lower at 2,000-10,000 requests/s than the per-warp queue; 2% less
     // throughput saturated, where the host loop is the faster one anyway)
     march_kernel<false, false, true><<<blocks, kWarps * 32, 0, stream>>>(args);
-    const int fin = num_sms * 6;   // the lean finalize's occupancy
+    const int fin = num_sms * 6;   // the persistent finalize's occupancy (6 CTAs per SM)
     switch (precision) {
         case LUMRAD_PRECISION_FP16: finalize_kernel<StoreF16, false, true, true><<<fin, kFinWarps * 32, 0, stream>>>(args); break;
         case LUMRAD_PRECISION_BF16: finalize_kernel<StoreBF16, false, true, true><<<fin, kFinWarps * 32, 0, stream>>>(args); break;
