@@ -15,7 +15,7 @@
 //                    read back, refine DDA, material, trilinear fetch of the previous radiance,
 //                    shading, xor-butterfly sum.  When R/32 divides 8 a probe's subgroups share a
 //                    CTA and their means are summed in order from shared memory (a lean
-//                    instantiation, 8 CTAs per SM over one world, 6 over a world table, when every
+//                    instantiation, 8 CTAs per SM, 6 in the device loop's persistent form, when every
 //                    probe of the launch does); otherwise through global scratch and a per-probe
 //                    counter.  Lookup and hit counters are summed per CTA.
 //
