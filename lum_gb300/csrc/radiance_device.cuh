@@ -171,15 +171,16 @@ __device__ __forceinline__ bool solid_at_w(const MarchView& m, int ix, int iy, i
 // (FP32, exact): trunc(p)/16 truncated is trunc(p/16), and -15 <= trunc(p) < 16*size holds exactly
 // when 0 <= trunc(p/16) < size (p in (-16, 0) gives -0, block 0 like OpSDiv).  The block index is
 // the float's integer through the bits of 1.5*2^23 + tb (an add; -0 becomes +0), and the range test
-// one unsigned compare per axis.
+// one unsigned compare per axis; `in` reports it (the grid's range: -16 < p < 16*size per axis).
 template <bool WIDE, bool SMEM>
 __device__ __forceinline__ bool solid_at_tbp(const uint8_t* cg, const uint16_t* rows, int X, int Y, int Z, float tbx,
-                                             float tby, float tbz, int ix, int iy, int iz, int& cid) {
+                                             float tby, float tbz, int ix, int iy, int iz, int& cid, bool& in) {
     const int bx = __float_as_int(fadd(tbx, 12582912.0f)) - 0x4B400000;
     const int by = __float_as_int(fadd(tby, 12582912.0f)) - 0x4B400000;
     const int bz = __float_as_int(fadd(tbz, 12582912.0f)) - 0x4B400000;
     int c = 0;
-    if ((unsigned)bx < (unsigned)X && (unsigned)by < (unsigned)Y && (unsigned)bz < (unsigned)Z) {
+    in = (unsigned)bx < (unsigned)X && (unsigned)by < (unsigned)Y && (unsigned)bz < (unsigned)Z;
+    if (in) {
         const int idx = bx + X * (by + Y * bz);
         if (SMEM) c = WIDE ? (int)reinterpret_cast<const uint16_t*>(cg)[idx] : (int)cg[idx];
         else c = WIDE ? (int)__ldg(reinterpret_cast<const uint16_t*>(cg) + idx) : (int)__ldg(cg + idx);

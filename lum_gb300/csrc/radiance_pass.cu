@@ -48,9 +48,9 @@ namespace {
 // per step.  Hence, for it:
 //   (a) GLSL's min/max (y < x ? y : x) equal the hardware's min/max: they differ only on NaN and
 //       on the sign of a zero, and the skip's 0.01 floor maps both zeros alike;
-//   (b) a position lies outside [0, 16*size) exactly when its bits, read as unsigned, are at
-//       least those of 16*size (no position is -0: no origin is, and a sum is -0 only if both
-//       terms are);
+//   (b) a position lies outside [0, 16*size) exactly when it lies outside the grid lookup's
+//       range (-16, 16*size) or is negative (no position is -0: no origin is, and a sum is -0
+//       only if both terms are), so the exit test is the lookup's range test and the sign bits;
 //   (c) the 2*max_dist+2 step bound is never reached: the fraction passes max_dist first;
 //   (d) the grid lookup can take the block index and the range test from trunc(p/16) in FP32
 //       (solid_at_tbp), which the empty-block skip needs anyway.
@@ -319,7 +319,6 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
         constexpr bool WIDE = decltype(wide_tag)::value;
         const uint8_t* cgp = STAGE ? s_cg : mv.cgrid;
         const uint16_t* rowp = STAGE ? s_rows : reinterpret_cast<const uint16_t*>(mv.cbits);
-        const uint32_t uwx = __float_as_uint(wx), uwy = __float_as_uint(wy), uwz = __float_as_uint(wz);
         while (true) {
             bool fin = false;
 #pragma unroll
@@ -340,8 +339,9 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                 const int ix = f2i(px), iy = f2i(py), iz = f2i(pz);
                 const float tbx = truncf(fmul(px, 0.0625f)), tby = truncf(fmul(py, 0.0625f)), tbz = truncf(fmul(pz, 0.0625f));
                 int cid;
+                bool in_range = true;
                 const bool solid =
-                    FAST ? solid_at_tbp<WIDE, STAGE>(cgp, rowp, mv.X, mv.Y, mv.Z, tbx, tby, tbz, ix, iy, iz, cid)
+                    FAST ? solid_at_tbp<WIDE, STAGE>(cgp, rowp, mv.X, mv.Y, mv.Z, tbx, tby, tbz, ix, iy, iz, cid, in_range)
                          : solid_at_p<WIDE, STAGE>(cgp, rowp, mv.X, mv.Y, mv.Z, ix, iy, iz, cid);
                 // tb*16 is exact (tb = trunc(p/16), an integer of at most |p|/16)
                 const float bx = fadd_exact_mul(cx, tbx, 16.0f);
@@ -353,8 +353,11 @@ march_kernel(const __grid_constant__ LaunchArgs la) {
                 const float sk = FAST ? fmaxf(fminf(tx, fminf(ty, tz)), 0.01f) : gmax(gmin(tx, gmin(ty, tz)), 0.01f);
                 const float f2 = cid == 0 ? fadd(f1, sk) : f1;
                 bool out;
+                // a regular ray's position is outside [0, 16*size) on an axis exactly when it is
+                // outside the lookup's range (-16, 16*size) or negative (no position is -0): one
+                // test of the three sign bits beside the lookup's own range test
                 if (FAST)
-                    out = __float_as_uint(px) >= uwx || __float_as_uint(py) >= uwy || __float_as_uint(pz) >= uwz ||
+                    out = !in_range || (int)(__float_as_uint(px) | __float_as_uint(py) | __float_as_uint(pz)) < 0 ||
                           f2 >= max_dist;
                 else
                     out = px < 0.0f || py < 0.0f || pz < 0.0f || px >= wx || py >= wy || pz >= wz || f2 >= max_dist;
