@@ -61,15 +61,15 @@ BATCH_ROUND_TASKS = 1 << 20   # 32-ray tasks per march/finalize round of a batch
 # DRAM bytes (read + write) of one step's kernels (the march launch over 8 passes and the 8
 # finalize launches, whose extra CTAs copy each pass's unlisted probes) in ncu captures of this
 # workload (the march's launch, and 3 of the 8 finalize launches scaled to 8); ncu replays with cold
-# caches (march 1.11 + 376.25 MB: most of the step's 430 MB of 32-byte ray results leave the L2
+# caches (march 1.09 + 376.37 MB: most of the step's 430 MB of 32-byte ray results leave the L2
 # before their finalize launches; finalizes 442.51 + 0.77 MB)
-NCU_DRAM_BYTES_PER_STEP = 820.64e6
-# L2 bytes (lts__t_bytes.sum) of the same launches in the same captures (march 825.8 MB: its world
+NCU_DRAM_BYTES_PER_STEP = 820.74e6
+# L2 bytes (lts__t_bytes.sum) of the same launches in the same captures (march 825.5 MB: its world
 # lookups are shared-memory loads, finalizes 1255.3 MB)
-NCU_L2_BYTES_PER_STEP = 2081.1e6
+NCU_L2_BYTES_PER_STEP = 2080.8e6
 # Warp instructions (smsp__inst_executed.sum) of the same launches: the march over the 8 passes
-# (467.6 M) and the 8 finalize launches (302.8 M); deterministic up to the march queue's task order
-NCU_WARP_INST_PER_STEP = 467.6e6 + 302.8e6
+# (464.5 M) and the 8 finalize launches (302.8 M); deterministic up to the march queue's task order
+NCU_WARP_INST_PER_STEP = 464.5e6 + 302.8e6
 SCHEDULERS_PER_SM = 4
 
 
