@@ -28,6 +28,19 @@ def test_library_loads_and_exports_every_declared_symbol():
     assert set(names) <= set(_native._SIGS), "binding lacks a signature for a declared symbol"
 
 
+def test_binding_constants_match_header():
+    """Every LUMRAD_ status code, test hook and limit the binding copies equals the header's."""
+    src = open(os.path.join(ROOT, "include", "lumrad.h")).read()
+    defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(LUMRAD_\w+)\s+\(?(-?\d+)\)?", src)}
+    enums = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(LUMRAD_\w+)\s*=\s*(-?\d+)", src)}
+    header = {**enums, **defines}
+    copied = {k: v for k, v in vars(_native).items() if k.startswith("LUMRAD_") and isinstance(v, int)}
+    assert "LUMRAD_MAX_CHUNK" in copied and "LUMRAD_OK" in copied
+    for k, v in copied.items():
+        assert k in header, k
+        assert header[k] == v, (k, header[k], v)
+
+
 def test_struct_sizes_match_header():
     assert C.sizeof(_native.Settings) == 24
     assert C.sizeof(_native.Material) == 24
